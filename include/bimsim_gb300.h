@@ -1,0 +1,175 @@
+/*
+ * bimsim_gb300.h -- C ABI of the GB300 near-field-to-detector library.
+ *
+ * The reference (seberisha/bimsim-cuda) has no plugin or FFI interface: its
+ * boundary is the `bimsim` executable, whose flags fill the global
+ * `microscopeStruct* SCOPE` (arguments.h:564-593) and whose fileoutStruct
+ * writes the detector images (fileout.cu:47-159).  Internally the path is
+ *     microscopeStruct::init()      microscope.cu:537
+ *     microscopeStruct::Simulate()  microscope.cu:849
+ *     microscopeStruct::get*()      microscope.cu:722-814
+ *     scalarslice::toEnvi()         scalarslice.cu:146-166
+ * This header replaces that object with an opaque context and plain C entry
+ * points (pointers, sizes, status codes).  Every call returns a bs_status;
+ * the reference instead printed CUDA errors and carried on
+ * (rts/cuda/error.h:12-21) or called exit(1) (arguments.h:175,249,292).
+ *
+ * Units follow the reference: lengths in micrometres, wavelength in
+ * micrometres, numerical apertures as plain numbers.
+ */
+#ifndef BIMSIM_GB300_H
+#define BIMSIM_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum bs_status {
+    BS_OK = 0,
+    BS_ERR_ARG = 1,          /* invalid argument (reference: exit(1) in arguments.h) */
+    BS_ERR_CUDA = 2,         /* CUDA runtime error (reference: printed and ignored) */
+    BS_ERR_NOMEM = 3,        /* device allocation failed or over the HBM budget */
+    BS_ERR_STATE = 4,        /* call out of order (e.g. image before simulate) */
+    BS_ERR_IO = 5,           /* file could not be opened or written */
+    BS_ERR_TIMEOUT = 6,      /* a bounded wait ran out */
+    BS_ERR_UNSUPPORTED = 7,  /* feature not built */
+    BS_ERR_NOTREADY = 8      /* serving: result not finished yet */
+} bs_status;
+
+/* Arithmetic of the per-pixel work.  FP64 keeps every stage in double; MIXED
+ * keeps Mie coefficients, Bessel tables, the LUT build, the incident field
+ * and per-(pixel, sphere) geometry in double and runs the per-sample sums and
+ * the detector transform in float with compensated accumulation. */
+typedef enum bs_precision { BS_PREC_FP64 = 0, BS_PREC_MIXED = 1 } bs_precision;
+
+/* Detector images (microscope.cu:722-814). */
+typedef enum bs_image_kind {
+    BS_IMG_INTENSITY = 0,     /* getIntensity():          D             */
+    BS_IMG_INCIDENT = 1,      /* getIncidentFieldImage(): Di            */
+    BS_IMG_ABSORBANCE = 2,    /* getAbsorbance():         -log10(D/Di)  */
+    BS_IMG_TRANSMITTANCE = 3  /* getTransmittance():      D/Di          */
+} bs_image_kind;
+
+/* Near-field planes (nearfieldStruct::U and ::Uf, nearfield.h:38-42). */
+typedef enum bs_field_kind { BS_FIELD_TOTAL = 0, BS_FIELD_INCIDENT = 1 } bs_field_kind;
+
+/*
+ * Simulation state after the reference's LoadParameters (arguments.h:564-593):
+ * the fields of nearfieldStruct (nearfield.h:14-120) and microscopeStruct
+ * (microscope.h:23-142) that the single-source path reads.  The `bimsim` CLI
+ * of this project fills it from the reference's flags.
+ */
+typedef struct bs_params {
+    double lambda;            /* nf.lambda, um (arguments.h:115-132)                  */
+    double amplitude;         /* nf.A (arguments.h:455)                                */
+    double k_dir[3];          /* nf.k, unit incident direction (arguments.h:484-493)   */
+    double focus[3];          /* nf.focus (arguments.h:479-481)                        */
+    double condenser[2];      /* nf.condenser NA inner/outer (arguments.h:459-468)     */
+    double objective[2];      /* SCOPE->objective NA inner/outer (arguments.h:322-338) */
+    double plane_min[3];      /* detector plane corners and normal given to            */
+    double plane_max[3];      /*   microscopeStruct::setPos (arguments.h:340-407)      */
+    double plane_normal[3];
+    int32_t resolution;       /* detector pixels per side (--resolution)               */
+    int32_t padding;          /* --padding, FFT padding factor p                       */
+    int32_t supersample;      /* ss (arguments.h:411-418)                              */
+    int32_t field_order;      /* nf.m, incident-field order (--field-order)            */
+    int32_t scalar;           /* 1 = scalar, 0 = the reference's vector stub           */
+    int32_t plane_wave;       /* --plane-wave                                          */
+    int32_t lut_uf;           /* nf.lut_uf (arguments.h:92-113)                        */
+    int32_t lut_us;           /* nf.lut_us                                             */
+    int32_t us_lut_r;         /* Usp radial samples; 0 = reference 2*R (sphere.cpp:238)*/
+    int32_t us_lut_theta;     /* Usp/Uip angular samples; 0 = 1000 (defaults.h:83)     */
+    int32_t uf_lut_r;         /* Uf LUT radial samples; 0 = 2*R (nfScalarUfLut.cu:134) */
+    int32_t reserved;
+} bs_params;
+
+/* One sphere with its refractive index already evaluated at lambda
+ * (sphere.h:14-92; the material lookup is nearfield.cpp:119-124). */
+typedef struct bs_sphere {
+    double x, y, z;           /* centre, um  */
+    double a;                 /* radius, um  */
+    double n_re, n_im;        /* n + i k     */
+} bs_sphere;
+
+/* Derived sizes of a context (read back for tests and callers). */
+typedef struct bs_info {
+    int32_t nf_res;           /* near-field pixels per side R = res*ss*(2p+1) */
+    int32_t det_res;          /* detector pixels per side                      */
+    int32_t n_spheres;
+    int32_t n_waves;
+    int32_t uf_lut_r;
+    int32_t us_lut_theta;
+    int64_t device_bytes;     /* HBM held by the context                       */
+} bs_info;
+
+/* Per-stage device timings (ms) and launch count of the last bs_simulate. */
+typedef struct bs_stats {
+    double ms_total;
+    double ms_uf;
+    double ms_mie;
+    double ms_lut;
+    double ms_us;
+    double ms_detector;
+    int64_t kernel_launches;
+    int64_t us_interactions;  /* (pixel, sphere, wave) triples evaluated */
+} bs_stats;
+
+typedef struct bs_ctx bs_ctx;
+
+/* Library version string. */
+const char* bs_version(void);
+
+/* Last error message of this host thread (empty string if none). */
+const char* bs_last_error(void);
+
+/* Allocate a context on the current CUDA device (microscopeStruct::init,
+ * microscope.cu:537; nearfieldStruct::init, nearfield.cpp:25).  The context
+ * owns all device memory and one CUDA stream. */
+bs_status bs_create(const bs_params* params, bs_ctx** out);
+
+/* Free everything the context holds (microscopeStruct::destroy). */
+bs_status bs_destroy(bs_ctx* ctx);
+
+/* Sphere list (lSpheres arguments.h:193-320, with the material resolved). */
+bs_status bs_set_spheres(bs_ctx* ctx, const bs_sphere* spheres, int32_t n);
+
+/* Monte Carlo plane-wave directions, 3*nk doubles (x,y,z per wave).
+ * Replaces nearfieldStruct::calcWaves (nearfield.cpp:96-108) so that results
+ * do not depend on a random generator. */
+bs_status bs_set_waves(bs_ctx* ctx, const double* dirs, int32_t nk);
+
+/* The reference's own sampler: glibc rand() from seed 0 (nearfield.cpp:102,
+ * montecarlo.cpp:9-71), restated bit-for-bit in single precision. */
+bs_status bs_sample_waves_compat(bs_ctx* ctx, int32_t nk);
+
+/* Run the near field and the detector (microscopeStruct::Simulate,
+ * microscope.cu:849-857).  Synchronous. */
+bs_status bs_simulate(bs_ctx* ctx, bs_precision precision);
+
+/* Copy a detector image to host memory (float32, row-major, det_res^2). */
+bs_status bs_get_image(bs_ctx* ctx, bs_image_kind kind, float* host, size_t count);
+
+/* Same image in double precision (FP64 runs keep double images). */
+bs_status bs_get_image_f64(bs_ctx* ctx, bs_image_kind kind, double* host, size_t count);
+
+/* Copy a near-field plane to host memory as interleaved (re, im) doubles,
+ * nf_res^2 complex values. */
+bs_status bs_get_field(bs_ctx* ctx, bs_field_kind kind, double* host, size_t count);
+
+/* Append or write one band to an ENVI file (scalarslice::toEnvi,
+ * scalarslice.cu:146-166; rts/envi/envi.h:196-433).  band_value is the
+ * header's wavelength entry (lambda, or 1e4/lambda for --nu). */
+bs_status bs_write_envi(bs_ctx* ctx, bs_image_kind kind, const char* path,
+                        int32_t append, double band_value);
+
+bs_status bs_get_info(bs_ctx* ctx, bs_info* out);
+bs_status bs_get_stats(bs_ctx* ctx, bs_stats* out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* BIMSIM_GB300_H */
