@@ -1,0 +1,151 @@
+"""ctypes binding of libbimsim_gb300.so and a thin context wrapper."""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import abi
+
+PKG = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+_LIB = None
+
+
+class BimsimError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"{abi.STATUS_NAMES.get(status, status)}: {msg}")
+        self.status = status
+
+
+def library_path():
+    return os.path.join(PKG, "lib", "libbimsim_gb300.so")
+
+
+def library():
+    """Load the CUDA library; raises if it was not built (no fallback)."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = library_path()
+    if not os.path.exists(path):
+        raise RuntimeError(f"{path} is missing: build it with __graft_entry__.build() "
+                           "or python -m bimsim_gb300.build")
+    lib = C.CDLL(path)
+    vp, i32, sz = C.c_void_p, C.c_int32, C.c_size_t
+    proto = {
+        "bs_version": ([], C.c_char_p),
+        "bs_last_error": ([], C.c_char_p),
+        "bs_create": ([vp, C.POINTER(vp)], C.c_int),
+        "bs_destroy": ([vp], C.c_int),
+        "bs_set_spheres": ([vp, vp, i32], C.c_int),
+        "bs_set_waves": ([vp, vp, i32], C.c_int),
+        "bs_sample_waves_compat": ([vp, i32], C.c_int),
+        "bs_set_lut_budget": ([vp, sz], C.c_int),
+        "bs_simulate": ([vp, C.c_int], C.c_int),
+        "bs_get_image": ([vp, C.c_int, vp, sz], C.c_int),
+        "bs_get_image_f64": ([vp, C.c_int, vp, sz], C.c_int),
+        "bs_get_field": ([vp, C.c_int, vp, sz], C.c_int),
+        "bs_write_envi": ([vp, C.c_int, C.c_char_p, i32, C.c_double], C.c_int),
+        "bs_get_info": ([vp, vp], C.c_int),
+        "bs_get_stats": ([vp, vp], C.c_int),
+        "bs_get_mie": ([vp, i32, vp, vp, i32], C.c_int),
+        "bs_get_lut": ([vp, i32, i32, vp, sz], C.c_int),
+    }
+    for name, (args, res) in proto.items():
+        f = getattr(lib, name)
+        f.argtypes = args
+        f.restype = res
+    _LIB = lib
+    return lib
+
+
+def _p(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+class Context:
+    """One simulation context (owns device memory and a CUDA stream)."""
+
+    def __init__(self, params):
+        self.lib = library()
+        self.params = params
+        h = C.c_void_p()
+        self._check(self.lib.bs_create(C.byref(params), C.byref(h)))
+        self.h = h
+
+    def _check(self, st):
+        if st != 0:
+            raise BimsimError(st, self.lib.bs_last_error().decode())
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.bs_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def set_spheres(self, spheres):
+        arr, n = spheres if isinstance(spheres, tuple) else abi.sphere_array(spheres)
+        self._check(self.lib.bs_set_spheres(self.h, C.cast(arr, C.c_void_p), n))
+
+    def set_waves(self, dirs):
+        d = np.ascontiguousarray(dirs, dtype=np.float64).reshape(-1)
+        self._check(self.lib.bs_set_waves(self.h, _p(d), len(d) // 3))
+
+    def sample_waves_compat(self, nk):
+        self._check(self.lib.bs_sample_waves_compat(self.h, nk))
+
+    def set_lut_budget(self, nbytes):
+        self._check(self.lib.bs_set_lut_budget(self.h, nbytes))
+
+    def simulate(self, precision=abi.BS_PREC_MIXED):
+        self._check(self.lib.bs_simulate(self.h, precision))
+
+    def info(self):
+        i = abi.Info()
+        self._check(self.lib.bs_get_info(self.h, C.byref(i)))
+        return i
+
+    def stats(self):
+        s = abi.Stats()
+        self._check(self.lib.bs_get_stats(self.h, C.byref(s)))
+        return s
+
+    def image(self, kind=abi.BS_IMG_INTENSITY, f64=False):
+        res = self.params.resolution
+        if f64:
+            out = np.zeros(res * res, dtype=np.float64)
+            self._check(self.lib.bs_get_image_f64(self.h, kind, _p(out), out.size))
+        else:
+            out = np.zeros(res * res, dtype=np.float32)
+            self._check(self.lib.bs_get_image(self.h, kind, _p(out), out.size))
+        return out.reshape(res, res)
+
+    def field(self, kind=abi.BS_FIELD_TOTAL):
+        R = self.info().nf_res
+        out = np.zeros(2 * R * R, dtype=np.float64)
+        self._check(self.lib.bs_get_field(self.h, kind, _p(out), R * R))
+        return out.view(np.complex128).reshape(R, R)
+
+    def mie(self, sphere, nl):
+        A = np.zeros(2 * (nl + 1))
+        B = np.zeros(2 * (nl + 1))
+        self._check(self.lib.bs_get_mie(self.h, sphere, _p(A), _p(B), nl + 1))
+        return A.view(np.complex128), B.view(np.complex128)
+
+    def lut(self, sphere, which, rows, thetaR):
+        out = np.zeros(2 * rows * thetaR)
+        self._check(self.lib.bs_get_lut(self.h, sphere, which, _p(out), rows * thetaR))
+        return out.view(np.complex128).reshape(rows, thetaR)
+
+    def write_envi(self, kind, path, append, band_value):
+        self._check(self.lib.bs_write_envi(self.h, kind, path.encode(), 1 if append else 0, band_value))

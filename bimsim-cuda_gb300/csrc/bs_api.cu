@@ -1,0 +1,788 @@
+// bs_api.cu -- the C ABI of include/bimsim_gb300.h: context, device memory,
+// the per-slice stage pipeline, and result readback.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <type_traits>
+#include <vector>
+
+#include "bimsim_gb300.h"
+#include "bs_internal.h"
+#include "bs_kernels.h"
+#include "bs_math.cuh"
+
+using namespace bs;
+
+namespace {
+
+thread_local std::string g_err;
+
+bs_status fail(bs_status st, const char* fmt, ...) {
+    char buf[1024];
+    va_list ap;
+    va_start(ap, fmt);
+    std::vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    return st;
+}
+
+#define CK(x)                                                                                               \
+    do {                                                                                                    \
+        cudaError_t e_ = (x);                                                                               \
+        if (e_ != cudaSuccess)                                                                              \
+            return fail(e_ == cudaErrorMemoryAllocation ? BS_ERR_NOMEM : BS_ERR_CUDA, "%s failed: %s (%s:%d)", \
+                        #x, cudaGetErrorString(e_), __FILE__, __LINE__);                                    \
+    } while (0)
+
+#define LAUNCHED(ctx)                                                                                   \
+    do {                                                                                                \
+        (ctx)->launches++;                                                                              \
+        cudaError_t e_ = cudaGetLastError();                                                            \
+        if (e_ != cudaSuccess)                                                                          \
+            return fail(BS_ERR_CUDA, "kernel launch failed: %s (%s:%d)", cudaGetErrorString(e_), __FILE__, \
+                        __LINE__);                                                                      \
+    } while (0)
+
+struct DevBuf {
+    void* p = nullptr;
+    size_t n = 0;
+    cudaError_t ensure(size_t bytes) {
+        if (bytes == 0) bytes = 256;
+        if (bytes <= n) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+        cudaError_t e = cudaMalloc(&p, bytes);
+        if (e == cudaSuccess) n = bytes;
+        return e;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    template <class X>
+    X* as() const {
+        return reinterpret_cast<X*>(p);
+    }
+};
+
+bool valid_params(const bs_params* p, std::string& why) {
+    if (!(p->lambda > 0)) { why = "lambda must be > 0"; return false; }
+    if (p->resolution <= 0) { why = "resolution must be > 0"; return false; }
+    if (p->padding < 0) { why = "padding must be >= 0"; return false; }
+    if (p->supersample < 1) { why = "supersample must be >= 1"; return false; }
+    if (p->field_order < 0 || p->field_order > MAX_ORDER) { why = "field order out of range"; return false; }
+    if (p->condenser[0] < 0 || p->condenser[1] > 1 || p->condenser[0] > p->condenser[1]) {
+        why = "condenser NA must satisfy 0 <= NA_in <= NA_out <= 1"; return false;
+    }
+    long long R = (long long)p->resolution * p->supersample * (2LL * p->padding + 1);
+    if (R > 65536) { why = "near-field resolution above 65536"; return false; }
+    if (p->us_lut_r == 1 || p->us_lut_theta == 1 || p->uf_lut_r == 1 || p->us_lut_r < 0 || p->us_lut_theta < 0 ||
+        p->uf_lut_r < 0) {
+        why = "LUT sizes must be 0 (reference default) or >= 2"; return false;
+    }
+    return true;
+}
+
+}  // namespace
+
+struct bs_ctx {
+    bs_params prm{};
+    std::vector<bs_sphere> spheres;
+    std::vector<double> waves;
+    bool waves_set = false;
+    int device = 0;
+    cudaStream_t st = nullptr;
+    cudaEvent_t ev[6] = {};
+    size_t budget = 0;  // LUT bytes allowed; 0 = automatic
+
+    // derived per simulate
+    Scene sc{};
+    std::vector<Sphere> hs;
+    int res = 0, ss = 1, crop = 0, off = 0, R = 0, Lmax = 1;
+    int prec = -1;
+    bool have = false;
+
+    DevBuf d_sph, d_waves, d_kw4, d_cones, d_ph, d_A, d_B, d_mie, d_tab, d_tabscr, d_legP, d_lut, d_uft, d_uftscr;
+    DevBuf d_fields;  // [2][R*R] U then Uf
+    DevBuf d_su, d_sv, d_mask, d_wx, d_wy, d_wix, d_wiy, d_f1, d_f2, d_g1, d_I, d_D, d_img;
+    int legP_theta = 0, legP_L = 0;
+    int64_t launches = 0;
+    int64_t interactions = 0;
+    bs_stats stats{};
+};
+
+static size_t elem_r(int prec) { return prec == BS_PREC_FP64 ? sizeof(double) : sizeof(float); }
+
+extern "C" {
+
+const char* bs_version(void) { return "bimsim-gb300 0.1 (sm_103a)"; }
+
+const char* bs_last_error(void) { return g_err.c_str(); }
+
+bs_status bs_create(const bs_params* params, bs_ctx** out) {
+    if (!params || !out) return fail(BS_ERR_ARG, "bs_create: null argument");
+    std::string why;
+    if (!valid_params(params, why)) return fail(BS_ERR_ARG, "bs_create: %s", why.c_str());
+    bs_ctx* c = new bs_ctx();
+    c->prm = *params;
+    cudaError_t e = cudaGetDevice(&c->device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking);
+    for (int i = 0; i < 6 && e == cudaSuccess; i++) e = cudaEventCreate(&c->ev[i]);
+    if (e != cudaSuccess) {
+        delete c;
+        return fail(BS_ERR_CUDA, "bs_create: %s", cudaGetErrorString(e));
+    }
+    *out = c;
+    return BS_OK;
+}
+
+bs_status bs_destroy(bs_ctx* c) {
+    if (!c) return BS_OK;
+    if (c->st) cudaStreamSynchronize(c->st);
+    DevBuf* bufs[] = {&c->d_sph, &c->d_waves, &c->d_kw4, &c->d_cones, &c->d_ph, &c->d_A, &c->d_B, &c->d_mie, &c->d_tab,
+                      &c->d_tabscr, &c->d_legP, &c->d_lut, &c->d_uft, &c->d_uftscr, &c->d_fields, &c->d_su,
+                      &c->d_sv, &c->d_mask, &c->d_wx, &c->d_wy, &c->d_wix, &c->d_wiy, &c->d_f1, &c->d_f2,
+                      &c->d_g1, &c->d_I, &c->d_D, &c->d_img};
+    for (DevBuf* b : bufs) b->release();
+    for (int i = 0; i < 6; i++)
+        if (c->ev[i]) cudaEventDestroy(c->ev[i]);
+    if (c->st) cudaStreamDestroy(c->st);
+    delete c;
+    return BS_OK;
+}
+
+bs_status bs_set_spheres(bs_ctx* c, const bs_sphere* s, int32_t n) {
+    if (!c || n < 0 || (n > 0 && !s)) return fail(BS_ERR_ARG, "bs_set_spheres: bad arguments");
+    for (int i = 0; i < n; i++)
+        if (!(s[i].a > 0) || !std::isfinite(s[i].x) || !std::isfinite(s[i].y) || !std::isfinite(s[i].z))
+            return fail(BS_ERR_ARG, "bs_set_spheres: sphere %d has a non-positive radius or bad centre", i + 1);
+    c->spheres.assign(s, s + n);
+    c->have = false;
+    return BS_OK;
+}
+
+bs_status bs_set_waves(bs_ctx* c, const double* dirs, int32_t nk) {
+    if (!c || nk < 1 || !dirs) return fail(BS_ERR_ARG, "bs_set_waves: need at least one direction");
+    c->waves.assign(dirs, dirs + 3 * (size_t)nk);
+    c->waves_set = true;
+    c->have = false;
+    return BS_OK;
+}
+
+bs_status bs_sample_waves_compat(bs_ctx* c, int32_t nk) {
+    if (!c || nk < 1) return fail(BS_ERR_ARG, "bs_sample_waves_compat: nk must be >= 1");
+    c->waves.resize(3 * (size_t)nk);
+    mc_sample_compat(nk, c->prm.k_dir, c->prm.condenser[0], c->prm.condenser[1], c->waves.data());
+    c->waves_set = true;
+    c->have = false;
+    return BS_OK;
+}
+
+bs_status bs_set_lut_budget(bs_ctx* c, size_t bytes) {
+    if (!c) return fail(BS_ERR_ARG, "bs_set_lut_budget: null context");
+    c->budget = bytes;
+    return BS_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Derivation of the slice and sphere parameters (arguments.h:340-438,
+// microscope.cu:700-718, sphere.cpp:222-240, nfScalarUpLut.cu:365-379)
+// ---------------------------------------------------------------------------
+static bs_status derive(bs_ctx* c) {
+    const bs_params& p = c->prm;
+    Quad det = quad_from(p.plane_min, p.plane_max, p.plane_normal);
+    Quad nf = quad_scale(det, (double)(2 * p.padding + 1));
+    c->res = p.resolution;
+    c->ss = p.supersample;
+    c->crop = c->res * c->ss;
+    c->off = p.padding * c->crop;
+    c->R = c->crop * (2 * p.padding + 1);
+    Scene& sc = c->sc;
+    sc = Scene{};
+    const V3* v[3] = {&nf.A, &nf.X, &nf.Y};
+    double* d[3] = {sc.A, sc.X, sc.Y};
+    for (int i = 0; i < 3; i++) {
+        d[i][0] = v[i]->x;
+        d[i][1] = v[i]->y;
+        d[i][2] = v[i]->z;
+    }
+    for (int i = 0; i < 3; i++) {
+        sc.focus[i] = p.focus[i];
+        sc.kdir[i] = p.k_dir[i];
+    }
+    sc.kmag = 2 * PI_REF / p.lambda;
+    sc.amp = p.amplitude;
+    sc.cos_a = std::cos(std::asin(p.condenser[0]));
+    sc.cos_b = std::cos(std::asin(p.condenser[1]));
+    sc.R = c->R;
+    sc.m = p.field_order;
+    sc.plane_wave = p.plane_wave;
+    sc.lut_uf = p.lut_uf;
+    sc.lut_us = p.lut_us;
+    sc.scalar = p.scalar;
+    if (p.plane_wave) {
+        sc.nk = 1;
+        sc.wave_amp = p.amplitude;
+    } else {
+        if (!c->waves_set)
+            return fail(BS_ERR_STATE, "bs_simulate: no plane-wave directions (call bs_set_waves or bs_sample_waves_compat)");
+        sc.nk = (int)(c->waves.size() / 3);
+        double sub = 2 * PI_REF * p.amplitude * ((1 - sc.cos_b) - (1 - sc.cos_a));
+        sc.wave_amp = (1.0 / sc.nk) * sub;
+    }
+    V3 f{p.focus[0], p.focus[1], p.focus[2]};
+    sc.uf_dmin = quad_dist(nf, f);
+    sc.uf_dmax = quad_dist_max(nf, f);
+    sc.uf_dR = p.uf_lut_r > 0 ? p.uf_lut_r : 2 * c->R;
+    sc.ns = (int)c->spheres.size();
+    c->hs.resize(sc.ns);
+    double diag = v3_len(V3{nf.X.x + nf.Y.x, nf.X.y + nf.Y.y, nf.X.z + nf.Y.z});
+    int coef = 0;
+    c->Lmax = std::max(2, sc.m + 1);
+    for (int i = 0; i < sc.ns; i++) {
+        const bs_sphere& in = c->spheres[i];
+        Sphere& S = c->hs[i];
+        S = Sphere{};
+        S.p[0] = in.x;
+        S.p[1] = in.y;
+        S.p[2] = in.z;
+        S.a = in.a;
+        S.n_re = in.n_re;
+        S.n_im = in.n_im;
+        S.Nl = calc_nl(in.a, p.lambda);
+        if (S.Nl < 1 || S.Nl > MAX_ORDER) return fail(BS_ERR_ARG, "sphere %d: order %d out of range", i + 1, S.Nl);
+        V3 ctr{in.x, in.y, in.z};
+        S.dmin = quad_dist(nf, ctr);
+        S.dmax = quad_dist_max(nf, ctr);
+        double a_inter = (S.dmin < in.a) ? std::sqrt(in.a - S.dmin) : 0.0;  // sphere.cpp:231-233 (sic)
+        S.aR = (int)(1 + 2.0 * c->R * a_inter / diag);
+        S.dR = p.us_lut_r > 0 ? p.us_lut_r : 2 * c->R;
+        S.thetaR = p.us_lut_theta > 0 ? p.us_lut_theta : 1000;
+        S.r0 = std::max(in.a, S.dmin);
+        S.coef_off = coef;
+        coef += S.Nl + 1;
+        c->Lmax = std::max(c->Lmax, S.Nl + 1);
+    }
+    return BS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// The band-limited detector (microscope.cu:495-526, 608-662)
+// ---------------------------------------------------------------------------
+template <class T>
+static bs_status run_detector(bs_ctx* c) {
+    const bs_params& p = c->prm;
+    const int R = c->R;
+    double du = 1.0 / std::sqrt(c->sc.X[0] * c->sc.X[0] + c->sc.X[1] * c->sc.X[1] + c->sc.X[2] * c->sc.X[2]);
+    double dv = 1.0 / std::sqrt(c->sc.Y[0] * c->sc.Y[0] + c->sc.Y[1] * c->sc.Y[1] + c->sc.Y[2] * c->sc.Y[2]);
+    double lo = p.objective[0] / p.lambda, hi = p.objective[1] / p.lambda;
+    // frequency of bin i as the reference's bandpass kernel assigns it (note
+    // -(R-1-i) rather than -(R-i) on the negative side)
+    auto freq = [R](int i, double step) { return (i <= R / 2) ? i * step : -(double)(R - 1 - i) * step; };
+    std::vector<int> su, sv;
+    for (int i = 0; i < R; i++) {
+        if (std::fabs(freq(i, du)) <= hi) su.push_back(i);
+        if (std::fabs(freq(i, dv)) <= hi) sv.push_back(i);
+    }
+    const int Nu = (int)su.size(), Nv = (int)sv.size(), C = c->crop, res = c->res;
+    CK(c->d_D.ensure(2 * (size_t)res * res * sizeof(T)));
+    if (Nu == 0 || Nv == 0) {
+        CK(cudaMemsetAsync(c->d_D.p, 0, 2 * (size_t)res * res * sizeof(T), c->st));
+        return BS_OK;
+    }
+    std::vector<float> mask((size_t)Nv * Nu);
+    for (int j = 0; j < Nv; j++)
+        for (int k = 0; k < Nu; k++) {
+            double u = freq(su[k], du), v = freq(sv[j], dv);
+            double fm = std::sqrt(u * u + v * v);
+            mask[(size_t)j * Nu + k] = (fm < lo || fm > hi) ? 0.f : 1.f;
+        }
+    size_t ce = sizeof(cpx<T>);
+    CK(c->d_su.ensure(Nu * sizeof(int)));
+    CK(c->d_sv.ensure(Nv * sizeof(int)));
+    CK(c->d_mask.ensure(mask.size() * sizeof(float)));
+    CK(c->d_wx.ensure((size_t)R * Nu * ce));
+    CK(c->d_wy.ensure((size_t)Nv * R * ce));
+    CK(c->d_wix.ensure((size_t)Nu * C * ce));
+    CK(c->d_wiy.ensure((size_t)C * Nv * ce));
+    CK(c->d_f1.ensure(2 * (size_t)R * Nu * ce));
+    CK(c->d_f2.ensure(2 * (size_t)Nv * Nu * ce));
+    CK(c->d_g1.ensure(2 * (size_t)Nv * C * ce));
+    CK(c->d_I.ensure(2 * (size_t)C * C * sizeof(T)));
+    CK(cudaMemcpyAsync(c->d_su.p, su.data(), Nu * sizeof(int), cudaMemcpyHostToDevice, c->st));
+    CK(cudaMemcpyAsync(c->d_sv.p, sv.data(), Nv * sizeof(int), cudaMemcpyHostToDevice, c->st));
+    CK(cudaMemcpyAsync(c->d_mask.p, mask.data(), mask.size() * sizeof(float), cudaMemcpyHostToDevice, c->st));
+    cpx<T>* wx = c->d_wx.as<cpx<T>>();
+    cpx<T>* wy = c->d_wy.as<cpx<T>>();
+    cpx<T>* wix = c->d_wix.as<cpx<T>>();
+    cpx<T>* wiy = c->d_wiy.as<cpx<T>>();
+    // forward x: Wx[x][k] = e^{-2 pi i x su_k / R}; forward y: Wy[j][y] = e^{-2 pi i y sv_j / R}
+    launch_twiddle<T>(R, Nu, c->d_su.as<int>(), 0, R, -1, Nu, 1, wx, c->st);
+    LAUNCHED(c);
+    launch_twiddle<T>(R, Nv, c->d_sv.as<int>(), 0, R, -1, 1, R, wy, c->st);
+    LAUNCHED(c);
+    // inverse on the crop only: Wix[k][x] = e^{+2 pi i (off+x) su_k / R}, Wiy[y][j] likewise
+    launch_twiddle<T>(C, Nu, c->d_su.as<int>(), c->off, R, +1, 1, C, wix, c->st);
+    LAUNCHED(c);
+    launch_twiddle<T>(C, Nv, c->d_sv.as<int>(), c->off, R, +1, Nv, 1, wiy, c->st);
+    LAUNCHED(c);
+    const cpx<T>* fields = c->d_fields.as<cpx<T>>();
+    cpx<T>* f1 = c->d_f1.as<cpx<T>>();
+    cpx<T>* f2 = c->d_f2.as<cpx<T>>();
+    cpx<T>* g1 = c->d_g1.as<cpx<T>>();
+    T* I = c->d_I.as<T>();
+    long long RR = (long long)R * R;
+    launch_cgemm<T>(R, Nu, R, 2, fields, R, RR, wx, Nu, 0, f1, Nu, (long long)R * Nu, 0, nullptr, (T)1, nullptr,
+                    c->st);
+    LAUNCHED(c);
+    launch_cgemm<T>(Nv, Nu, R, 2, wy, R, 0, f1, Nu, (long long)R * Nu, f2, Nu, (long long)Nv * Nu, 1,
+                    c->d_mask.as<float>(), (T)1, nullptr, c->st);
+    LAUNCHED(c);
+    launch_cgemm<T>(Nv, C, Nu, 2, f2, Nu, (long long)Nv * Nu, wix, C, 0, g1, C, (long long)Nv * C, 0, nullptr, (T)1,
+                    nullptr, c->st);
+    LAUNCHED(c);
+    T scale = (T)(1.0 / ((double)R * (double)R));
+    launch_cgemm<T>(C, C, Nv, 2, wiy, Nv, 0, g1, C, (long long)Nv * C, nullptr, C, (long long)C * C, 2, nullptr,
+                    scale, I, c->st);
+    LAUNCHED(c);
+    launch_bin<T>(res, c->ss, 2, I, c->d_D.as<T>(), c->st);
+    LAUNCHED(c);
+    return BS_OK;
+}
+
+// Place each sphere's Usp and Uip patches in the LUT pool; spheres whose
+// tables together exceed the budget go to later chunks (each chunk is built
+// and applied before the next one overwrites the pool).
+static bs_status plan_luts(bs_ctx* c, size_t patch, std::vector<int>& chunk_start, size_t& pool, size_t& maxrows,
+                           size_t& maxL) {
+    const int ns = (int)c->hs.size();
+    size_t free_b = 0, total_b = 0;
+    CK(cudaMemGetInfo(&free_b, &total_b));
+    size_t budget = c->budget ? c->budget : (size_t)(0.80 * (double)(free_b + c->d_lut.n));
+    chunk_start.clear();
+    size_t acc = 0;
+    pool = 0;
+    maxrows = 0;
+    maxL = 0;
+    for (int i = 0; i < ns; i++) {
+        Sphere& S = c->hs[i];
+        size_t need = (size_t)(S.dR + S.aR) * S.thetaR * patch;
+        if (need > budget)
+            return fail(BS_ERR_NOMEM, "LUT of sphere %d needs %zu bytes, over the budget of %zu", i + 1, need, budget);
+        if (i == 0 || acc + need > budget) {
+            chunk_start.push_back(i);
+            acc = 0;
+        }
+        S.usp_off = (int64_t)(acc / patch);
+        S.uip_off = S.usp_off + (int64_t)S.dR * S.thetaR;
+        acc += need;
+        pool = std::max(pool, acc);
+        maxrows = std::max(maxrows, (size_t)(S.dR + S.aR));
+        maxL = std::max(maxL, (size_t)(S.Nl + 1));
+    }
+    chunk_start.push_back(ns);
+    return BS_OK;
+}
+
+// Order plane waves along a Hilbert curve of their projection on the plane
+// perpendicular to the mean direction.  The sum over waves does not depend
+// on the order (up to rounding), but neighbouring waves then give
+// neighbouring LUT angles for every pixel, which keeps each block's LUT
+// working set small enough for the L1 cache.
+static uint32_t hilbert_d(uint32_t n, uint32_t x, uint32_t y) {
+    uint32_t d = 0;
+    for (uint32_t s = n / 2; s > 0; s /= 2) {
+        uint32_t rx = (x & s) > 0, ry = (y & s) > 0;
+        d += s * s * ((3 * rx) ^ ry);
+        if (ry == 0) {
+            if (rx == 1) {
+                x = s - 1 - x;
+                y = s - 1 - y;
+            }
+            uint32_t t = x;
+            x = y;
+            y = t;
+        }
+    }
+    return d;
+}
+
+static void sort_waves(std::vector<double>& w) {
+    size_t nk = w.size() / 3;
+    if (nk < 3) return;
+    double m[3] = {0, 0, 0};
+    for (size_t i = 0; i < nk; i++)
+        for (int c = 0; c < 3; c++) m[c] += w[3 * i + c];
+    double ml = std::sqrt(m[0] * m[0] + m[1] * m[1] + m[2] * m[2]);
+    if (!(ml > 0)) return;
+    for (int c = 0; c < 3; c++) m[c] /= ml;
+    double a[3] = {1, 0, 0};
+    if (std::fabs(m[0]) > 0.9) a[0] = 0, a[1] = 1;
+    double e1[3] = {a[1] * m[2] - a[2] * m[1], a[2] * m[0] - a[0] * m[2], a[0] * m[1] - a[1] * m[0]};
+    double l1 = std::sqrt(e1[0] * e1[0] + e1[1] * e1[1] + e1[2] * e1[2]);
+    for (int c = 0; c < 3; c++) e1[c] /= l1;
+    double e2[3] = {m[1] * e1[2] - m[2] * e1[1], m[2] * e1[0] - m[0] * e1[2], m[0] * e1[1] - m[1] * e1[0]};
+    std::vector<std::pair<uint32_t, size_t>> key(nk);
+    const uint32_t G = 1024;
+    for (size_t i = 0; i < nk; i++) {
+        const double* k = &w[3 * i];
+        double x = k[0] * e1[0] + k[1] * e1[1] + k[2] * e1[2];
+        double y = k[0] * e2[0] + k[1] * e2[1] + k[2] * e2[2];
+        uint32_t gx = (uint32_t)std::min<double>(G - 1, std::max(0.0, (x + 1.0) * 0.5 * G));
+        uint32_t gy = (uint32_t)std::min<double>(G - 1, std::max(0.0, (y + 1.0) * 0.5 * G));
+        key[i] = {hilbert_d(G, gx, gy), i};
+    }
+    std::stable_sort(key.begin(), key.end());
+    std::vector<double> out(w.size());
+    for (size_t i = 0; i < nk; i++)
+        for (int c = 0; c < 3; c++) out[3 * i + c] = w[3 * key[i].second + c];
+    w.swap(out);
+}
+
+// Bounding cone (unit axis, half-angle in radians) of every WAVE_CHUNK
+// consecutive waves, with a small margin for single-precision rounding.
+static std::vector<float4> wave_cones(const std::vector<double>& w) {
+    size_t nk = w.size() / 3;
+    size_t nch = (nk + WAVE_CHUNK - 1) / WAVE_CHUNK;
+    std::vector<float4> out(nch);
+    for (size_t ch = 0; ch < nch; ch++) {
+        size_t a = ch * WAVE_CHUNK, b = std::min(nk, a + WAVE_CHUNK);
+        double m[3] = {0, 0, 0};
+        for (size_t i = a; i < b; i++)
+            for (int c = 0; c < 3; c++) m[c] += w[3 * i + c];
+        double ml = std::sqrt(m[0] * m[0] + m[1] * m[1] + m[2] * m[2]);
+        if (ml > 0)
+            for (int c = 0; c < 3; c++) m[c] /= ml;
+        double beta = 0;
+        for (size_t i = a; i < b; i++) {
+            const double* k = &w[3 * i];
+            double kl = std::sqrt(k[0] * k[0] + k[1] * k[1] + k[2] * k[2]);
+            double cth = (k[0] * m[0] + k[1] * m[1] + k[2] * m[2]) / (kl > 0 ? kl : 1);
+            beta = std::max(beta, std::acos(std::min(1.0, std::max(-1.0, cth))));
+        }
+        if (!(ml > 0)) beta = TRUE_PI;
+        out[ch] = make_float4((float)m[0], (float)m[1], (float)m[2], (float)(beta + 1e-4));
+    }
+    return out;
+}
+
+// ---------------------------------------------------------------------------
+// The near field
+// ---------------------------------------------------------------------------
+template <class T>
+static bs_status run_nearfield(bs_ctx* c) {
+    Scene& sc = c->sc;
+    const bs_params& p = c->prm;
+    const int R = c->R, ns = sc.ns, nk = sc.nk;
+    const bool fp64 = std::is_same<T, double>::value;
+    CK(c->d_fields.ensure(2 * (size_t)R * R * sizeof(cpx<T>)));
+    cpx<T>* U = c->d_fields.as<cpx<T>>();
+    cpx<T>* Uf = U + (size_t)R * R;
+    // upload spheres and waves
+    CK(c->d_sph.ensure(std::max(1, ns) * sizeof(Sphere)));
+    std::vector<double> w(c->waves);
+    if (p.plane_wave) w.assign(p.k_dir, p.k_dir + 3);
+    else sort_waves(w);
+    CK(c->d_waves.ensure(w.size() * sizeof(double)));
+    CK(cudaMemcpyAsync(c->d_waves.p, w.data(), w.size() * sizeof(double), cudaMemcpyHostToDevice, c->st));
+
+    // ---- incident field ----
+    cudaEventRecord(c->ev[0], c->st);
+    if (p.lut_uf && !p.plane_wave && p.scalar) {
+        CK(c->d_uft.ensure((size_t)sc.uf_dR * (sc.m + 1) * sizeof(double)));
+        CK(c->d_uftscr.ensure((size_t)sc.uf_dR * (sc.m + 1) * sizeof(double)));
+        launch_uf_table(sc, c->d_uft.as<double>(), c->d_uftscr.as<double>(), c->st);
+        LAUNCHED(c);
+    }
+    launch_uf<T>(sc, c->d_uft.as<double>(), Uf, c->st);
+    LAUNCHED(c);
+    cudaEventRecord(c->ev[1], c->st);
+
+    // ---- LUT placement (before the sphere table goes to the device) ----
+    std::vector<int> chunk_start;
+    size_t pool = 0, maxrows = 0, maxL = 0;
+    if (p.scalar && p.lut_us && ns > 0) {
+        bs_status pst = plan_luts(c, fp64 ? sizeof(Patch<double>) : sizeof(Patch<float>), chunk_start, pool, maxrows, maxL);
+        if (pst != BS_OK) return pst;
+    }
+
+    // ---- Mie coefficients ----
+    int ncoef = 0;
+    for (auto& S : c->hs) ncoef += S.Nl + 1;
+    const bool scatter = p.scalar && ns > 0;
+    if (scatter) {
+        CK(c->d_A.ensure(ncoef * sizeof(zd)));
+        CK(c->d_B.ensure(ncoef * sizeof(zd)));
+        CK(c->d_mie.ensure((size_t)ns * 6 * c->Lmax * sizeof(zd)));
+        CK(cudaMemcpyAsync(c->d_sph.p, c->hs.data(), ns * sizeof(Sphere), cudaMemcpyHostToDevice, c->st));
+        launch_mie(c->d_sph.as<Sphere>(), ns, sc.kmag, c->d_mie.as<zd>(), c->Lmax, c->d_A.as<zd>(),
+                   c->d_B.as<zd>(), c->st);
+        LAUNCHED(c);
+        CK(c->d_ph.ensure((size_t)ns * nk * sizeof(cpx<T>)));
+        std::vector<float4> cones = wave_cones(w);
+        CK(c->d_cones.ensure(cones.size() * sizeof(float4)));
+        CK(cudaMemcpyAsync(c->d_cones.p, cones.data(), cones.size() * sizeof(float4), cudaMemcpyHostToDevice, c->st));
+        CK(c->d_kw4.ensure((size_t)nk * sizeof(float4)));
+        launch_phase<T>(sc, c->d_sph.as<Sphere>(), c->d_waves.as<double>(), c->d_ph.as<cpx<T>>(),
+                        c->d_kw4.as<float4>(), c->st);
+        LAUNCHED(c);
+    } else if (ns > 0) {
+        CK(cudaMemcpyAsync(c->d_sph.p, c->hs.data(), ns * sizeof(Sphere), cudaMemcpyHostToDevice, c->st));
+    }
+    cudaEventRecord(c->ev[2], c->st);
+    c->interactions = 0;
+
+    if (!p.scalar) {
+        launch_sum_only<T>(sc, c->d_sph.as<Sphere>(), Uf, U, c->st);
+        LAUNCHED(c);
+        cudaEventRecord(c->ev[3], c->st);
+    } else if (!p.lut_us) {
+        cudaEventRecord(c->ev[3], c->st);
+        if (ns == 0) {
+            CK(cudaMemcpyAsync(U, Uf, (size_t)R * R * sizeof(cpx<T>), cudaMemcpyDeviceToDevice, c->st));
+        } else {
+            launch_us_direct<T>(sc, c->d_sph.as<Sphere>(), c->Lmax, c->d_A.as<zd>(), c->d_B.as<zd>(),
+                                c->d_waves.as<double>(), c->d_ph.as<cpx<T>>(), Uf, U, c->st);
+            LAUNCHED(c);
+        }
+        c->interactions = (long long)R * R * ns * nk;
+    } else {
+        int thetaR = ns > 0 ? c->hs[0].thetaR : 1000;
+        if (ns > 0) {
+            CK(c->d_lut.ensure(pool));
+            CK(c->d_tab.ensure(maxrows * maxL * sizeof(zd)));
+            CK(c->d_tabscr.ensure(maxrows * 2 * maxL * sizeof(double)));
+            if (c->legP_theta != thetaR || c->legP_L < c->Lmax) {
+                CK(c->d_legP.ensure((size_t)thetaR * c->Lmax * sizeof(double)));
+                launch_legendre_table(thetaR, c->Lmax, c->d_legP.as<double>(), c->st);
+                LAUNCHED(c);
+                c->legP_theta = thetaR;
+                c->legP_L = c->Lmax;
+            }
+        }
+        const int nchunks = (int)chunk_start.size() - 1;
+        bool first_build = true;
+        for (int ci = 0; ci < std::max(1, nchunks); ci++) {
+            int s0 = ns > 0 ? chunk_start[ci] : 0, s1 = ns > 0 ? chunk_start[ci + 1] : 0;
+            for (int i = s0; i < s1; i++) {
+                const Sphere& S = c->hs[i];
+                const int L = S.Nl + 1;
+                launch_coef_rows(S, sc.kmag, c->d_A.as<zd>(), c->d_B.as<zd>(), c->d_tab.as<zd>(),
+                                 c->d_tabscr.as<double>(), c->st);
+                LAUNCHED(c);
+                Patch<T>* lut = c->d_lut.as<Patch<T>>();
+                launch_lut_build<T>(c->d_tab.as<zd>(), S.dR, L, c->d_legP.as<double>(), c->legP_L, S.thetaR,
+                                    lut + S.usp_off, c->st);
+                LAUNCHED(c);
+                launch_lut_build<T>(c->d_tab.as<zd>() + (size_t)S.dR * L, S.aR, L, c->d_legP.as<double>(),
+                                    c->legP_L, S.thetaR, lut + S.uip_off, c->st);
+                LAUNCHED(c);
+            }
+            if (first_build) {
+                cudaEventRecord(c->ev[3], c->st);
+                first_build = false;
+            }
+            int finalize = (ci == std::max(1, nchunks) - 1);
+            if (fp64) {
+                launch_us_lut_f64(sc, c->d_sph.as<Sphere>(), s0, s1, ci > 0, finalize, c->d_waves.as<double>(),
+                                  c->d_ph.as<zd>(), c->d_lut.as<Patch<double>>(), (const zd*)Uf, (zd*)U, c->st);
+            } else {
+                launch_us_lut_f32(sc, c->d_sph.as<Sphere>(), s0, s1, ci > 0, finalize, c->d_kw4.as<float4>(),
+                                  c->d_cones.as<float4>(), c->d_ph.as<cpx<float>>(), c->d_lut.as<Patch<float>>(), (const cpx<float>*)Uf,
+                                  (cpx<float>*)U, c->st);
+            }
+            LAUNCHED(c);
+        }
+        c->interactions = (long long)R * R * ns * nk;
+    }
+    cudaEventRecord(c->ev[4], c->st);
+    return BS_OK;
+}
+
+extern "C" {
+
+bs_status bs_simulate(bs_ctx* c, bs_precision prec) {
+    if (!c) return fail(BS_ERR_ARG, "bs_simulate: null context");
+    if (prec != BS_PREC_FP64 && prec != BS_PREC_MIXED) return fail(BS_ERR_ARG, "bs_simulate: unknown precision");
+    c->have = false;
+    bs_status st = derive(c);
+    if (st != BS_OK) return st;
+    c->prec = prec;
+    int64_t l0 = c->launches;
+    st = (prec == BS_PREC_FP64) ? run_nearfield<double>(c) : run_nearfield<float>(c);
+    if (st != BS_OK) return st;
+    st = (prec == BS_PREC_FP64) ? run_detector<double>(c) : run_detector<float>(c);
+    if (st != BS_OK) return st;
+    cudaEventRecord(c->ev[5], c->st);
+    CK(cudaStreamSynchronize(c->st));
+    CK(cudaGetLastError());
+    float t[5] = {0, 0, 0, 0, 0};
+    for (int i = 0; i < 5; i++) cudaEventElapsedTime(&t[i], c->ev[i], c->ev[i + 1]);
+    c->stats.ms_uf = t[0];
+    c->stats.ms_mie = t[1];
+    c->stats.ms_lut = t[2];
+    c->stats.ms_us = t[3];
+    c->stats.ms_detector = t[4];
+    float tot = 0;
+    cudaEventElapsedTime(&tot, c->ev[0], c->ev[5]);
+    c->stats.ms_total = tot;
+    c->stats.kernel_launches = c->launches - l0;
+    c->stats.us_interactions = c->interactions;
+    c->have = true;
+    return BS_OK;
+}
+
+static bs_status image_to_host(bs_ctx* c, bs_image_kind kind, std::vector<double>& out) {
+    if (!c) return fail(BS_ERR_ARG, "null context");
+    if (!c->have) return fail(BS_ERR_STATE, "no simulation result (call bs_simulate first)");
+    if (kind < BS_IMG_INTENSITY || kind > BS_IMG_TRANSMITTANCE) return fail(BS_ERR_ARG, "unknown image kind");
+    int n = c->res * c->res;
+    size_t es = elem_r(c->prec);
+    CK(c->d_img.ensure((size_t)n * es));
+    if (c->prec == BS_PREC_FP64) {
+        const double* D = c->d_D.as<double>();
+        launch_image<double>(n, kind, D, D + n, c->d_img.as<double>(), c->st);
+    } else {
+        const float* D = c->d_D.as<float>();
+        launch_image<float>(n, kind, D, D + n, c->d_img.as<float>(), c->st);
+    }
+    LAUNCHED(c);
+    out.resize(n);
+    if (c->prec == BS_PREC_FP64) {
+        CK(cudaMemcpyAsync(out.data(), c->d_img.p, n * sizeof(double), cudaMemcpyDeviceToHost, c->st));
+        CK(cudaStreamSynchronize(c->st));
+    } else {
+        std::vector<float> tmp(n);
+        CK(cudaMemcpyAsync(tmp.data(), c->d_img.p, n * sizeof(float), cudaMemcpyDeviceToHost, c->st));
+        CK(cudaStreamSynchronize(c->st));
+        for (int i = 0; i < n; i++) out[i] = tmp[i];
+    }
+    return BS_OK;
+}
+
+bs_status bs_get_image(bs_ctx* c, bs_image_kind kind, float* host, size_t count) {
+    if (!host) return fail(BS_ERR_ARG, "bs_get_image: null buffer");
+    if (c && count < (size_t)c->res * c->res) return fail(BS_ERR_ARG, "bs_get_image: buffer holds %zu of %d values", count, c->res * c->res);
+    std::vector<double> v;
+    bs_status st = image_to_host(c, kind, v);
+    if (st != BS_OK) return st;
+    for (size_t i = 0; i < v.size(); i++) host[i] = (float)v[i];
+    return BS_OK;
+}
+
+bs_status bs_get_image_f64(bs_ctx* c, bs_image_kind kind, double* host, size_t count) {
+    if (!host) return fail(BS_ERR_ARG, "bs_get_image_f64: null buffer");
+    if (c && count < (size_t)c->res * c->res) return fail(BS_ERR_ARG, "bs_get_image_f64: buffer too small");
+    std::vector<double> v;
+    bs_status st = image_to_host(c, kind, v);
+    if (st != BS_OK) return st;
+    std::memcpy(host, v.data(), v.size() * sizeof(double));
+    return BS_OK;
+}
+
+bs_status bs_get_field(bs_ctx* c, bs_field_kind kind, double* host, size_t count) {
+    if (!c || !host) return fail(BS_ERR_ARG, "bs_get_field: null argument");
+    if (!c->have) return fail(BS_ERR_STATE, "bs_get_field: no simulation result");
+    size_t n = (size_t)c->R * c->R;
+    if (count < n) return fail(BS_ERR_ARG, "bs_get_field: buffer holds %zu of %zu complex values", count, n);
+    size_t off = (kind == BS_FIELD_INCIDENT) ? n : 0;
+    if (c->prec == BS_PREC_FP64) {
+        CK(cudaMemcpy(host, c->d_fields.as<zd>() + off, n * sizeof(zd), cudaMemcpyDeviceToHost));
+    } else {
+        std::vector<cpx<float>> tmp(n);
+        CK(cudaMemcpy(tmp.data(), c->d_fields.as<cpx<float>>() + off, n * sizeof(cpx<float>), cudaMemcpyDeviceToHost));
+        for (size_t i = 0; i < n; i++) {
+            host[2 * i] = tmp[i].re;
+            host[2 * i + 1] = tmp[i].im;
+        }
+    }
+    return BS_OK;
+}
+
+bs_status bs_write_envi(bs_ctx* c, bs_image_kind kind, const char* path, int32_t append, double band_value) {
+    if (!path) return fail(BS_ERR_ARG, "bs_write_envi: null path");
+    std::vector<double> v;
+    bs_status st = image_to_host(c, kind, v);
+    if (st != BS_OK) return st;
+    std::vector<float> f(v.begin(), v.end());
+    char err[512] = {0};
+    if (envi_add_band(path, f.data(), c->res, c->res, band_value, append, err, sizeof(err)) != 0)
+        return fail(BS_ERR_IO, "%s", err);
+    return BS_OK;
+}
+
+bs_status bs_get_info(bs_ctx* c, bs_info* out) {
+    if (!c || !out) return fail(BS_ERR_ARG, "bs_get_info: null argument");
+    const bs_params& p = c->prm;
+    int R = p.resolution * p.supersample * (2 * p.padding + 1);
+    out->nf_res = R;
+    out->det_res = p.resolution;
+    out->n_spheres = (int)c->spheres.size();
+    out->n_waves = p.plane_wave ? 1 : (int)(c->waves.size() / 3);
+    out->uf_lut_r = p.uf_lut_r > 0 ? p.uf_lut_r : 2 * R;
+    out->us_lut_theta = p.us_lut_theta > 0 ? p.us_lut_theta : 1000;
+    const DevBuf* bufs[] = {&c->d_sph, &c->d_waves, &c->d_kw4, &c->d_cones, &c->d_ph, &c->d_A, &c->d_B, &c->d_mie, &c->d_tab,
+                            &c->d_tabscr, &c->d_legP, &c->d_lut, &c->d_uft, &c->d_uftscr, &c->d_fields, &c->d_su,
+                            &c->d_sv, &c->d_mask, &c->d_wx, &c->d_wy, &c->d_wix, &c->d_wiy, &c->d_f1, &c->d_f2,
+                            &c->d_g1, &c->d_I, &c->d_D, &c->d_img};
+    int64_t tot = 0;
+    for (const DevBuf* b : bufs) tot += (int64_t)b->n;
+    out->device_bytes = tot;
+    return BS_OK;
+}
+
+bs_status bs_get_stats(bs_ctx* c, bs_stats* out) {
+    if (!c || !out) return fail(BS_ERR_ARG, "bs_get_stats: null argument");
+    *out = c->stats;
+    return BS_OK;
+}
+
+bs_status bs_get_mie(bs_ctx* c, int32_t sphere, double* A, double* B, int32_t count) {
+    if (!c || !A || !B) return fail(BS_ERR_ARG, "bs_get_mie: null argument");
+    if (!c->have || sphere < 0 || sphere >= (int)c->hs.size() || !c->prm.scalar)
+        return fail(BS_ERR_STATE, "bs_get_mie: no coefficients for sphere %d", sphere);
+    const Sphere& S = c->hs[sphere];
+    if (count < S.Nl + 1) return fail(BS_ERR_ARG, "bs_get_mie: need %d orders", S.Nl + 1);
+    CK(cudaMemcpy(A, c->d_A.as<zd>() + S.coef_off, (S.Nl + 1) * sizeof(zd), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(B, c->d_B.as<zd>() + S.coef_off, (S.Nl + 1) * sizeof(zd), cudaMemcpyDeviceToHost));
+    return BS_OK;
+}
+
+bs_status bs_get_lut(bs_ctx* c, int32_t sphere, int32_t which, double* host, size_t count) {
+    if (!c || !host) return fail(BS_ERR_ARG, "bs_get_lut: null argument");
+    if (!c->have || !c->prm.lut_us || !c->prm.scalar || sphere < 0 || sphere >= (int)c->hs.size())
+        return fail(BS_ERR_STATE, "bs_get_lut: no table for sphere %d", sphere);
+    const Sphere& S = c->hs[sphere];
+    size_t rows = which == 0 ? S.dR : S.aR;
+    size_t n = rows * S.thetaR;
+    if (count < n) return fail(BS_ERR_ARG, "bs_get_lut: need %zu complex values", n);
+    int64_t off = which == 0 ? S.usp_off : S.uip_off;
+    if (c->prec == BS_PREC_FP64) {
+        std::vector<Patch<double>> t(n);
+        CK(cudaMemcpy(t.data(), c->d_lut.as<Patch<double>>() + off, n * sizeof(Patch<double>), cudaMemcpyDeviceToHost));
+        for (size_t i = 0; i < n; i++) {
+            host[2 * i] = t[i].v[0];
+            host[2 * i + 1] = t[i].v[1];
+        }
+    } else {
+        std::vector<Patch<float>> t(n);
+        CK(cudaMemcpy(t.data(), c->d_lut.as<Patch<float>>() + off, n * sizeof(Patch<float>), cudaMemcpyDeviceToHost));
+        for (size_t i = 0; i < n; i++) {
+            host[2 * i] = t[i].v[0];
+            host[2 * i + 1] = t[i].v[1];
+        }
+    }
+    return BS_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,74 @@
+// bs_kernels.h -- launchers of the CUDA kernels (bs_nearfield.cu, bs_detector.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+
+#include "bs_internal.h"
+
+namespace bs {
+
+// Plane waves are processed in chunks of this many (after a Hilbert-curve
+// sort); the host supplies one bounding cone per chunk.
+constexpr int WAVE_CHUNK = 64;
+
+template <class T>
+struct cpx;
+using zd = cpx<double>;
+
+// One bilinear LUT cell at (r, t): {T00, T10 - T00, T01 - T00, T11 - T10 - T01 + T00}
+// as (re, im) pairs, so that T(r + a, t + b) = (v0 + a v1) + b (v2 + a v3).
+template <class T>
+struct alignas(8 * sizeof(T)) Patch {
+    T v[8];
+};
+
+// ---- near field ----
+template <class T>
+void launch_uf(const Scene& sc, const double* tab, cpx<T>* Uf, cudaStream_t st);
+void launch_uf_table(const Scene& sc, double* tab, double* scratch, cudaStream_t st);
+void launch_mie(const Sphere* sph, int ns, double k, zd* scratch, int lstride, zd* A, zd* B, cudaStream_t st);
+void launch_coef_rows(const Sphere& S, double k, const zd* A, const zd* B, zd* tab, double* scratch, cudaStream_t st);
+void launch_legendre_table(int thetaR, int Lmax, double* P, cudaStream_t st);
+template <class T>
+void launch_lut_build(const zd* tab, int rows, int L, const double* P, int Pstride, int thetaR, Patch<T>* out,
+                      cudaStream_t st);
+template <class T>
+void launch_phase(const Scene& sc, const Sphere* sph, const double* waves, cpx<T>* ph, float4* kw4, cudaStream_t st);
+void launch_us_lut_f64(const Scene& sc, const Sphere* sph, int s0, int s1, int accumulate, int finalize,
+                       const double* waves, const zd* ph, const Patch<double>* lut, const zd* Uf, zd* U,
+                       cudaStream_t st);
+void launch_us_lut_f32(const Scene& sc, const Sphere* sph, int s0, int s1, int accumulate, int finalize,
+                       const float4* kw4, const float4* cones, const cpx<float>* ph, const Patch<float>* lut,
+                       const cpx<float>* Uf, cpx<float>* U, cudaStream_t st);
+template <class T>
+void launch_us_direct(const Scene& sc, const Sphere* sph, int lstride, const zd* A, const zd* B, const double* waves,
+                      const cpx<T>* ph, const cpx<T>* Uf, cpx<T>* U, cudaStream_t st);
+template <class T>
+void launch_sum_only(const Scene& sc, const Sphere* sph, const cpx<T>* Uf, cpx<T>* U, cudaStream_t st);
+
+// ---- detector ----
+// twiddles: out[i * ld_i + j * ld_j] = exp(sign 2 pi i ((off_i + i) * freq[j] mod R) / R)
+template <class T>
+void launch_twiddle(int ni, int nj, const int* freq, int off_i, int R, int sign, int ld_i, int ld_j, cpx<T>* out,
+                    cudaStream_t st);
+
+// C[b] (M x N) = A[b] (M x K) * B[b] (K x N), complex, row-major, batch over
+// blockIdx.z with element strides sA, sB, sC (0 = shared operand).
+// epi 0: store; epi 1: multiply by mask[m*N + n]; epi 2: store |scale * c|^2
+// into the real array I[b] (M x N, batch stride sC).
+template <class T>
+void launch_cgemm(int M, int N, int K, int batch, const cpx<T>* A, int lda, long long sA, const cpx<T>* B, int ldb,
+                  long long sB, cpx<T>* C, int ldc, long long sC, int epi, const float* mask, T scale, T* I,
+                  cudaStream_t st);
+
+// D[b][iv][iu] = sum over the ss x ss block of I[b] / ss^2 (fieldslice.cu:71-108)
+template <class T>
+void launch_bin(int res, int ss, int batch, const T* I, T* D, cudaStream_t st);
+
+// image kinds 2, 3: -log10(D/Di), D/Di (microscope.cu:722-775); 0, 1: copies
+template <class T>
+void launch_image(int n, int kind, const T* D, const T* Di, T* out, cudaStream_t st);
+
+}  // namespace bs

@@ -1,0 +1,817 @@
+// bs_nearfield.cu -- near-field kernels: incident field Uf, Mie coefficients,
+// per-sphere lookup tables, and the scattered field Us summed over spheres
+// and Monte Carlo plane waves, with the Uf + Us assembly of nfSumUf.cu fused
+// into the epilogue.
+#include <cuda_runtime.h>
+
+#include <climits>
+
+#include "bs_kernels.h"
+#include "bs_math.cuh"
+
+namespace bs {
+
+// Geometry that feeds a discrete decision (inside/outside a sphere, d == 0,
+// d < 1e-6) is rounded operation by operation in the order of the host
+// restatement, with no fused multiply-add, so the GPU and the double
+// precision reference agree on every boundary pixel.
+__device__ __forceinline__ void pixel_pos(const Scene& sc, int iu, int iv, double p[3]) {
+    // quad::operator()(u, v) = (A + X u) + Y v with u = iu / R (nfScalarUf.cu:66-71)
+    double u = __ddiv_rn((double)iu, (double)sc.R), v = __ddiv_rn((double)iv, (double)sc.R);
+#pragma unroll
+    for (int c = 0; c < 3; c++) p[c] = __dadd_rn(__dadd_rn(sc.A[c], __dmul_rn(sc.X[c], u)), __dmul_rn(sc.Y[c], v));
+}
+
+// |p - c| as sqrt((x*x + y*y) + z*z), each operation rounded separately
+__device__ __forceinline__ double dist_exact(const double p[3], const double c[3], double r[3]) {
+    r[0] = __dsub_rn(p[0], c[0]);
+    r[1] = __dsub_rn(p[1], c[1]);
+    r[2] = __dsub_rn(p[2], c[2]);
+    double s = __dadd_rn(__dadd_rn(__dmul_rn(r[0], r[0]), __dmul_rn(r[1], r[1])), __dmul_rn(r[2], r[2]));
+    return __dsqrt_rn(s);
+}
+
+// ---------------------------------------------------------------------------
+// Incident field (double precision; stored as T)
+// ---------------------------------------------------------------------------
+// gpuScalarUf, nfScalarUf.cu:46-175: Debye-focused field as a Legendre series
+// over l = 0..m with the clamped upward j_l recurrence.
+__device__ zd uf_direct(const Scene& sc, const double p[3]) {
+    double r[3];
+    double d = dist_exact(p, sc.focus, r);
+    if (d < EPS_FLOAT) return mk(sc.amp * 2 * PI_REF * (sc.cos_a - sc.cos_b), 0.0);
+    double inv = 1.0 / d;
+    double cth = sc.kdir[0] * (r[0] * inv) + sc.kdir[1] * (r[1] * inv) + sc.kdir[2] * (r[2] * inv);
+    double kd = sc.kmag * d;
+    double s, c;
+    sincos(kd, &s, &c);
+    double j0 = s / kd, j1 = j0 / kd - c / kd;
+    double P0 = 1, P1 = cth;
+    double a0 = 1, a1 = sc.cos_a, a2 = 1, b0 = 1, b1 = sc.cos_b, b2 = 1;
+    zd sum = mk(0.0, 0.0), il = mk(1.0, 0.0);
+    for (int l = 0; l <= sc.m; l++) {
+        double jl, Pl;
+        if (l == 0) {
+            jl = j0;
+            Pl = P0;
+        } else if (l == 1) {
+            jl = j1;
+            Pl = P1;
+            a2 = a0;
+            legendre_step(l + 1, sc.cos_a, a0, a1);
+            b2 = b0;
+            legendre_step(l + 1, sc.cos_b, b0, b1);
+        } else {
+            sbesselj_step(l, kd, j0, j1);
+            legendre_step(l, cth, P0, P1);
+            jl = j1;
+            Pl = P1;
+            a2 = a0;
+            legendre_step(l + 1, sc.cos_a, a0, a1);
+            b2 = b0;
+            legendre_step(l + 1, sc.cos_b, b0, b1);
+        }
+        double w = jl * Pl * (a1 - a2 - b1 + b2);
+        sum = sum + il * w;
+        il = il * mk(0.0, 1.0);
+    }
+    return sum * (2.0 * PI_REF * sc.amp);
+}
+
+// gpuScalarUfLut, nfScalarUfLut.cu:11-123: j_l(k d) read from the table with
+// linear filtering along d (texture y) and exact order (texture x = l + 0.5).
+__device__ zd uf_lut(const Scene& sc, const double* __restrict__ tab, const double p[3]) {
+    double r[3];
+    double d = dist_exact(p, sc.focus, r);
+    if (d == 0) return mk(sc.amp * 2 * PI_REF * (sc.cos_a - sc.cos_b), 0.0);
+    double inv = 1.0 / d;
+    double cth = sc.kdir[0] * (r[0] * inv) + sc.kdir[1] * (r[1] * inv) + sc.kdir[2] * (r[2] * inv);
+    int L = sc.m + 1;
+    double y = ((d - sc.uf_dmin) / (sc.uf_dmax - sc.uf_dmin)) * (sc.uf_dR - 1);
+    y = fmin(fmax(y, 0.0), (double)(sc.uf_dR - 1));
+    int i0 = (int)floor(y);
+    double be = y - i0;
+    int i1 = min(i0 + 1, sc.uf_dR - 1);
+    const double* t0 = tab + (size_t)i0 * L;
+    const double* t1 = tab + (size_t)i1 * L;
+    double P0 = 1, P1 = cth;
+    double a0 = 1, a1 = sc.cos_a, a2 = 1, b0 = 1, b1 = sc.cos_b, b2 = 1;
+    zd sum = mk(0.0, 0.0), il = mk(1.0, 0.0);
+    for (int l = 0; l <= sc.m; l++) {
+        double jl = (1 - be) * t0[l] + be * t1[l];
+        double Pl;
+        if (l == 0) {
+            Pl = P0;
+        } else {
+            if (l > 1) legendre_step(l, cth, P0, P1);
+            Pl = P1;
+            a2 = a0;
+            legendre_step(l + 1, sc.cos_a, a0, a1);
+            b2 = b0;
+            legendre_step(l + 1, sc.cos_b, b0, b1);
+        }
+        double w = jl * Pl * (a1 - a2 - b1 + b2);
+        sum = sum + il * w;
+        il = il * mk(0.0, 1.0);
+    }
+    return sum * (2.0 * PI_REF * sc.amp);
+}
+
+template <class T>
+__global__ void uf_kernel(Scene sc, const double* __restrict__ tab, cpx<T>* __restrict__ Uf) {
+    int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= sc.R * sc.R) return;
+    double p[3];
+    pixel_pos(sc, idx % sc.R, idx / sc.R, p);
+    zd v;
+    if (!sc.scalar && sc.lut_uf) {
+        v = mk(0.0, 0.0);  // nfVectorUfLut.cu:7-10 is empty
+    } else if (sc.plane_wave) {
+        // gpuScalarUfp, nfScalarUf.cu:9-44
+        double kr = sc.kmag * (sc.kdir[0] * (p[0] - sc.focus[0]) + sc.kdir[1] * (p[1] - sc.focus[1]) +
+                               sc.kdir[2] * (p[2] - sc.focus[2]));
+        double s, c;
+        sincos(kr, &s, &c);
+        v = mk(c * sc.amp, s * sc.amp);
+    } else if (sc.lut_uf) {
+        v = uf_lut(sc, tab, p);
+    } else {
+        v = uf_direct(sc, p);
+    }
+    Uf[idx] = mk((T)v.re, (T)v.im);
+}
+
+// nearfieldStruct::calcBesselLut (nearfield.cpp:222-283): j_l(k d) for
+// d in [dmin, dmax], NaN/Inf replaced by 0 (1 for l = 0 at k d = 0).
+__global__ void uf_table_kernel(Scene sc, double* __restrict__ tab, double* __restrict__ scratch) {
+    int id = blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= sc.uf_dR) return;
+    int L = sc.m + 1;
+    double dr = (sc.uf_dmax - sc.uf_dmin) / (sc.uf_dR - 1);
+    double d = id * dr + sc.uf_dmin;
+    double kd = sc.kmag * d;
+    double* j = tab + (size_t)id * L;
+    double* y = scratch + (size_t)id * L;
+    sph_real(sc.m, kd, j, y, 1);
+    for (int l = 0; l < L; l++) {
+        double v = j[l];
+        if (isnan(v) || isinf(v)) j[l] = (kd == 0 && l == 0) ? 1.0 : 0.0;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Mie coefficients (sphere::calcCoeff, sphere.cpp:21-97), one thread per sphere
+// ---------------------------------------------------------------------------
+__global__ void mie_kernel(const Sphere* __restrict__ sph, int ns, double k, zd* __restrict__ scratch, int lstride,
+                           zd* __restrict__ A, zd* __restrict__ B) {
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= ns) return;
+    Sphere S = sph[s];
+    int N = S.Nl;
+    zd* ja = scratch + (size_t)s * 6 * lstride;
+    zd* ya = ja + lstride;
+    zd* jpa = ya + lstride;
+    zd* ypa = jpa + lstride;
+    zd* jn = ypa + lstride;
+    zd* jpn = jn + lstride;
+    zd n = mk(S.n_re, S.n_im);
+    zd ka = mk(k * S.a, 0.0);
+    zd kna = (n * k) * S.a;
+    sph_complex(N, ka, true, ja, ya, jpa, ypa);
+    sph_complex(N, kna, true, jn, nullptr, jpn, nullptr);
+    for (int l = 0; l <= N; l++) {
+        zd h = mk(ja[l].re - ya[l].im, ja[l].im + ya[l].re);      // j + i y
+        zd hp = mk(jpa[l].re - ypa[l].im, jpa[l].im + ypa[l].re);
+        zd an = ja[l] * hp - jpa[l] * h;
+        zd bn = jn[l] * hp - (h * jpn[l]) * n;
+        zd cn = (ja[l] * jpn[l]) * n - jn[l] * jpa[l];
+        zd f = mk(2.0 * l + 1.0, 0.0) * ipow(l);
+        A[S.coef_off + l] = f * (an / bn);
+        B[S.coef_off + l] = f * (cn / bn);
+    }
+}
+
+// Per-row order coefficients of one sphere:
+//   rows [0, dR):  C_l(r) = B_l (j_l + i y_l)(k r),  r in [r0, dmax]  (sphere.cpp:154-203)
+//   rows [dR, dR+aR): D_l(r) = A_l j_l(k n r),       r in [0, a]      (sphere.cpp:99-152)
+__global__ void coef_rows_kernel(Sphere S, double k, const zd* __restrict__ A, const zd* __restrict__ B,
+                                 zd* __restrict__ tab, double* __restrict__ scratch) {
+    int row = blockIdx.x * blockDim.x + threadIdx.x;
+    int rows = S.dR + S.aR;
+    if (row >= rows) return;
+    int L = S.Nl + 1;
+    zd* out = tab + (size_t)row * L;
+    double* sj = scratch + (size_t)row * 2 * L;
+    if (row < S.dR) {
+        double dr = (S.dmax - S.r0) / (S.dR - 1);
+        double r = row * dr + S.r0;
+        sph_real(S.Nl, k * r, sj, sj + L, 1);
+        for (int l = 0; l < L; l++) out[l] = B[S.coef_off + l] * mk(sj[l], sj[L + l]);
+    } else {
+        int ia = row - S.dR;
+        if (ia == 0) {
+            for (int l = 0; l < L; l++) out[l] = (l == 0) ? A[S.coef_off] * mk(1.0, 0.0) : A[S.coef_off + l] * mk(0.0, 0.0);
+            return;
+        }
+        double da = S.a / (S.aR - 1);
+        double r = ia * da;
+        zd knr = (mk(S.n_re, S.n_im) * k) * r;
+        sph_complex(S.Nl, knr, true, out, nullptr, nullptr, nullptr);
+        for (int l = 0; l < L; l++) out[l] = A[S.coef_off + l] * out[l];
+    }
+}
+
+// P_l(cos theta_t), theta_t = t * PI_REF / (thetaR - 1) (sphere.cu:16-21)
+__global__ void legendre_table_kernel(int thetaR, int Lmax, double* __restrict__ P) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= thetaR) return;
+    double dtheta = PI_REF / (thetaR - 1);
+    double x = cos(dtheta * t);
+    double* row = P + (size_t)t * Lmax;
+    double P0 = 1, P1 = x;
+    row[0] = P0;
+    if (Lmax > 1) row[1] = P1;
+    for (int l = 2; l < Lmax; l++) {
+        legendre_step(l, x, P0, P1);
+        row[l] = P1;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// LUT build: T(r, t) = sum_l coef_l(r) P_l(cos theta_t) (gpuScalarUsp /
+// gpuScalarUip, sphere.cu:4-99), then stored as bilinear patches
+//     {T00, T10 - T00, T01 - T00, T11 - T10 - T01 + T00}
+// at (r, t), with r+1 and t+1 clamped, so that one 32-byte (float) or 64-byte
+// (double) load gives a whole bilinear cell.
+// ---------------------------------------------------------------------------
+constexpr int LB_TR = 8, LB_TT = 32;
+
+template <class T>
+__global__ void __launch_bounds__(256) lut_build_kernel(const zd* __restrict__ tab, int rows, int L,
+                                                        const double* __restrict__ P, int Pstride, int thetaR,
+                                                        Patch<T>* __restrict__ out) {
+    __shared__ zd sv[LB_TR + 1][LB_TT + 1];
+    int r0 = blockIdx.y * LB_TR, t0 = blockIdx.x * LB_TT;
+    for (int e = threadIdx.x; e < (LB_TR + 1) * (LB_TT + 1); e += blockDim.x) {
+        int i = e / (LB_TT + 1), j = e % (LB_TT + 1);
+        int r = min(r0 + i, rows - 1), t = min(t0 + j, thetaR - 1);
+        const zd* c = tab + (size_t)r * L;
+        const double* pl = P + (size_t)t * Pstride;
+        zd acc = mk(0.0, 0.0);
+        for (int l = 0; l < L; l++) acc = acc + c[l] * pl[l];
+        sv[i][j] = acc;
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < LB_TR * LB_TT; e += blockDim.x) {
+        int i = e / LB_TT, j = e % LB_TT;
+        int r = r0 + i, t = t0 + j;
+        if (r >= rows || t >= thetaR) continue;
+        zd a = sv[i][j], b = sv[i + 1][j], c = sv[i][j + 1], d = sv[i + 1][j + 1];
+        Patch<T> pt;
+        pt.v[0] = (T)a.re;
+        pt.v[1] = (T)a.im;
+        pt.v[2] = (T)(b.re - a.re);
+        pt.v[3] = (T)(b.im - a.im);
+        pt.v[4] = (T)(c.re - a.re);
+        pt.v[5] = (T)(c.im - a.im);
+        pt.v[6] = (T)(d.re - b.re - c.re + a.re);
+        pt.v[7] = (T)(d.im - b.im - c.im + a.im);
+        out[(size_t)r * thetaR + t] = pt;
+    }
+}
+
+// Per (sphere, wave): (subA / nk) exp(i k k_w . (p_s - f)) (nfScalarUpLut.cu:71,84,90)
+template <class T>
+__global__ void phase_kernel(Scene sc, const Sphere* __restrict__ sph, const double* __restrict__ waves,
+                             cpx<T>* __restrict__ ph, float4* __restrict__ kw4) {
+    int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx < sc.nk && kw4) {
+        kw4[idx] = make_float4((float)waves[3 * idx], (float)waves[3 * idx + 1], (float)waves[3 * idx + 2], 0.f);
+    }
+    if (idx >= sc.ns * sc.nk) return;
+    int s = idx / sc.nk, w = idx % sc.nk;
+    const double* k = waves + 3 * w;
+    double c0 = sph[s].p[0] - sc.focus[0], c1 = sph[s].p[1] - sc.focus[1], c2 = sph[s].p[2] - sc.focus[2];
+    double arg = sc.kmag * (k[0] * c0 + k[1] * c1 + k[2] * c2);
+    double sn, cs;
+    sincos(arg, &sn, &cs);
+    ph[idx] = mk((T)(sc.wave_amp * cs), (T)(sc.wave_amp * sn));
+}
+
+// ---------------------------------------------------------------------------
+// Scattered field from the LUTs (gpuScalarUpLut, nfScalarUpLut.cu:11-97),
+// all spheres of [s0, s1) in one launch, then Uf added where the pixel is
+// outside every sphere (nfSumUf.cu:6-49).
+// ---------------------------------------------------------------------------
+struct TableSel {
+    int64_t off;
+    int rows;
+    double x;  // fractional row index
+};
+
+__device__ __forceinline__ TableSel select_table(const Sphere& S, double d) {
+    TableSel t;
+    if (d < S.a) {  // internal field, ai = (d - dmin)/(a - dmin) (aR - 1)  (nfScalarUpLut.cu:54)
+        t.off = S.uip_off;
+        t.rows = S.aR;
+        t.x = ((d - S.dmin) / (S.a - S.dmin)) * (S.aR - 1);
+    } else {        // scattered field, di = (d - r0)/(dmax - r0) (dR - 1)  (nfScalarUpLut.cu:53)
+        t.off = S.usp_off;
+        t.rows = S.dR;
+        t.x = ((d - S.r0) / (S.dmax - S.r0)) * (S.dR - 1);
+    }
+    // unnormalised texture coordinates with clamp addressing = clamped index
+    t.x = fmin(fmax(t.x, 0.0), (double)(t.rows - 1));
+    return t;
+}
+
+// plain double precision, one pixel per thread
+__global__ void __launch_bounds__(128) us_lut_f64_kernel(Scene sc, const Sphere* __restrict__ sph, int s0, int s1,
+                                                          int accumulate, int finalize,
+                                                          const double* __restrict__ waves,
+                                                          const zd* __restrict__ ph, const Patch<double>* __restrict__ lut,
+                                                          const zd* __restrict__ Uf, zd* __restrict__ U) {
+    int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= sc.R * sc.R) return;
+    double p[3];
+    pixel_pos(sc, idx % sc.R, idx / sc.R, p);
+    zd total = accumulate ? U[idx] : mk(0.0, 0.0);
+    const double tscale = 1.0 / PI_REF;
+    for (int s = s0; s < s1; s++) {
+        const Sphere& S = sph[s];
+        double r[3];
+        double d = dist_exact(p, S.p, r);
+        TableSel ts = select_table(S, d);
+        int ir = (int)floor(ts.x);
+        double al = ts.x - ir;
+        const Patch<double>* row = lut + ts.off + (size_t)ir * S.thetaR;
+        double rn[3] = {0, 0, 0}, cb = 1.0;  // d == 0: cos(theta) := 1
+        if (d != 0) {
+            rn[0] = r[0] / d;
+            rn[1] = r[1] / d;
+            rn[2] = r[2] / d;
+            cb = 0.0;
+        }
+        double tmax = S.thetaR - 1;
+        zd sum = mk(0.0, 0.0);
+        const zd* phs = ph + (size_t)s * sc.nk;
+        for (int w = 0; w < sc.nk; w++) {
+            const double* k = waves + 3 * w;
+            double c = (d != 0) ? (k[0] * rn[0] + k[1] * rn[1] + k[2] * rn[2]) : cb;
+            c = fmin(fmax(c, -1.0), 1.0);
+            double t = (acos(c) * tscale) * tmax;
+            t = fmin(t, tmax);
+            int it = (int)floor(t);
+            double be = t - it;
+            const Patch<double>& q = row[it];
+            double vr = (q.v[0] + al * q.v[2]) + be * (q.v[4] + al * q.v[6]);
+            double vi = (q.v[1] + al * q.v[3]) + be * (q.v[5] + al * q.v[7]);
+            zd pw = phs[w];
+            sum = sum + pw * mk(vr, vi);
+        }
+        total = total + sum;
+    }
+    if (finalize) {
+        bool outside = true;
+        for (int s = 0; s < sc.ns; s++) {
+            const Sphere& S = sph[s];
+            double r[3];
+            if (dist_exact(p, S.p, r) < S.a) outside = false;
+        }
+        if (outside) total = total + Uf[idx];
+    }
+    U[idx] = total;
+}
+
+// Mixed precision: per-(pixel, sphere) geometry in double, per-wave work in
+// float, per-chunk partial sums combined with Kahan compensation.
+//
+// A block owns a 16 x 16 pixel tile.  Waves arrive sorted along a Hilbert
+// curve and are processed in chunks of WAVE_CHUNK; the host gives each chunk
+// a cone (axis c_k, half-angle beta_k).  For a tile whose pixels all lie
+// outside the sphere and see it within an angle gamma of the tile-centre
+// direction r_c, every lookup angle of the chunk lies in
+//     angle(c_k, r_c) +- (beta_k + gamma)            (triangle inequality),
+// so the LUT rows of the tile times that angular window are copied to shared
+// memory once per chunk and all lookups read shared memory.  Tiles that
+// touch or contain the sphere, or whose window is too large, read the LUT
+// from global memory.
+constexpr int USF_BLOCK = 256;     // 16 x 16 pixel tile
+constexpr int USF_STAGE = 2048;    // LUT patches staged per chunk (64 KB)
+constexpr float USF_MARGIN = 2e-3f;  // radians added to every angular bound
+
+__global__ void __launch_bounds__(USF_BLOCK, 3) us_lut_f32_kernel(Scene sc, const Sphere* __restrict__ sph, int s0, int s1,
+                                                                    int accumulate, int finalize,
+                                                                    const float4* __restrict__ kw4,
+                                                                    const float4* __restrict__ cones,
+                                                                    const cpx<float>* __restrict__ ph,
+                                                                    const Patch<float>* __restrict__ lut,
+                                                                    const cpx<float>* __restrict__ Uf,
+                                                                    cpx<float>* __restrict__ U) {
+    extern __shared__ float4 s_stage[];  // USF_STAGE patches, two float4 each
+    __shared__ float4 s_k[WAVE_CHUNK];
+    __shared__ float2 s_p[WAVE_CHUNK];
+    __shared__ int s_red[4][USF_BLOCK / 32];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    // each warp covers an 8 x 4 pixel block of the 16 x 16 tile
+    const int tiles_u = (sc.R + 15) / 16;
+    const int tu = (blockIdx.x % tiles_u) * 16, tv = (blockIdx.x / tiles_u) * 16;
+    const int iu = tu + (lane & 7) + 8 * (warp & 1);
+    const int iv = tv + (lane >> 3) + 4 * (warp >> 1);
+    const bool valid = iu < sc.R && iv < sc.R;
+    const int idx = iv * sc.R + iu;
+    double p[3];
+    pixel_pos(sc, min(iu, sc.R - 1), min(iv, sc.R - 1), p);
+    // tile centre in single precision (only used for bounds, with margins)
+    float pc[3];
+    {
+        float u = ((float)tu + 7.5f) / (float)sc.R, v = ((float)tv + 7.5f) / (float)sc.R;
+#pragma unroll
+        for (int c = 0; c < 3; c++) pc[c] = (float)sc.A[c] + (float)sc.X[c] * u + (float)sc.Y[c] * v;
+    }
+    float tot_r = 0.f, tot_i = 0.f, cmp_r = 0.f, cmp_i = 0.f;  // Kahan sum over chunk partials
+    if (accumulate && valid) {
+        tot_r = U[idx].re;
+        tot_i = U[idx].im;
+    }
+    const int nchunks = (sc.nk + WAVE_CHUNK - 1) / WAVE_CHUNK;
+    for (int s = s0; s < s1; s++) {
+        const Sphere& S = sph[s];
+        double r[3];
+        double d = dist_exact(p, S.p, r);
+        TableSel ts = select_table(S, d);
+        int ir = (int)floor(ts.x);
+        float al = (float)(ts.x - ir);
+        float rx = 0.f, ry = 0.f, rz = 0.f, cb = 1.f;  // d == 0: cos(theta) := 1
+        if (d != 0) {
+            double inv = 1.0 / d;
+            rx = (float)(r[0] * inv);
+            ry = (float)(r[1] * inv);
+            rz = (float)(r[2] * inv);
+            cb = 0.f;
+        }
+        // ---- tile bounds: rows, angular extent gamma ----
+        float cx = pc[0] - (float)S.p[0], cy = pc[1] - (float)S.p[1], cz = pc[2] - (float)S.p[2];
+        float cl = sqrtf(cx * cx + cy * cy + cz * cz);
+        bool far_ok = valid ? (d >= S.a && d != 0) : true;
+        float gam = 0.f;
+        if (cl > 0.f) {
+            cx /= cl;
+            cy /= cl;
+            cz /= cl;
+            if (valid) gam = acosf(fminf(fmaxf(rx * cx + ry * cy + rz * cz, -1.f), 1.f));
+        } else {
+            far_ok = false;
+        }
+        int rlo = valid ? ir : INT_MAX, rhi = valid ? ir : INT_MIN;
+        rlo = __reduce_min_sync(0xffffffffu, rlo);
+        rhi = __reduce_max_sync(0xffffffffu, rhi);
+        int gbits = (int)__reduce_max_sync(0xffffffffu, (unsigned)__float_as_int(gam));
+        int ok = __all_sync(0xffffffffu, far_ok);
+        __syncthreads();  // s_red reuse across spheres
+        if (lane == 0) {
+            s_red[0][warp] = rlo;
+            s_red[1][warp] = rhi;
+            s_red[2][warp] = gbits;
+            s_red[3][warp] = ok;
+        }
+        __syncthreads();
+        for (int w = 0; w < USF_BLOCK / 32; w++) {
+            rlo = min(rlo, s_red[0][w]);
+            rhi = max(rhi, s_red[1][w]);
+            gbits = max(gbits, s_red[2][w]);
+            ok = ok && s_red[3][w];
+        }
+        const int rows = rhi - rlo + 1;
+        const float gam_all = __int_as_float(gbits) + USF_MARGIN;
+        const bool tile_staged = ok && rows >= 1 && rows <= USF_STAGE / 4;
+        const int lr = min(max(ir - rlo, 0), max(rows, 1) - 1);  // lanes off the slice did not vote
+
+        const float tmax = (float)(S.thetaR - 1);
+        const float tsc = (float)((S.thetaR - 1) / PI_REF);
+        const Patch<float>* table = lut + ts.off;
+        const Patch<float>* row = table + (size_t)ir * S.thetaR;
+        const cpx<float>* phs = ph + (size_t)s * sc.nk;
+        for (int ch = 0; ch < nchunks; ch++) {
+            const int w0 = ch * WAVE_CHUNK;
+            const int nw = min(WAVE_CHUNK, sc.nk - w0);
+            int t_lo = 0, W = 0;
+            bool staged = false;
+            if (tile_staged) {
+                float4 cone = cones[ch];
+                float thc = acosf(fminf(fmaxf(cone.x * cx + cone.y * cy + cone.z * cz, -1.f), 1.f));
+                float lo = thc - cone.w - gam_all, hi = thc + cone.w + gam_all;
+                t_lo = max(0, (int)floorf(lo * tsc) - 1);
+                int t_hi = min(S.thetaR - 1, (int)floorf(hi * tsc) + 1);
+                W = t_hi - t_lo + 1;
+                staged = W >= 1 && rows * W <= USF_STAGE;
+            }
+            __syncthreads();  // previous chunk's readers are done
+            if (threadIdx.x < nw) {
+                s_k[threadIdx.x] = kw4[w0 + threadIdx.x];
+                s_p[threadIdx.x] = make_float2(phs[w0 + threadIdx.x].re, phs[w0 + threadIdx.x].im);
+            }
+            if (staged) {
+                const int n = rows * W;
+                for (int e = threadIdx.x; e < n; e += USF_BLOCK) {
+                    int rr = e / W, tt = e - rr * W;
+                    const float4* src = reinterpret_cast<const float4*>(table + (size_t)(rlo + rr) * S.thetaR + t_lo + tt);
+                    s_stage[2 * e] = __ldg(src);
+                    s_stage[2 * e + 1] = __ldg(src + 1);
+                }
+            }
+            __syncthreads();
+            float ar = 0.f, ai = 0.f;
+            if (staged) {
+                const float4* srow = s_stage + 2 * (lr * W);
+#pragma unroll 4
+                for (int w = 0; w < nw; w++) {
+                    float4 k = s_k[w];
+                    float c = fmaf(k.x, rx, fmaf(k.y, ry, fmaf(k.z, rz, cb)));
+                    c = fminf(fmaxf(c, -1.f), 1.f);
+                    float t = fminf(acosf(c) * tsc, tmax);
+                    float tf = floorf(t);
+                    float be = t - tf;
+                    int lt = min(max((int)tf - t_lo, 0), W - 1);
+                    float4 q0 = srow[2 * lt], q1 = srow[2 * lt + 1];
+                    float vr = fmaf(be, fmaf(al, q1.z, q1.x), fmaf(al, q0.z, q0.x));
+                    float vi = fmaf(be, fmaf(al, q1.w, q1.y), fmaf(al, q0.w, q0.y));
+                    float2 pw = s_p[w];
+                    ar = fmaf(pw.x, vr, fmaf(-pw.y, vi, ar));
+                    ai = fmaf(pw.x, vi, fmaf(pw.y, vr, ai));
+                }
+            } else {
+#pragma unroll 4
+                for (int w = 0; w < nw; w++) {
+                    float4 k = s_k[w];
+                    float c = fmaf(k.x, rx, fmaf(k.y, ry, fmaf(k.z, rz, cb)));
+                    c = fminf(fmaxf(c, -1.f), 1.f);
+                    float t = fminf(acosf(c) * tsc, tmax);
+                    float tf = floorf(t);
+                    float be = t - tf;
+                    const float4* q = reinterpret_cast<const float4*>(row + (int)tf);
+                    float4 q0 = __ldg(q), q1 = __ldg(q + 1);
+                    float vr = fmaf(be, fmaf(al, q1.z, q1.x), fmaf(al, q0.z, q0.x));
+                    float vi = fmaf(be, fmaf(al, q1.w, q1.y), fmaf(al, q0.w, q0.y));
+                    float2 pw = s_p[w];
+                    ar = fmaf(pw.x, vr, fmaf(-pw.y, vi, ar));
+                    ai = fmaf(pw.x, vi, fmaf(pw.y, vr, ai));
+                }
+            }
+            // Kahan: add the chunk partial to the running total
+            float yr = ar - cmp_r, yi = ai - cmp_i;
+            float tr = tot_r + yr, ti = tot_i + yi;
+            cmp_r = (tr - tot_r) - yr;
+            cmp_i = (ti - tot_i) - yi;
+            tot_r = tr;
+            tot_i = ti;
+        }
+    }
+    if (!valid) return;
+    if (finalize) {
+        bool outside = true;
+        for (int s = 0; s < sc.ns; s++) {
+            const Sphere& S = sph[s];
+            double r[3];
+            if (dist_exact(p, S.p, r) < S.a) outside = false;
+        }
+        if (outside) {
+            tot_r += Uf[idx].re - cmp_r;
+            tot_i += Uf[idx].im - cmp_i;
+        }
+    }
+    U[idx] = mk(tot_r, tot_i);
+}
+
+// ---------------------------------------------------------------------------
+// Scattered field by recurrences (--recursive; nfScalarUs.cu:17-95, 201-245,
+// 333-491).  The Bessel recurrences depend on (pixel, sphere) only, so they
+// run once per pair in double and give coefficients c_l:
+//   outside (d > a):  c_l = B_l (j_l + i y_l)(k d)   with the reference clamps
+//   inside  (d <= a): c_l = A_l j_l(k n d)           (c_0 = A_0 only when
+//                                                      Re(k n d) < 1e-6)
+// The per-wave work is then sum_l c_l P_l(k_w . r^).
+// ---------------------------------------------------------------------------
+template <class T>
+__global__ void __launch_bounds__(64) us_direct_kernel(Scene sc, const Sphere* __restrict__ sph, int lstride,
+                                                       const zd* __restrict__ A, const zd* __restrict__ B,
+                                                       const double* __restrict__ waves,
+                                                       const cpx<T>* __restrict__ ph, const cpx<T>* __restrict__ Uf,
+                                                       cpx<T>* __restrict__ U) {
+    extern __shared__ unsigned char smem_raw[];
+    cpx<T>* cl = reinterpret_cast<cpx<T>*>(smem_raw);  // [lstride][blockDim.x]
+    const int tid = threadIdx.x;
+    int idx = blockIdx.x * blockDim.x + tid;
+    bool valid = idx < sc.R * sc.R;
+    if (!valid) idx = sc.R * sc.R - 1;
+    double p[3];
+    pixel_pos(sc, idx % sc.R, idx / sc.R, p);
+    T tot_r = 0, tot_i = 0, cmp_r = 0, cmp_i = 0;
+    bool outside = true;
+    for (int s = 0; s < sc.ns; s++) {
+        const Sphere& S = sph[s];
+        double r[3];
+        double d = dist_exact(p, S.p, r);
+        if (d < S.a) outside = false;
+        int L = S.Nl + 1, Leff = L;
+        const zd* coef;
+        if (d <= S.a) {
+            coef = A + S.coef_off;
+            zd knd = mk(sc.kmag * d * S.n_re, sc.kmag * d * S.n_im);
+            if (knd.re < EPS_FLOAT) {
+                Leff = 1;
+                cl[tid] = mk((T)coef[0].re, (T)coef[0].im);
+            } else {
+                zd j0 = zsin(knd) / knd;
+                zd j1 = j0 / knd - zcos(knd) / knd;
+                for (int l = 0; l < L; l++) {
+                    zd jl;
+                    if (l == 0) {
+                        jl = j0;
+                    } else {
+                        if (l > 1) sbesselj_step_c(l, knd, j0, j1);
+                        jl = j1;
+                    }
+                    zd c = coef[l] * jl;
+                    cl[l * blockDim.x + tid] = mk((T)c.re, (T)c.im);
+                }
+            }
+        } else {
+            coef = B + S.coef_off;
+            double kd = sc.kmag * d;
+            double sn, cs;
+            sincos(kd, &sn, &cs);
+            double j0 = sn / kd, j1 = j0 / kd - cs / kd;
+            double y0 = -cs / kd, y1 = y0 / kd - sn / kd;
+            for (int l = 0; l < L; l++) {
+                double jl, yl;
+                if (l == 0) {
+                    jl = j0;
+                    yl = y0;
+                } else {
+                    if (l > 1) {
+                        sbesselj_step(l, kd, j0, j1);
+                        sbessely_step(l, kd, y0, y1);
+                    }
+                    jl = j1;
+                    yl = y1;
+                }
+                zd c = coef[l] * mk(jl, yl);
+                cl[l * blockDim.x + tid] = mk((T)c.re, (T)c.im);
+            }
+        }
+        // direction cosines; at d == 0 only the l = 0 term remains (inside)
+        T rx = 0, ry = 0, rz = 0;
+        if (d != 0) {
+            rx = (T)(r[0] / d);
+            ry = (T)(r[1] / d);
+            rz = (T)(r[2] / d);
+        }
+        const cpx<T>* phs = ph + (size_t)s * sc.nk;
+        T sr = 0, si = 0;
+        for (int w = 0; w < sc.nk; w++) {
+            const double* k = waves + 3 * w;
+            T x = (T)k[0] * rx + (T)k[1] * ry + (T)k[2] * rz;
+            T Pa = 1, Pb = x;
+            cpx<T> c0 = cl[tid];
+            T ur = c0.re, ui = c0.im;
+            if (Leff > 1) {
+                cpx<T> c1 = cl[blockDim.x + tid];
+                ur += c1.re * Pb;
+                ui += c1.im * Pb;
+                for (int l = 2; l < Leff; l++) {
+                    T Pn = ((2 * l - 1) * x * Pb - (l - 1) * Pa) / l;
+                    Pa = Pb;
+                    Pb = Pn;
+                    cpx<T> cc = cl[l * blockDim.x + tid];
+                    ur += cc.re * Pb;
+                    ui += cc.im * Pb;
+                }
+            }
+            cpx<T> pw = phs[w];
+            sr += pw.re * ur - pw.im * ui;
+            si += pw.re * ui + pw.im * ur;
+        }
+        T yr = sr - cmp_r, yi = si - cmp_i;
+        T tr = tot_r + yr, ti = tot_i + yi;
+        cmp_r = (tr - tot_r) - yr;
+        cmp_i = (ti - tot_i) - yi;
+        tot_r = tr;
+        tot_i = ti;
+    }
+    if (!valid) return;
+    if (outside) {
+        tot_r += Uf[idx].re - cmp_r;
+        tot_i += Uf[idx].im - cmp_i;
+    }
+    U[idx] = mk(tot_r, tot_i);
+}
+
+// Vector stub of the reference: no scattered field, U = Uf outside every sphere.
+template <class T>
+__global__ void sum_only_kernel(Scene sc, const Sphere* __restrict__ sph, const cpx<T>* __restrict__ Uf,
+                                cpx<T>* __restrict__ U) {
+    int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= sc.R * sc.R) return;
+    double p[3];
+    pixel_pos(sc, idx % sc.R, idx / sc.R, p);
+    bool outside = true;
+    for (int s = 0; s < sc.ns; s++) {
+        const Sphere& S = sph[s];
+        double r[3];
+        if (dist_exact(p, S.p, r) < S.a) outside = false;
+    }
+    U[idx] = outside ? Uf[idx] : mk((T)0, (T)0);
+}
+
+// ---------------------------------------------------------------------------
+// Launchers
+// ---------------------------------------------------------------------------
+static inline unsigned blocks_for(long long n, int b) { return (unsigned)((n + b - 1) / b); }
+
+template <class T>
+void launch_uf(const Scene& sc, const double* tab, cpx<T>* Uf, cudaStream_t st) {
+    long long n = (long long)sc.R * sc.R;
+    uf_kernel<T><<<blocks_for(n, 128), 128, 0, st>>>(sc, tab, Uf);
+}
+
+void launch_uf_table(const Scene& sc, double* tab, double* scratch, cudaStream_t st) {
+    uf_table_kernel<<<blocks_for(sc.uf_dR, 128), 128, 0, st>>>(sc, tab, scratch);
+}
+
+void launch_mie(const Sphere* sph, int ns, double k, zd* scratch, int lstride, zd* A, zd* B, cudaStream_t st) {
+    mie_kernel<<<blocks_for(ns, 64), 64, 0, st>>>(sph, ns, k, scratch, lstride, A, B);
+}
+
+void launch_coef_rows(const Sphere& S, double k, const zd* A, const zd* B, zd* tab, double* scratch,
+                      cudaStream_t st) {
+    coef_rows_kernel<<<blocks_for(S.dR + S.aR, 64), 64, 0, st>>>(S, k, A, B, tab, scratch);
+}
+
+void launch_legendre_table(int thetaR, int Lmax, double* P, cudaStream_t st) {
+    legendre_table_kernel<<<blocks_for(thetaR, 128), 128, 0, st>>>(thetaR, Lmax, P);
+}
+
+template <class T>
+void launch_lut_build(const zd* tab, int rows, int L, const double* P, int Pstride, int thetaR, Patch<T>* out,
+                      cudaStream_t st) {
+    dim3 grid(blocks_for(thetaR, LB_TT), blocks_for(rows, LB_TR));
+    lut_build_kernel<T><<<grid, 256, 0, st>>>(tab, rows, L, P, Pstride, thetaR, out);
+}
+
+template <class T>
+void launch_phase(const Scene& sc, const Sphere* sph, const double* waves, cpx<T>* ph, float4* kw4, cudaStream_t st) {
+    long long n = std::max<long long>((long long)sc.ns * sc.nk, sc.nk);
+    phase_kernel<T><<<blocks_for(n, 128), 128, 0, st>>>(sc, sph, waves, ph, kw4);
+}
+
+void launch_us_lut_f64(const Scene& sc, const Sphere* sph, int s0, int s1, int accumulate, int finalize,
+                       const double* waves, const zd* ph, const Patch<double>* lut, const zd* Uf, zd* U,
+                       cudaStream_t st) {
+    long long n = (long long)sc.R * sc.R;
+    us_lut_f64_kernel<<<blocks_for(n, 128), 128, 0, st>>>(sc, sph, s0, s1, accumulate, finalize, waves, ph, lut,
+                                                           Uf, U);
+}
+
+void launch_us_lut_f32(const Scene& sc, const Sphere* sph, int s0, int s1, int accumulate, int finalize,
+                       const float4* kw4, const float4* cones, const cpx<float>* ph, const Patch<float>* lut,
+                       const cpx<float>* Uf, cpx<float>* U, cudaStream_t st) {
+    int tiles = (sc.R + 15) / 16;
+    const int smem = USF_STAGE * (int)sizeof(Patch<float>);
+    static bool configured = false;
+    if (!configured) {
+        cudaFuncSetAttribute(us_lut_f32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        configured = true;
+    }
+    us_lut_f32_kernel<<<(unsigned)tiles * tiles, USF_BLOCK, smem, st>>>(sc, sph, s0, s1, accumulate, finalize, kw4,
+                                                                         cones, ph, lut, Uf, U);
+}
+
+template <class T>
+void launch_us_direct(const Scene& sc, const Sphere* sph, int lstride, const zd* A, const zd* B,
+                      const double* waves, const cpx<T>* ph, const cpx<T>* Uf, cpx<T>* U, cudaStream_t st) {
+    const int bt = 64;
+    size_t smem = (size_t)lstride * bt * sizeof(cpx<T>);
+    if (smem > 48 * 1024)
+        cudaFuncSetAttribute(us_direct_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    long long n = (long long)sc.R * sc.R;
+    us_direct_kernel<T><<<blocks_for(n, bt), bt, smem, st>>>(sc, sph, lstride, A, B, waves, ph, Uf, U);
+}
+
+template <class T>
+void launch_sum_only(const Scene& sc, const Sphere* sph, const cpx<T>* Uf, cpx<T>* U, cudaStream_t st) {
+    long long n = (long long)sc.R * sc.R;
+    sum_only_kernel<T><<<blocks_for(n, 128), 128, 0, st>>>(sc, sph, Uf, U);
+}
+
+#define BS_INST(T)                                                                                              \
+    template void launch_uf<T>(const Scene&, const double*, cpx<T>*, cudaStream_t);                             \
+    template void launch_lut_build<T>(const zd*, int, int, const double*, int, int, Patch<T>*, cudaStream_t);   \
+    template void launch_phase<T>(const Scene&, const Sphere*, const double*, cpx<T>*, float4*, cudaStream_t);  \
+    template void launch_us_direct<T>(const Scene&, const Sphere*, int, const zd*, const zd*, const double*,    \
+                                      const cpx<T>*, const cpx<T>*, cpx<T>*, cudaStream_t);                     \
+    template void launch_sum_only<T>(const Scene&, const Sphere*, const cpx<T>*, cpx<T>*, cudaStream_t);
+BS_INST(float)
+BS_INST(double)
+
+}  // namespace bs

@@ -165,8 +165,24 @@ bs_status bs_get_field(bs_ctx* ctx, bs_field_kind kind, double* host, size_t cou
 bs_status bs_write_envi(bs_ctx* ctx, bs_image_kind kind, const char* path,
                         int32_t append, double band_value);
 
+/* Upper bound on the bytes of per-sphere lookup tables held at once; spheres
+ * beyond it are processed in successive chunks.  0 (default) = 80% of free HBM.
+ * No reference counterpart: the reference allocated one cudaArray per sphere
+ * (nfScalarUpLut.cu:388-399). */
+bs_status bs_set_lut_budget(bs_ctx* ctx, size_t bytes);
+
 bs_status bs_get_info(bs_ctx* ctx, bs_info* out);
 bs_status bs_get_stats(bs_ctx* ctx, bs_stats* out);
+
+/* Mie coefficients A_l, B_l (l = 0..Nl) of one sphere from the last run, as
+ * interleaved complex doubles; sphere::A / sphere::B (sphere.h:39-43). */
+bs_status bs_get_mie(bs_ctx* ctx, int32_t sphere, double* A, double* B, int32_t count);
+
+/* Lookup table of one sphere from the last run (which = 0: Usp, dR x thetaR;
+ * 1: Uip, aR x thetaR), radial-major interleaved complex doubles; the values
+ * of sphere::Usp / sphere::Uip (sphere.cpp:222-272, sphere.cu:4-99).  Valid
+ * for spheres of the last table chunk. */
+bs_status bs_get_lut(bs_ctx* ctx, int32_t sphere, int32_t which, double* host, size_t count);
 
 #ifdef __cplusplus
 }

@@ -1,0 +1,202 @@
+"""GPU path vs the oracle, through the C ABI.
+
+Tolerances (relative L2, ||gpu - oracle|| / ||oracle||):
+  * FP64 path: 1e-10 on every output (near fields, Mie coefficients, LUTs, detector images)
+  * mixed path: 1e-5 on the detector images and 1e-4 on the near field
+"""
+import numpy as np
+import pytest
+
+import oracle_lib
+from bimsim_gb300 import (BS_FIELD_INCIDENT, BS_FIELD_TOTAL, BS_IMG_ABSORBANCE, BS_IMG_INCIDENT, BS_IMG_INTENSITY,
+                          BS_IMG_TRANSMITTANCE, BS_PREC_FP64, BS_PREC_MIXED, Context, abi, scenes)
+
+pytestmark = pytest.mark.gpu
+
+TOL64 = 1e-10
+TOL_MIXED_IMG = 1e-5
+TOL_MIXED_FIELD = 1e-4
+
+
+def rel(a, b):
+    return float(np.linalg.norm((np.asarray(a) - np.asarray(b)).ravel()) / max(np.linalg.norm(np.asarray(b).ravel()), 1e-300))
+
+
+def scene(name):
+    w = scenes.mc_waves
+    if name == "lut":
+        p = abi.make_params(lam=3.0, condenser=(0, 0.5), objective=(0, 0.5), xy=(16, 0), resolution=16, padding=1,
+                            us_lut_theta=200)
+        s = [(0, 0, 0, 2.5, 1.4, 0.05), (4.5, -3.0, 0.8, 1.1, 1.55, 0.01), (-5.0, 4.0, -1.5, 1.8, 1.25, 0.0)]
+        return p, s, w(40, 0, 0.5, seed=3)
+    if name == "lut_ufLUT":
+        p = abi.make_params(lam=3.0, condenser=(0.1, 0.5), objective=(0.05, 0.45), xy=(14, 0.5), resolution=16,
+                            padding=1, lut_uf=True, us_lut_r=150, us_lut_theta=128, uf_lut_r=200)
+        s = [(1.0, 0.5, 0.0, 2.0, 1.45, 0.03), (-4.0, -3.5, 0.2, 1.3, 1.3, 0.02)]
+        return p, s, w(32, 0.1, 0.5, seed=4)
+    if name == "direct_cfg1":
+        # config 1 at reduced size: ka = 12.57 > 12 exercises cbessjy.cpp:541
+        p = abi.make_params(lam=2.5, condenser=(0, 0.5), objective=(0, 0.5), xy=(20, 0), resolution=12, padding=2,
+                            lut_us=False)
+        return p, [(0, 0, 0, 5.0, 1.4, 0.05)], w(24, 0, 0.5, seed=1)
+    if name == "direct_multi":
+        p = abi.make_params(lam=3.0, condenser=(0, 0.6), objective=(0, 0.6), xy=(16, 0), resolution=16, padding=1,
+                            lut_us=False, lut_uf=True)
+        s = [(0.3, -0.2, 0, 2.2, 1.5, 0.04), (5.0, 4.0, 1.0, 1.0, 1.3, 0.0)]
+        return p, s, w(20, 0, 0.6, seed=5)
+    if name == "plane_wave":
+        p = abi.make_params(lam=2.0, condenser=(0, 0.5), objective=(0, 0.8), xy=(12, 0), resolution=16, padding=1,
+                            plane_wave=True, us_lut_theta=256)
+        return p, [(0.5, 0.0, 0.0, 2.0, 1.4, 0.02)], None
+    if name == "oblique_xz":
+        k = (np.sin(0.3), 0.0, np.cos(0.3))
+        p = abi.make_params(lam=2.5, k_dir=k, condenser=(0, 0.4), objective=(0, 0.5),
+                            plane=((-6, 0, -6), (6, 0, 6), (0, -1, 0)), resolution=12, padding=1, us_lut_theta=180)
+        return p, [(0.0, 1.0, 0.0, 1.6, 1.35, 0.02)], w(28, 0, 0.4, seed=6, kdir=k)
+    if name == "vector":
+        p = abi.make_params(lam=3.0, condenser=(0, 0.5), objective=(0, 0.5), xy=(12, 0), resolution=12, padding=1,
+                            scalar=False)
+        return p, [(0, 0, 0, 2.0, 1.4, 0.05)], w(16, 0, 0.5, seed=7)
+    if name == "no_spheres":
+        p = abi.make_params(lam=3.0, condenser=(0, 0.5), objective=(0, 0.5), xy=(12, 0), resolution=12, padding=1)
+        return p, [], w(16, 0, 0.5, seed=8)
+    if name == "supersample":
+        # s/res = 6/6 > lambda/2 -> ss = ceil(2 s / (res lambda)) = 2 (arguments.h:411-418)
+        p = abi.make_params(lam=1.5, condenser=(0, 0.5), objective=(0, 0.5), xy=(6, 0), resolution=6, padding=1,
+                            us_lut_theta=128)
+        assert p.supersample == 2
+        return p, [(0.2, 0.1, 0.0, 1.0, 1.4, 0.05)], w(16, 0, 0.5, seed=9)
+    raise KeyError(name)
+
+
+ALL = ["lut", "lut_ufLUT", "direct_cfg1", "direct_multi", "plane_wave", "oblique_xz", "vector", "no_spheres",
+       "supersample"]
+_oracle_cache = {}
+
+
+def oracle_result(name):
+    if name not in _oracle_cache:
+        p, s, waves = scene(name)
+        arr, ns = abi.sphere_array(s)
+        w = waves if waves is not None else np.zeros((0, 3))
+        _oracle_cache[name] = oracle_lib.simulate(p, arr, ns, w)
+    return _oracle_cache[name]
+
+
+def run_gpu(name, prec, budget=0):
+    p, s, waves = scene(name)
+    ctx = Context(p)
+    ctx.set_spheres(s)
+    if waves is not None:
+        ctx.set_waves(waves)
+    if budget:
+        ctx.set_lut_budget(budget)
+    ctx.simulate(prec)
+    out = dict(U=ctx.field(BS_FIELD_TOTAL), Uf=ctx.field(BS_FIELD_INCIDENT),
+               D=ctx.image(BS_IMG_INTENSITY, f64=True), Di=ctx.image(BS_IMG_INCIDENT, f64=True),
+               A=ctx.image(BS_IMG_ABSORBANCE, f64=True), T=ctx.image(BS_IMG_TRANSMITTANCE, f64=True),
+               stats=ctx.stats())
+    ctx.close()
+    return out
+
+
+@pytest.mark.parametrize("name", ALL)
+def test_fp64_matches_oracle(name):
+    U, Uf, D, Di = oracle_result(name)
+    g = run_gpu(name, BS_PREC_FP64)
+    errs = {"Uf": rel(g["Uf"], Uf), "U": rel(g["U"], U), "D": rel(g["D"], D), "Di": rel(g["Di"], Di)}
+    assert max(errs.values()) <= TOL64, errs
+    assert g["stats"].kernel_launches > 0
+
+
+@pytest.mark.parametrize("name", ALL)
+def test_mixed_matches_oracle(name):
+    U, Uf, D, Di = oracle_result(name)
+    g = run_gpu(name, BS_PREC_MIXED)
+    img = {"D": rel(g["D"], D), "Di": rel(g["Di"], Di)}
+    fld = {"U": rel(g["U"], U), "Uf": rel(g["Uf"], Uf)}
+    assert max(img.values()) <= TOL_MIXED_IMG, (img, fld)
+    assert max(fld.values()) <= TOL_MIXED_FIELD, (img, fld)
+
+
+def test_images_are_derived_consistently():
+    _, _, D, Di = oracle_result("lut")
+    g = run_gpu("lut", BS_PREC_FP64)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        assert rel(g["A"], -np.log10(D / Di)) <= TOL64
+        assert rel(g["T"], D / Di) <= TOL64
+
+
+def test_zero_spheres_total_equals_incident():
+    g = run_gpu("no_spheres", BS_PREC_FP64)
+    assert np.array_equal(g["U"], g["Uf"])
+    assert np.array_equal(g["D"], g["Di"])
+
+
+def test_mie_coefficients_fp64():
+    p, s, waves = scene("direct_cfg1")
+    with Context(p) as ctx:
+        ctx.set_spheres(s)
+        ctx.set_waves(waves)
+        ctx.simulate(BS_PREC_FP64)
+        nl = oracle_lib.load().bso_calc_nl(s[0][3], p.lambda_)
+        A, B = ctx.mie(0, nl)
+    Ao = np.zeros(2 * nl + 2)
+    Bo = np.zeros(2 * nl + 2)
+    g = oracle_lib.geom(p)
+    oracle_lib.load().bso_mie(g.kmag, s[0][3], s[0][4], s[0][5], nl, oracle_lib.P(Ao), oracle_lib.P(Bo))
+    assert rel(A, Ao.view(np.complex128)) <= 1e-12
+    assert rel(B, Bo.view(np.complex128)) <= 1e-12
+
+
+@pytest.mark.parametrize("prec,tol", [(BS_PREC_FP64, 1e-12), (BS_PREC_MIXED, 1e-6)])
+def test_lut_tables(prec, tol):
+    p, s, waves = scene("lut")
+    lib = oracle_lib.load()
+    with Context(p) as ctx:
+        ctx.set_spheres(s)
+        ctx.set_waves(waves)
+        ctx.simulate(prec)
+        for i, sp in enumerate(s):
+            sg = oracle_lib.sphere_geom(p, abi.Sphere(*sp))
+            usp = np.zeros(2 * sg.dR * sg.thetaR)
+            uip = np.zeros(2 * sg.aR * sg.thetaR)
+            lib.bso_sphere_luts(oracle_lib.C.byref(p), oracle_lib.C.byref(abi.Sphere(*sp)), oracle_lib.P(usp),
+                                oracle_lib.P(uip))
+            gu = ctx.lut(i, 0, sg.dR, sg.thetaR)
+            gi = ctx.lut(i, 1, sg.aR, sg.thetaR)
+            assert rel(gu, usp.view(np.complex128).reshape(sg.dR, sg.thetaR)) <= tol
+            assert rel(gi, uip.view(np.complex128).reshape(sg.aR, sg.thetaR)) <= tol
+
+
+def test_chunked_tables_match_single_pass():
+    """A LUT budget that holds one sphere at a time gives the same slice."""
+    full = run_gpu("lut", BS_PREC_FP64)
+    p, s, _ = scene("lut")
+    one = max(oracle_lib.sphere_geom(p, abi.Sphere(*sp)).dR for sp in s) * 200 * 64 * 2
+    chunked = run_gpu("lut", BS_PREC_FP64, budget=one)
+    assert rel(chunked["U"], full["U"]) <= 1e-14
+    assert rel(chunked["D"], full["D"]) <= 1e-14
+
+
+def test_repeatable():
+    a = run_gpu("lut", BS_PREC_MIXED)
+    b = run_gpu("lut", BS_PREC_MIXED)
+    assert np.array_equal(a["U"], b["U"]) and np.array_equal(a["D"], b["D"])
+
+
+def test_compat_sampler_matches_reference_rule():
+    """bs_sample_waves_compat reproduces the oracle's restatement of mcSampleNA."""
+    p, s, _ = scene("lut")
+    with Context(p) as ctx:
+        ctx.set_spheres(s)
+        ctx.sample_waves_compat(64)
+        ctx.simulate(BS_PREC_FP64)
+        D = ctx.image(BS_IMG_INTENSITY, f64=True)
+    lib = oracle_lib.load()
+    w = np.zeros(3 * 64)
+    kd = np.array(p.k_dir[:])
+    lib.bso_mc_sample(64, oracle_lib.P(kd), p.condenser[0], p.condenser[1], oracle_lib.P(w))
+    arr, ns = abi.sphere_array(s)
+    _, _, Do, _ = oracle_lib.simulate(p, arr, ns, w.reshape(-1, 3))
+    assert rel(D, Do) <= TOL64
