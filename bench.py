@@ -1,0 +1,310 @@
+"""Benchmark: field-slice pixels/s of the near-field-to-detector path.
+
+Workload (one "step" = one full slice): the 1024^2-detector scene with 50
+spheres over 100 um, lambda 3 um, 1000 Monte Carlo plane waves, scalar LUT
+mode with the incident-field LUT, LUTs of 4096 radial x 1024 angular samples,
+padding 1 (near field 3072^2), mixed precision.  Seeded synthetic scene
+(bimsim_gb300.scenes.config2); the reference publishes no dataset.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+N > 1 runs under torch.distributed.run as independent replicas (one slice per
+rank per step, no collective in the data path; weak scaling).  `--impl
+reference` times the CPU implementation of the path (the double-precision
+restatement in oracle/; the reference's own GPU code cannot be built, see
+the design doc) on a bounded band of near-field rows and extrapolates.
+"""
+import argparse
+import json
+import math
+import os
+import re
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(REPO, "bimsim-cuda_gb300"))
+
+METRIC = "field-slice pixels/s (1024², 50 spheres) & served p50/p99, mixed vs FP64 at 1e-5"
+FLOP_PER_LOOKUP = 30  # (pixel, sphere, wave) interaction of the Us LUT stage
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi samples during the timed region (SM clock, throttle reasons)."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def profile_traffic():
+    """DRAM bytes per launch of the dominant kernel from the committed ncu summary."""
+    path = os.path.join(REPO, "profiles", "us_lut_tex_config2.md")
+    try:
+        m = re.search(r"traffic_bytes_per_launch:\s*([0-9.eE+]+)", open(path).read())
+        return float(m.group(1)) if m else None
+    except OSError:
+        return None
+
+
+def measured_peaks():
+    try:
+        return json.load(open(os.path.join(REPO, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        return {}
+
+
+def cpu_reference(p, spheres, waves, rows, threads):
+    """Time the CPU implementation (oracle) on `rows` near-field rows of the
+    slice through all spheres and waves; tables warmed first.  Returns
+    (seconds for the band, R)."""
+    sys.path.insert(0, os.path.join(REPO, "tests"))
+    import numpy as np
+
+    import oracle_lib
+    from bimsim_gb300 import abi
+    lib = oracle_lib.load()
+    g = oracle_lib.geom(p)
+    R = g.R
+    row0 = R // 2 - rows // 2
+    arr, ns = abi.sphere_array(spheres)
+    w = np.ascontiguousarray(waves, dtype=np.float64).reshape(-1)
+    out = np.zeros(2 * rows * R)
+    t0 = time.perf_counter()
+    lib.bso_nearfield_rows(oracle_lib.C.byref(p), arr, ns, oracle_lib.P(w), len(w) // 3, threads, row0, row0 + rows,
+                           oracle_lib.P(out))
+    return time.perf_counter() - t0, R
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    from bimsim_gb300 import scenes
+    p, spheres, waves = scenes.config2()
+    threads = os.cpu_count() or 1
+    rows = args.ref_rows
+    per = []
+    for i in range(args.warmup + args.steps):
+        dt, R = cpu_reference(p, spheres, waves, rows, threads)
+        if i >= args.warmup:
+            per.append(dt)
+    t_band = statistics.median(per)
+    t_slice = t_band * R / rows
+    value = R * R / t_slice
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "pixels/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_slice * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+        "config": {"workload": "config2: 1024^2 detector, 50 spheres, 1000 waves, LUT 4096x1024, near field 3072^2",
+                   "sample": f"{rows} of {R} near-field rows through all spheres and waves, scaled by {R}/{rows}"},
+        "cpu_baseline": {"value": value, "unit": "pixels/s", "cores": threads, "kind": "port",
+                         "sample": f"{rows} near-field rows x 50 spheres x 1000 waves per step, extrapolated"},
+        "e2e": {"value": value, "unit": "pixels/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def run_gb300(args):
+    import numpy as np
+    import torch
+
+    from bimsim_gb300 import BS_IMG_ABSORBANCE, BS_IMG_INTENSITY, BS_PREC_FP64, BS_PREC_MIXED, Context, scenes
+    from bimsim_gb300.lib import measure_fma_peak
+
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    else:
+        dist = None
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    p, spheres, waves = scenes.config2()
+    ctx = Context(p)
+    ctx.set_spheres(spheres)
+    ctx.set_waves(waves)
+    R = ctx.info().nf_res
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)  # > L2 (126 MB)
+
+    def barrier():
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+
+    for _ in range(args.warmup):
+        ctx.simulate(BS_PREC_MIXED)
+    # ---- device-resident timing (inputs already in HBM) ----
+    sampler = ClockSampler(local)
+    sampler.start()
+    times, us_ms, launches = [], [], 0
+    for _ in range(args.steps):
+        flush.fill_(1.0)  # L2 flushed between timed steps
+        barrier()
+        t0 = time.perf_counter()
+        ctx.simulate(BS_PREC_MIXED)
+        torch.cuda.synchronize()
+        times.append(time.perf_counter() - t0)
+        st = ctx.stats()
+        us_ms.append(st.ms_us)
+        launches += st.kernel_launches
+    clocks = sampler.stop()
+    total = sum(times)
+    if dist:
+        t = torch.tensor([total], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total = float(t.item())
+    value = ws * args.steps * R * R / total
+    # ---- end to end through the C ABI with host buffers ----
+    pinned_waves = torch.from_numpy(np.ascontiguousarray(waves)).pin_memory()
+    img = torch.empty((p.resolution, p.resolution), dtype=torch.float32).pin_memory()
+    e2e_times = []
+    d2h = 2 * p.resolution * p.resolution * 4
+    h2d = len(spheres) * 48 + waves.size * 8
+    for _ in range(max(1, args.steps)):
+        flush.fill_(1.0)
+        barrier()
+        t0 = time.perf_counter()
+        ctx.set_spheres(spheres)
+        ctx.set_waves(pinned_waves.numpy())
+        ctx.simulate(BS_PREC_MIXED)
+        a = ctx.image(BS_IMG_INTENSITY)
+        b = ctx.image(BS_IMG_ABSORBANCE)
+        img.copy_(torch.from_numpy(a))
+        e2e_times.append(time.perf_counter() - t0)
+    e2e_total = sum(e2e_times)
+    if dist:
+        t = torch.tensor([e2e_total], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_total = float(t.item())
+    e2e_value = ws * len(e2e_times) * R * R / e2e_total
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+    if rank != 0:
+        return
+    # ---- roofline of the dominant kernel (Us LUT apply) ----
+    fp32_tf, fp64_tf = measure_fma_peak()
+    ns, nk = len(spheres), waves.shape[0]
+    lookups = R * R * ns * nk
+    us_s = statistics.median(us_ms) * 1e-3
+    achieved = FLOP_PER_LOOKUP * lookups / us_s / 1e12
+    # ---- accuracy: mixed vs FP64 on the same scene at 256^2 (FP64 at 1024^2 takes minutes) ----
+    ps, ss, wv = scenes.config2(resolution=256, fov=25.0, n_spheres=8, samples=200)
+    with Context(ps) as c2:
+        c2.set_spheres(ss)
+        c2.set_waves(wv)
+        c2.simulate(BS_PREC_FP64)
+        ref = c2.image(BS_IMG_INTENSITY, f64=True)
+        c2.simulate(BS_PREC_MIXED)
+        mix = c2.image(BS_IMG_INTENSITY, f64=True)
+    rel = float(np.linalg.norm(mix - ref) / np.linalg.norm(ref))
+    # ---- CPU baseline (oracle on a bounded band of rows) ----
+    cpu = None
+    if not args.no_cpu:
+        rows = args.ref_rows
+        dt, Rr = cpu_reference(p, spheres, waves, rows, os.cpu_count() or 1)
+        cpu = {"value": Rr * Rr / (dt * Rr / rows), "unit": "pixels/s", "cores": os.cpu_count() or 1,
+               "kind": "port",
+               "sample": f"{rows} of {Rr} near-field rows x 50 spheres x 1000 waves, double precision, "
+                         f"scaled by {Rr}/{rows}"}
+    peaks = measured_peaks()
+    line = {
+        "metric": METRIC, "value": value, "unit": "pixels/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total / args.steps * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 (FP64 tables and geometry)",
+        "data": "synthetic (seeded Philox scene and waves)",
+        "config": {"workload": "config2: 1024^2 detector over 100 um, 50 spheres a~U(1,5) n~U(1.2,1.6)+iU(0,.05), "
+                               "lambda 3 um, 1000 MC waves, scalar LUT + Uf LUT, LUT 4096x1024, near field 3072^2",
+                   "precision": "mixed", "l2": "flushed between timed steps (256 MB write); LUTs 1.6 GB > L2",
+                   "parallelism": f"replicas x{ws}"},
+        "e2e": {"value": e2e_value, "unit": "pixels/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": launches,
+        "roofline": {"bound": "fp32", "kernel": "us_lut_tex_kernel", "achieved": achieved,
+                     "peak": fp32_tf, "unit": "TFLOP/s", "frac": achieved / fp32_tf,
+                     "traffic": profile_traffic(),
+                     "peak_source": "measured FP32 FMA loop on this GPU (bs_measure_fma_peak)",
+                     "work": f"{FLOP_PER_LOOKUP} flop x {lookups} (pixel, sphere, wave) lookups per launch",
+                     "launch_ms": us_s * 1e3, "lookups_per_s": lookups / us_s,
+                     "hbm_peak_gbs": peaks.get("hbm_gbs"), "fp64_peak_tflops": fp64_tf},
+        "mixed_vs_fp64_rel_l2": {"value": rel, "tolerance": 1e-5,
+                                 "case": "intensity image, same scene family at 256^2, 8 spheres, 200 waves"},
+        "clocks": clocks,
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--ref-rows", type=int, default=int(os.environ.get("BS_REF_ROWS", "12")))
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gb300(args)
+
+
+if __name__ == "__main__":
+    main()

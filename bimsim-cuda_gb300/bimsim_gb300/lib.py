@@ -49,6 +49,7 @@ def library():
         "bs_get_stats": ([vp, vp], C.c_int),
         "bs_get_mie": ([vp, i32, vp, vp, i32], C.c_int),
         "bs_get_lut": ([vp, i32, i32, vp, sz], C.c_int),
+        "bs_measure_fma_peak": ([vp, vp], C.c_int),
     }
     for name, (args, res) in proto.items():
         f = getattr(lib, name)
@@ -56,6 +57,16 @@ def library():
         f.restype = res
     _LIB = lib
     return lib
+
+
+def measure_fma_peak():
+    """(fp32, fp64) FMA throughput of the current GPU in TFLOP/s."""
+    lib = library()
+    a, b = C.c_double(), C.c_double()
+    st = lib.bs_measure_fma_peak(C.byref(a), C.byref(b))
+    if st != 0:
+        raise BimsimError(st, "FMA peak measurement failed")
+    return a.value, b.value
 
 
 def _p(a):

@@ -91,6 +91,58 @@ bool valid_params(const bs_params* p, std::string& why) {
     return true;
 }
 
+// One sphere's tables for the mixed path: real and imaginary float planes of
+// Usp (thetaR x dR) and Uip (thetaR x aR) in CUDA arrays, with a surface
+// object per plane for the build and a texture object per plane for the
+// gathers.  Index k: 0 Usp re, 1 Usp im, 2 Uip re, 3 Uip im.
+struct TexSlot {
+    cudaArray_t arr[4] = {};
+    cudaTextureObject_t tex[4] = {};
+    cudaSurfaceObject_t surf[4] = {};
+    int w = 0, h[4] = {0, 0, 0, 0};
+
+    void release() {
+        for (int k = 0; k < 4; k++) {
+            if (tex[k]) cudaDestroyTextureObject(tex[k]);
+            if (surf[k]) cudaDestroySurfaceObject(surf[k]);
+            if (arr[k]) cudaFreeArray(arr[k]);
+            tex[k] = surf[k] = 0;
+            arr[k] = nullptr;
+            h[k] = 0;
+        }
+        w = 0;
+    }
+
+    // (re)allocate plane k with at least `rows` rows of `width` floats
+    cudaError_t ensure(int k, int width, int rows) {
+        if (arr[k] && w == width && h[k] >= rows) return cudaSuccess;
+        if (tex[k]) cudaDestroyTextureObject(tex[k]);
+        if (surf[k]) cudaDestroySurfaceObject(surf[k]);
+        if (arr[k]) cudaFreeArray(arr[k]);
+        tex[k] = surf[k] = 0;
+        arr[k] = nullptr;
+        cudaChannelFormatDesc fd = cudaCreateChannelDesc<float>();
+        cudaError_t e = cudaMallocArray(&arr[k], &fd, width, rows, cudaArraySurfaceLoadStore | cudaArrayTextureGather);
+        if (e != cudaSuccess) return e;
+        cudaResourceDesc rd = {};
+        rd.resType = cudaResourceTypeArray;
+        rd.res.array.array = arr[k];
+        e = cudaCreateSurfaceObject(&surf[k], &rd);
+        if (e != cudaSuccess) return e;
+        cudaTextureDesc td = {};
+        td.addressMode[0] = cudaAddressModeClamp;
+        td.addressMode[1] = cudaAddressModeClamp;
+        td.filterMode = cudaFilterModePoint;
+        td.readMode = cudaReadModeElementType;
+        td.normalizedCoords = 0;
+        e = cudaCreateTextureObject(&tex[k], &rd, &td, nullptr);
+        if (e != cudaSuccess) return e;
+        w = width;
+        h[k] = rows;
+        return cudaSuccess;
+    }
+};
+
 }  // namespace
 
 struct bs_ctx {
@@ -110,10 +162,12 @@ struct bs_ctx {
     int prec = -1;
     bool have = false;
 
-    DevBuf d_sph, d_waves, d_kw4, d_cones, d_ph, d_A, d_B, d_mie, d_tab, d_tabscr, d_legP, d_lut, d_uft, d_uftscr;
+    DevBuf d_sph, d_waves, d_kw4, d_ph, d_A, d_B, d_mie, d_tab, d_tabscr, d_legP, d_lut, d_uft, d_uftscr;
     DevBuf d_fields;  // [2][R*R] U then Uf
     DevBuf d_su, d_sv, d_mask, d_wx, d_wy, d_wix, d_wiy, d_f1, d_f2, d_g1, d_I, d_D, d_img;
     int legP_theta = 0, legP_L = 0;
+    std::vector<TexSlot> slots;  // mixed-path tables, one per sphere of a chunk
+    DevBuf d_texobj;
     int64_t launches = 0;
     int64_t interactions = 0;
     bs_stats stats{};
@@ -147,11 +201,13 @@ bs_status bs_create(const bs_params* params, bs_ctx** out) {
 bs_status bs_destroy(bs_ctx* c) {
     if (!c) return BS_OK;
     if (c->st) cudaStreamSynchronize(c->st);
-    DevBuf* bufs[] = {&c->d_sph, &c->d_waves, &c->d_kw4, &c->d_cones, &c->d_ph, &c->d_A, &c->d_B, &c->d_mie, &c->d_tab,
+    DevBuf* bufs[] = {&c->d_sph, &c->d_waves, &c->d_kw4, &c->d_ph, &c->d_A, &c->d_B, &c->d_mie, &c->d_tab,
                       &c->d_tabscr, &c->d_legP, &c->d_lut, &c->d_uft, &c->d_uftscr, &c->d_fields, &c->d_su,
                       &c->d_sv, &c->d_mask, &c->d_wx, &c->d_wy, &c->d_wix, &c->d_wiy, &c->d_f1, &c->d_f2,
                       &c->d_g1, &c->d_I, &c->d_D, &c->d_img};
     for (DevBuf* b : bufs) b->release();
+    for (auto& sl : c->slots) sl.release();
+    c->d_texobj.release();
     for (int i = 0; i < 6; i++)
         if (c->ev[i]) cudaEventDestroy(c->ev[i]);
     if (c->st) cudaStreamDestroy(c->st);
@@ -449,33 +505,6 @@ static void sort_waves(std::vector<double>& w) {
     w.swap(out);
 }
 
-// Bounding cone (unit axis, half-angle in radians) of every WAVE_CHUNK
-// consecutive waves, with a small margin for single-precision rounding.
-static std::vector<float4> wave_cones(const std::vector<double>& w) {
-    size_t nk = w.size() / 3;
-    size_t nch = (nk + WAVE_CHUNK - 1) / WAVE_CHUNK;
-    std::vector<float4> out(nch);
-    for (size_t ch = 0; ch < nch; ch++) {
-        size_t a = ch * WAVE_CHUNK, b = std::min(nk, a + WAVE_CHUNK);
-        double m[3] = {0, 0, 0};
-        for (size_t i = a; i < b; i++)
-            for (int c = 0; c < 3; c++) m[c] += w[3 * i + c];
-        double ml = std::sqrt(m[0] * m[0] + m[1] * m[1] + m[2] * m[2]);
-        if (ml > 0)
-            for (int c = 0; c < 3; c++) m[c] /= ml;
-        double beta = 0;
-        for (size_t i = a; i < b; i++) {
-            const double* k = &w[3 * i];
-            double kl = std::sqrt(k[0] * k[0] + k[1] * k[1] + k[2] * k[2]);
-            double cth = (k[0] * m[0] + k[1] * m[1] + k[2] * m[2]) / (kl > 0 ? kl : 1);
-            beta = std::max(beta, std::acos(std::min(1.0, std::max(-1.0, cth))));
-        }
-        if (!(ml > 0)) beta = TRUE_PI;
-        out[ch] = make_float4((float)m[0], (float)m[1], (float)m[2], (float)(beta + 1e-4));
-    }
-    return out;
-}
-
 // ---------------------------------------------------------------------------
 // The near field
 // ---------------------------------------------------------------------------
@@ -512,7 +541,7 @@ static bs_status run_nearfield(bs_ctx* c) {
     std::vector<int> chunk_start;
     size_t pool = 0, maxrows = 0, maxL = 0;
     if (p.scalar && p.lut_us && ns > 0) {
-        bs_status pst = plan_luts(c, fp64 ? sizeof(Patch<double>) : sizeof(Patch<float>), chunk_start, pool, maxrows, maxL);
+        bs_status pst = plan_luts(c, fp64 ? sizeof(Patch<double>) : 2 * sizeof(float), chunk_start, pool, maxrows, maxL);
         if (pst != BS_OK) return pst;
     }
 
@@ -529,9 +558,6 @@ static bs_status run_nearfield(bs_ctx* c) {
                    c->d_B.as<zd>(), c->st);
         LAUNCHED(c);
         CK(c->d_ph.ensure((size_t)ns * nk * sizeof(cpx<T>)));
-        std::vector<float4> cones = wave_cones(w);
-        CK(c->d_cones.ensure(cones.size() * sizeof(float4)));
-        CK(cudaMemcpyAsync(c->d_cones.p, cones.data(), cones.size() * sizeof(float4), cudaMemcpyHostToDevice, c->st));
         CK(c->d_kw4.ensure((size_t)nk * sizeof(float4)));
         launch_phase<T>(sc, c->d_sph.as<Sphere>(), c->d_waves.as<double>(), c->d_ph.as<cpx<T>>(),
                         c->d_kw4.as<float4>(), c->st);
@@ -559,7 +585,7 @@ static bs_status run_nearfield(bs_ctx* c) {
     } else {
         int thetaR = ns > 0 ? c->hs[0].thetaR : 1000;
         if (ns > 0) {
-            CK(c->d_lut.ensure(pool));
+            if (fp64) CK(c->d_lut.ensure(pool));
             CK(c->d_tab.ensure(maxrows * maxL * sizeof(zd)));
             CK(c->d_tabscr.ensure(maxrows * 2 * maxL * sizeof(double)));
             if (c->legP_theta != thetaR || c->legP_L < c->Lmax) {
@@ -571,23 +597,47 @@ static bs_status run_nearfield(bs_ctx* c) {
             }
         }
         const int nchunks = (int)chunk_start.size() - 1;
+        int max_chunk = 0;
+        for (int ci = 0; ci < nchunks; ci++) max_chunk = std::max(max_chunk, chunk_start[ci + 1] - chunk_start[ci]);
+        if (!fp64 && ns > 0) {
+            if ((int)c->slots.size() < max_chunk) c->slots.resize(max_chunk);
+            CK(c->d_texobj.ensure((size_t)4 * max_chunk * sizeof(unsigned long long)));
+        }
         bool first_build = true;
         for (int ci = 0; ci < std::max(1, nchunks); ci++) {
             int s0 = ns > 0 ? chunk_start[ci] : 0, s1 = ns > 0 ? chunk_start[ci + 1] : 0;
+            std::vector<unsigned long long> handles;
             for (int i = s0; i < s1; i++) {
                 const Sphere& S = c->hs[i];
                 const int L = S.Nl + 1;
                 launch_coef_rows(S, sc.kmag, c->d_A.as<zd>(), c->d_B.as<zd>(), c->d_tab.as<zd>(),
                                  c->d_tabscr.as<double>(), c->st);
                 LAUNCHED(c);
-                Patch<T>* lut = c->d_lut.as<Patch<T>>();
-                launch_lut_build<T>(c->d_tab.as<zd>(), S.dR, L, c->d_legP.as<double>(), c->legP_L, S.thetaR,
-                                    lut + S.usp_off, c->st);
-                LAUNCHED(c);
-                launch_lut_build<T>(c->d_tab.as<zd>() + (size_t)S.dR * L, S.aR, L, c->d_legP.as<double>(),
-                                    c->legP_L, S.thetaR, lut + S.uip_off, c->st);
-                LAUNCHED(c);
+                if (fp64) {
+                    Patch<double>* lut = c->d_lut.as<Patch<double>>();
+                    launch_lut_build<double>(c->d_tab.as<zd>(), S.dR, L, c->d_legP.as<double>(), c->legP_L, S.thetaR,
+                                             lut + S.usp_off, c->st);
+                    LAUNCHED(c);
+                    launch_lut_build<double>(c->d_tab.as<zd>() + (size_t)S.dR * L, S.aR, L, c->d_legP.as<double>(),
+                                             c->legP_L, S.thetaR, lut + S.uip_off, c->st);
+                    LAUNCHED(c);
+                } else {
+                    TexSlot& sl = c->slots[i - s0];
+                    // one spare row repeats the last, so a gather at the last row clamps as the texture would
+                    const int rows[4] = {S.dR, S.dR, S.aR, S.aR};
+                    for (int k = 0; k < 4; k++) CK(sl.ensure(k, S.thetaR, rows[k] + 1));
+                    launch_lut_build_tex(c->d_tab.as<zd>(), S.dR + 1, L, c->d_legP.as<double>(), c->legP_L, S.thetaR,
+                                         sl.surf[0], sl.surf[1], c->st);
+                    LAUNCHED(c);
+                    launch_lut_build_tex(c->d_tab.as<zd>() + (size_t)S.dR * L, S.aR + 1, L, c->d_legP.as<double>(),
+                                         c->legP_L, S.thetaR, sl.surf[2], sl.surf[3], c->st);
+                    LAUNCHED(c);
+                    for (int k = 0; k < 4; k++) handles.push_back(sl.tex[k]);
+                }
             }
+            if (!fp64 && !handles.empty())
+                CK(cudaMemcpyAsync(c->d_texobj.p, handles.data(), handles.size() * sizeof(unsigned long long),
+                                   cudaMemcpyHostToDevice, c->st));
             if (first_build) {
                 cudaEventRecord(c->ev[3], c->st);
                 first_build = false;
@@ -597,11 +647,13 @@ static bs_status run_nearfield(bs_ctx* c) {
                 launch_us_lut_f64(sc, c->d_sph.as<Sphere>(), s0, s1, ci > 0, finalize, c->d_waves.as<double>(),
                                   c->d_ph.as<zd>(), c->d_lut.as<Patch<double>>(), (const zd*)Uf, (zd*)U, c->st);
             } else {
-                launch_us_lut_f32(sc, c->d_sph.as<Sphere>(), s0, s1, ci > 0, finalize, c->d_kw4.as<float4>(),
-                                  c->d_cones.as<float4>(), c->d_ph.as<cpx<float>>(), c->d_lut.as<Patch<float>>(), (const cpx<float>*)Uf,
-                                  (cpx<float>*)U, c->st);
+                launch_us_lut_tex(sc, c->d_sph.as<Sphere>(), s0, s1, ci > 0, finalize, c->d_kw4.as<float4>(),
+                                  c->d_ph.as<cpx<float>>(), c->d_texobj.as<unsigned long long>(),
+                                  (const cpx<float>*)Uf, (cpx<float>*)U, c->st);
             }
             LAUNCHED(c);
+            // the handle list and the table slots are reused by the next chunk
+            if (!fp64 && ci + 1 < std::max(1, nchunks)) CK(cudaStreamSynchronize(c->st));
         }
         c->interactions = (long long)R * R * ns * nk;
     }
@@ -731,12 +783,14 @@ bs_status bs_get_info(bs_ctx* c, bs_info* out) {
     out->n_waves = p.plane_wave ? 1 : (int)(c->waves.size() / 3);
     out->uf_lut_r = p.uf_lut_r > 0 ? p.uf_lut_r : 2 * R;
     out->us_lut_theta = p.us_lut_theta > 0 ? p.us_lut_theta : 1000;
-    const DevBuf* bufs[] = {&c->d_sph, &c->d_waves, &c->d_kw4, &c->d_cones, &c->d_ph, &c->d_A, &c->d_B, &c->d_mie, &c->d_tab,
+    const DevBuf* bufs[] = {&c->d_sph, &c->d_waves, &c->d_kw4, &c->d_ph, &c->d_A, &c->d_B, &c->d_mie, &c->d_tab,
                             &c->d_tabscr, &c->d_legP, &c->d_lut, &c->d_uft, &c->d_uftscr, &c->d_fields, &c->d_su,
                             &c->d_sv, &c->d_mask, &c->d_wx, &c->d_wy, &c->d_wix, &c->d_wiy, &c->d_f1, &c->d_f2,
                             &c->d_g1, &c->d_I, &c->d_D, &c->d_img};
     int64_t tot = 0;
     for (const DevBuf* b : bufs) tot += (int64_t)b->n;
+    for (const auto& sl : c->slots)
+        for (int k = 0; k < 4; k++) tot += (int64_t)sl.w * sl.h[k] * (int64_t)sizeof(float);
     out->device_bytes = tot;
     return BS_OK;
 }
@@ -775,11 +829,17 @@ bs_status bs_get_lut(bs_ctx* c, int32_t sphere, int32_t which, double* host, siz
             host[2 * i + 1] = t[i].v[1];
         }
     } else {
-        std::vector<Patch<float>> t(n);
-        CK(cudaMemcpy(t.data(), c->d_lut.as<Patch<float>>() + off, n * sizeof(Patch<float>), cudaMemcpyDeviceToHost));
+        int slot = sphere;  // valid when the last run held every sphere in one chunk
+        if (slot >= (int)c->slots.size() || !c->slots[slot].arr[which * 2])
+            return fail(BS_ERR_STATE, "bs_get_lut: table of sphere %d not resident", sphere);
+        std::vector<float> re(n), im(n);
+        CK(cudaMemcpy2DFromArray(re.data(), S.thetaR * sizeof(float), c->slots[slot].arr[which * 2], 0, 0,
+                                 S.thetaR * sizeof(float), rows, cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy2DFromArray(im.data(), S.thetaR * sizeof(float), c->slots[slot].arr[which * 2 + 1], 0, 0,
+                                 S.thetaR * sizeof(float), rows, cudaMemcpyDeviceToHost));
         for (size_t i = 0; i < n; i++) {
-            host[2 * i] = t[i].v[0];
-            host[2 * i + 1] = t[i].v[1];
+            host[2 * i] = re[i];
+            host[2 * i + 1] = im[i];
         }
     }
     return BS_OK;

@@ -9,10 +9,6 @@
 
 namespace bs {
 
-// Plane waves are processed in chunks of this many (after a Hilbert-curve
-// sort); the host supplies one bounding cone per chunk.
-constexpr int WAVE_CHUNK = 64;
-
 template <class T>
 struct cpx;
 using zd = cpx<double>;
@@ -39,9 +35,13 @@ void launch_phase(const Scene& sc, const Sphere* sph, const double* waves, cpx<T
 void launch_us_lut_f64(const Scene& sc, const Sphere* sph, int s0, int s1, int accumulate, int finalize,
                        const double* waves, const zd* ph, const Patch<double>* lut, const zd* Uf, zd* U,
                        cudaStream_t st);
-void launch_us_lut_f32(const Scene& sc, const Sphere* sph, int s0, int s1, int accumulate, int finalize,
-                       const float4* kw4, const float4* cones, const cpx<float>* ph, const Patch<float>* lut,
-                       const cpx<float>* Uf, cpx<float>* U, cudaStream_t st);
+// mixed path: tex holds, for sphere s0 + j, the texture objects of
+// {Usp re, Usp im, Uip re, Uip im} at [4 j .. 4 j + 3]
+void launch_us_lut_tex(const Scene& sc, const Sphere* sph, int s0, int s1, int accumulate, int finalize,
+                       const float4* kw4, const cpx<float>* ph, const unsigned long long* tex, const cpx<float>* Uf,
+                       cpx<float>* U, cudaStream_t st);
+void launch_lut_build_tex(const zd* tab, int rows, int L, const double* P, int Pstride, int thetaR,
+                          cudaSurfaceObject_t sre, cudaSurfaceObject_t sim, cudaStream_t st);
 template <class T>
 void launch_us_direct(const Scene& sc, const Sphere* sph, int lstride, const zd* A, const zd* B, const double* waves,
                       const cpx<T>* ph, const cpx<T>* Uf, cpx<T>* U, cudaStream_t st);

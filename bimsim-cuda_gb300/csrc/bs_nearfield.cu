@@ -4,8 +4,6 @@
 // into the epilogue.
 #include <cuda_runtime.h>
 
-#include <climits>
-
 #include "bs_kernels.h"
 #include "bs_math.cuh"
 
@@ -386,62 +384,50 @@ __global__ void __launch_bounds__(128) us_lut_f64_kernel(Scene sc, const Sphere*
 // Mixed precision: per-(pixel, sphere) geometry in double, per-wave work in
 // float, per-chunk partial sums combined with Kahan compensation.
 //
-// A block owns a 16 x 16 pixel tile.  Waves arrive sorted along a Hilbert
-// curve and are processed in chunks of WAVE_CHUNK; the host gives each chunk
-// a cone (axis c_k, half-angle beta_k).  For a tile whose pixels all lie
-// outside the sphere and see it within an angle gamma of the tile-centre
-// direction r_c, every lookup angle of the chunk lies in
-//     angle(c_k, r_c) +- (beta_k + gamma)            (triangle inequality),
-// so the LUT rows of the tile times that angular window are copied to shared
-// memory once per chunk and all lookups read shared memory.  Tiles that
-// touch or contain the sphere, or whose window is too large, read the LUT
-// from global memory.
-constexpr int USF_BLOCK = 256;     // 16 x 16 pixel tile
-constexpr int USF_STAGE = 2048;    // LUT patches staged per chunk (64 KB)
-constexpr float USF_MARGIN = 2e-3f;  // radians added to every angular bound
+// The tables live in CUDA arrays (block-linear layout, separate real and
+// imaginary float planes, x = angle, y = radius) so that the gather of a
+// bilinear cell goes through the texture path, whose 2-D tiled layout keeps
+// the scattered lookups of neighbouring pixels in few cache lines.
+// tex2Dgather returns the four texels of the cell, (i, j+1), (i+1, j+1),
+// (i+1, j), (i, j) in x, y, z, w; the interpolation is done here with exact
+// single-precision weights, and clamp addressing reproduces the edge
+// behaviour of the reference's texture fetch.
+constexpr int UST_BLOCK = 256;  // 16 x 16 pixel tile
+constexpr int UST_CHUNK = 256;  // waves staged in shared memory at a time
 
-__global__ void __launch_bounds__(USF_BLOCK, 3) us_lut_f32_kernel(Scene sc, const Sphere* __restrict__ sph, int s0, int s1,
-                                                                    int accumulate, int finalize,
-                                                                    const float4* __restrict__ kw4,
-                                                                    const float4* __restrict__ cones,
-                                                                    const cpx<float>* __restrict__ ph,
-                                                                    const Patch<float>* __restrict__ lut,
-                                                                    const cpx<float>* __restrict__ Uf,
-                                                                    cpx<float>* __restrict__ U) {
-    extern __shared__ float4 s_stage[];  // USF_STAGE patches, two float4 each
-    __shared__ float4 s_k[WAVE_CHUNK];
-    __shared__ float2 s_p[WAVE_CHUNK];
-    __shared__ int s_red[4][USF_BLOCK / 32];
+__global__ void __launch_bounds__(UST_BLOCK, 3) us_lut_tex_kernel(Scene sc, const Sphere* __restrict__ sph, int s0, int s1,
+                                                                 int accumulate, int finalize,
+                                                                 const float4* __restrict__ kw4,
+                                                                 const cpx<float>* __restrict__ ph,
+                                                                 const unsigned long long* __restrict__ tex,
+                                                                 const cpx<float>* __restrict__ Uf,
+                                                                 cpx<float>* __restrict__ U) {
+    __shared__ float4 s_k[UST_CHUNK];
+    __shared__ float2 s_p[UST_CHUNK];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     // each warp covers an 8 x 4 pixel block of the 16 x 16 tile
     const int tiles_u = (sc.R + 15) / 16;
-    const int tu = (blockIdx.x % tiles_u) * 16, tv = (blockIdx.x / tiles_u) * 16;
-    const int iu = tu + (lane & 7) + 8 * (warp & 1);
-    const int iv = tv + (lane >> 3) + 4 * (warp >> 1);
+    const int iu = (blockIdx.x % tiles_u) * 16 + (lane & 7) + 8 * (warp & 1);
+    const int iv = (blockIdx.x / tiles_u) * 16 + (lane >> 3) + 4 * (warp >> 1);
     const bool valid = iu < sc.R && iv < sc.R;
     const int idx = iv * sc.R + iu;
     double p[3];
     pixel_pos(sc, min(iu, sc.R - 1), min(iv, sc.R - 1), p);
-    // tile centre in single precision (only used for bounds, with margins)
-    float pc[3];
-    {
-        float u = ((float)tu + 7.5f) / (float)sc.R, v = ((float)tv + 7.5f) / (float)sc.R;
-#pragma unroll
-        for (int c = 0; c < 3; c++) pc[c] = (float)sc.A[c] + (float)sc.X[c] * u + (float)sc.Y[c] * v;
-    }
     float tot_r = 0.f, tot_i = 0.f, cmp_r = 0.f, cmp_i = 0.f;  // Kahan sum over chunk partials
     if (accumulate && valid) {
         tot_r = U[idx].re;
         tot_i = U[idx].im;
     }
-    const int nchunks = (sc.nk + WAVE_CHUNK - 1) / WAVE_CHUNK;
     for (int s = s0; s < s1; s++) {
         const Sphere& S = sph[s];
         double r[3];
         double d = dist_exact(p, S.p, r);
         TableSel ts = select_table(S, d);
         int ir = (int)floor(ts.x);
-        float al = (float)(ts.x - ir);
+        const float al = (float)(ts.x - ir);
+        const float y = (float)ir + 1.0f;  // gather footprint rows ir, ir + 1
+        const int k = 4 * (s - s0) + (d < S.a ? 2 : 0);
+        const cudaTextureObject_t tre = tex[k], tim = tex[k + 1];
         float rx = 0.f, ry = 0.f, rz = 0.f, cb = 1.f;  // d == 0: cos(theta) := 1
         if (d != 0) {
             double inv = 1.0 / d;
@@ -450,117 +436,39 @@ __global__ void __launch_bounds__(USF_BLOCK, 3) us_lut_f32_kernel(Scene sc, cons
             rz = (float)(r[2] * inv);
             cb = 0.f;
         }
-        // ---- tile bounds: rows, angular extent gamma ----
-        float cx = pc[0] - (float)S.p[0], cy = pc[1] - (float)S.p[1], cz = pc[2] - (float)S.p[2];
-        float cl = sqrtf(cx * cx + cy * cy + cz * cz);
-        bool far_ok = valid ? (d >= S.a && d != 0) : true;
-        float gam = 0.f;
-        if (cl > 0.f) {
-            cx /= cl;
-            cy /= cl;
-            cz /= cl;
-            if (valid) gam = acosf(fminf(fmaxf(rx * cx + ry * cy + rz * cz, -1.f), 1.f));
-        } else {
-            far_ok = false;
-        }
-        int rlo = valid ? ir : INT_MAX, rhi = valid ? ir : INT_MIN;
-        rlo = __reduce_min_sync(0xffffffffu, rlo);
-        rhi = __reduce_max_sync(0xffffffffu, rhi);
-        int gbits = (int)__reduce_max_sync(0xffffffffu, (unsigned)__float_as_int(gam));
-        int ok = __all_sync(0xffffffffu, far_ok);
-        __syncthreads();  // s_red reuse across spheres
-        if (lane == 0) {
-            s_red[0][warp] = rlo;
-            s_red[1][warp] = rhi;
-            s_red[2][warp] = gbits;
-            s_red[3][warp] = ok;
-        }
-        __syncthreads();
-        for (int w = 0; w < USF_BLOCK / 32; w++) {
-            rlo = min(rlo, s_red[0][w]);
-            rhi = max(rhi, s_red[1][w]);
-            gbits = max(gbits, s_red[2][w]);
-            ok = ok && s_red[3][w];
-        }
-        const int rows = rhi - rlo + 1;
-        const float gam_all = __int_as_float(gbits) + USF_MARGIN;
-        const bool tile_staged = ok && rows >= 1 && rows <= USF_STAGE / 4;
-        const int lr = min(max(ir - rlo, 0), max(rows, 1) - 1);  // lanes off the slice did not vote
-
         const float tmax = (float)(S.thetaR - 1);
         const float tsc = (float)((S.thetaR - 1) / PI_REF);
-        const Patch<float>* table = lut + ts.off;
-        const Patch<float>* row = table + (size_t)ir * S.thetaR;
         const cpx<float>* phs = ph + (size_t)s * sc.nk;
-        for (int ch = 0; ch < nchunks; ch++) {
-            const int w0 = ch * WAVE_CHUNK;
-            const int nw = min(WAVE_CHUNK, sc.nk - w0);
-            int t_lo = 0, W = 0;
-            bool staged = false;
-            if (tile_staged) {
-                float4 cone = cones[ch];
-                float thc = acosf(fminf(fmaxf(cone.x * cx + cone.y * cy + cone.z * cz, -1.f), 1.f));
-                float lo = thc - cone.w - gam_all, hi = thc + cone.w + gam_all;
-                t_lo = max(0, (int)floorf(lo * tsc) - 1);
-                int t_hi = min(S.thetaR - 1, (int)floorf(hi * tsc) + 1);
-                W = t_hi - t_lo + 1;
-                staged = W >= 1 && rows * W <= USF_STAGE;
-            }
-            __syncthreads();  // previous chunk's readers are done
+        for (int w0 = 0; w0 < sc.nk; w0 += UST_CHUNK) {
+            const int nw = min(UST_CHUNK, sc.nk - w0);
+            __syncthreads();
             if (threadIdx.x < nw) {
                 s_k[threadIdx.x] = kw4[w0 + threadIdx.x];
                 s_p[threadIdx.x] = make_float2(phs[w0 + threadIdx.x].re, phs[w0 + threadIdx.x].im);
             }
-            if (staged) {
-                const int n = rows * W;
-                for (int e = threadIdx.x; e < n; e += USF_BLOCK) {
-                    int rr = e / W, tt = e - rr * W;
-                    const float4* src = reinterpret_cast<const float4*>(table + (size_t)(rlo + rr) * S.thetaR + t_lo + tt);
-                    s_stage[2 * e] = __ldg(src);
-                    s_stage[2 * e + 1] = __ldg(src + 1);
-                }
-            }
             __syncthreads();
             float ar = 0.f, ai = 0.f;
-            if (staged) {
-                const float4* srow = s_stage + 2 * (lr * W);
-#pragma unroll 4
-                for (int w = 0; w < nw; w++) {
-                    float4 k = s_k[w];
-                    float c = fmaf(k.x, rx, fmaf(k.y, ry, fmaf(k.z, rz, cb)));
-                    c = fminf(fmaxf(c, -1.f), 1.f);
-                    float t = fminf(acosf(c) * tsc, tmax);
-                    float tf = floorf(t);
-                    float be = t - tf;
-                    int lt = min(max((int)tf - t_lo, 0), W - 1);
-                    float4 q0 = srow[2 * lt], q1 = srow[2 * lt + 1];
-                    float vr = fmaf(be, fmaf(al, q1.z, q1.x), fmaf(al, q0.z, q0.x));
-                    float vi = fmaf(be, fmaf(al, q1.w, q1.y), fmaf(al, q0.w, q0.y));
-                    float2 pw = s_p[w];
-                    ar = fmaf(pw.x, vr, fmaf(-pw.y, vi, ar));
-                    ai = fmaf(pw.x, vi, fmaf(pw.y, vr, ai));
-                }
-            } else {
-#pragma unroll 4
-                for (int w = 0; w < nw; w++) {
-                    float4 k = s_k[w];
-                    float c = fmaf(k.x, rx, fmaf(k.y, ry, fmaf(k.z, rz, cb)));
-                    c = fminf(fmaxf(c, -1.f), 1.f);
-                    float t = fminf(acosf(c) * tsc, tmax);
-                    float tf = floorf(t);
-                    float be = t - tf;
-                    const float4* q = reinterpret_cast<const float4*>(row + (int)tf);
-                    float4 q0 = __ldg(q), q1 = __ldg(q + 1);
-                    float vr = fmaf(be, fmaf(al, q1.z, q1.x), fmaf(al, q0.z, q0.x));
-                    float vi = fmaf(be, fmaf(al, q1.w, q1.y), fmaf(al, q0.w, q0.y));
-                    float2 pw = s_p[w];
-                    ar = fmaf(pw.x, vr, fmaf(-pw.y, vi, ar));
-                    ai = fmaf(pw.x, vi, fmaf(pw.y, vr, ai));
-                }
+#pragma unroll 2
+            for (int w = 0; w < nw; w++) {
+                const float4 kk = s_k[w];
+                float c = fmaf(kk.x, rx, fmaf(kk.y, ry, fmaf(kk.z, rz, cb)));
+                c = fminf(fmaxf(c, -1.f), 1.f);
+                const float t = fminf(acosf(c) * tsc, tmax);
+                const float tf = floorf(t);
+                const float be = t - tf;
+                const float4 gr = tex2Dgather<float4>(tre, tf + 1.0f, y, 0);
+                const float4 gi = tex2Dgather<float4>(tim, tf + 1.0f, y, 0);
+                const float ar0 = fmaf(be, gr.z - gr.w, gr.w), ar1 = fmaf(be, gr.y - gr.x, gr.x);
+                const float ai0 = fmaf(be, gi.z - gi.w, gi.w), ai1 = fmaf(be, gi.y - gi.x, gi.x);
+                const float vr = fmaf(al, ar1 - ar0, ar0);
+                const float vi = fmaf(al, ai1 - ai0, ai0);
+                const float2 pw = s_p[w];
+                ar = fmaf(pw.x, vr, fmaf(-pw.y, vi, ar));
+                ai = fmaf(pw.x, vi, fmaf(pw.y, vr, ai));
             }
             // Kahan: add the chunk partial to the running total
-            float yr = ar - cmp_r, yi = ai - cmp_i;
-            float tr = tot_r + yr, ti = tot_i + yi;
+            const float yr = ar - cmp_r, yi = ai - cmp_i;
+            const float tr = tot_r + yr, ti = tot_i + yi;
             cmp_r = (tr - tot_r) - yr;
             cmp_i = (ti - tot_i) - yi;
             tot_r = tr;
@@ -581,6 +489,23 @@ __global__ void __launch_bounds__(USF_BLOCK, 3) us_lut_f32_kernel(Scene sc, cons
         }
     }
     U[idx] = mk(tot_r, tot_i);
+}
+
+// LUT build into the real and imaginary planes of a CUDA array pair (same
+// sums as lut_build_kernel, written through surfaces).  `rows` counts one
+// spare row that repeats the last table row.
+__global__ void __launch_bounds__(256) lut_build_tex_kernel(const zd* __restrict__ tab, int rows, int L,
+                                                              const double* __restrict__ P, int Pstride, int thetaR,
+                                                              cudaSurfaceObject_t sre, cudaSurfaceObject_t sim) {
+    const int t = blockIdx.x * 32 + (threadIdx.x & 31);
+    const int r = blockIdx.y * 8 + (threadIdx.x >> 5);
+    if (t >= thetaR || r >= rows) return;
+    const zd* c = tab + (size_t)min(r, rows - 2) * L;  // the last row written repeats the one before
+    const double* pl = P + (size_t)t * Pstride;
+    zd acc = mk(0.0, 0.0);
+    for (int l = 0; l < L; l++) acc = acc + c[l] * pl[l];
+    surf2Dwrite((float)acc.re, sre, t * (int)sizeof(float), r);
+    surf2Dwrite((float)acc.im, sim, t * (int)sizeof(float), r);
 }
 
 // ---------------------------------------------------------------------------
@@ -773,18 +698,18 @@ void launch_us_lut_f64(const Scene& sc, const Sphere* sph, int s0, int s1, int a
                                                            Uf, U);
 }
 
-void launch_us_lut_f32(const Scene& sc, const Sphere* sph, int s0, int s1, int accumulate, int finalize,
-                       const float4* kw4, const float4* cones, const cpx<float>* ph, const Patch<float>* lut,
-                       const cpx<float>* Uf, cpx<float>* U, cudaStream_t st) {
+void launch_us_lut_tex(const Scene& sc, const Sphere* sph, int s0, int s1, int accumulate, int finalize,
+                       const float4* kw4, const cpx<float>* ph, const unsigned long long* tex, const cpx<float>* Uf,
+                       cpx<float>* U, cudaStream_t st) {
     int tiles = (sc.R + 15) / 16;
-    const int smem = USF_STAGE * (int)sizeof(Patch<float>);
-    static bool configured = false;
-    if (!configured) {
-        cudaFuncSetAttribute(us_lut_f32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-        configured = true;
-    }
-    us_lut_f32_kernel<<<(unsigned)tiles * tiles, USF_BLOCK, smem, st>>>(sc, sph, s0, s1, accumulate, finalize, kw4,
-                                                                         cones, ph, lut, Uf, U);
+    us_lut_tex_kernel<<<(unsigned)tiles * tiles, UST_BLOCK, 0, st>>>(sc, sph, s0, s1, accumulate, finalize, kw4, ph,
+                                                                      tex, Uf, U);
+}
+
+void launch_lut_build_tex(const zd* tab, int rows, int L, const double* P, int Pstride, int thetaR,
+                          cudaSurfaceObject_t sre, cudaSurfaceObject_t sim, cudaStream_t st) {
+    dim3 grid(blocks_for(thetaR, 32), blocks_for(rows, 8));
+    lut_build_tex_kernel<<<grid, 256, 0, st>>>(tab, rows, L, P, Pstride, thetaR, sre, sim);
 }
 
 template <class T>

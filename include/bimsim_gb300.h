@@ -184,6 +184,12 @@ bs_status bs_get_mie(bs_ctx* ctx, int32_t sphere, double* A, double* B, int32_t 
  * for spheres of the last table chunk. */
 bs_status bs_get_lut(bs_ctx* ctx, int32_t sphere, int32_t which, double* host, size_t count);
 
+/* Measured FMA throughput (TFLOP/s, 2 flop per FMA) of the current GPU in
+ * single and double precision, from bounded FMA-chain kernels timed with
+ * CUDA events.  The denominator of the scattered-field kernels' roofline.
+ * No reference counterpart. */
+bs_status bs_measure_fma_peak(double* fp32_tflops, double* fp64_tflops);
+
 #ifdef __cplusplus
 }
 #endif

@@ -884,10 +884,11 @@ void nearfield_rows(Scene& sc, int row0, int row1, int nthreads, cd* U, cd* Uf) 
     const int R = sc.g.R;
 #ifdef _OPENMP
     int nt = nthreads > 0 ? nthreads : omp_get_max_threads();
-#pragma omp parallel for schedule(dynamic, 1) num_threads(nt)
+#pragma omp parallel for schedule(dynamic, 16) num_threads(nt)
 #endif
-    for (int iv = row0; iv < row1; iv++) {
-        for (int iu = 0; iu < R; iu++) {
+    for (long long pix = (long long)row0 * R; pix < (long long)row1 * R; pix++) {
+        {
+            const int iv = (int)(pix / R), iu = (int)(pix % R);
             double u = (double)iu / R, v = (double)iv / R;
             V3 pt = quad_at(sc.g.nf, u, v);
             cd uf = incident(sc, pt);
