@@ -50,6 +50,7 @@ def library():
         "bs_get_mie": ([vp, i32, vp, vp, i32], C.c_int),
         "bs_get_lut": ([vp, i32, i32, vp, sz], C.c_int),
         "bs_measure_fma_peak": ([vp, vp], C.c_int),
+        "bs_mie_noalloc": ([vp, i32, i32, C.c_double, vp, vp, vp], C.c_int),
     }
     for name, (args, res) in proto.items():
         f = getattr(lib, name)

@@ -181,6 +181,15 @@ const char* bs_version(void) { return "bimsim-gb300 0.1 (sm_103a)"; }
 
 const char* bs_last_error(void) { return g_err.c_str(); }
 
+}  // extern "C"
+
+// Lets other translation units of the library report through bs_last_error().
+namespace bs {
+void set_last_error(const char* msg) { g_err = msg; }
+}  // namespace bs
+
+extern "C" {
+
 bs_status bs_create(const bs_params* params, bs_ctx** out) {
     if (!params || !out) return fail(BS_ERR_ARG, "bs_create: null argument");
     std::string why;

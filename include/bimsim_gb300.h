@@ -190,6 +190,25 @@ bs_status bs_get_lut(bs_ctx* ctx, int32_t sphere, int32_t which, double* host, s
  * No reference counterpart. */
 bs_status bs_measure_fma_peak(double* fp32_tflops, double* fp64_tflops);
 
+/* Mie coefficients without any device allocation, for callers that cannot
+ * call cudaMalloc (code inside CUDA stream capture, serving loops that reserve
+ * all memory up front, frameworks that own device memory through their own
+ * pool).  No counterpart in the reference; it computes what
+ * bs_simulate/bs_get_mie compute per sphere.
+ *   spheres  device array, ns x {a, n_re, n_im} (radius um, complex index)
+ *   ns       0..256;  nl: highest order, 0..127;  k: wavenumber 2*PI/lambda
+ *   A, B     device arrays, ns x (nl + 1) interleaved complex doubles
+ *   stream   cudaStream_t to run on (NULL = legacy default stream); the call is
+ *            asynchronous on it.
+ * The Bessel work space is a fixed 3 MiB device array inside this library,
+ * held by every GPU that loads it; it is fully rewritten before being read,
+ * so nothing needs clearing, but every call shares it: calls whose kernels
+ * overlap on the GPU (different streams, or threads sharing a device) race.
+ * The first call on a device resolves the array's device address, so make it
+ * before any stream capture.  Sizes beyond the limits return BS_ERR_ARG. */
+bs_status bs_mie_noalloc(const double* spheres, int32_t ns, int32_t nl, double k, double* A, double* B,
+                         void* stream);
+
 #ifdef __cplusplus
 }
 #endif
