@@ -55,7 +55,8 @@ class Info(C.Structure):
 class Stats(C.Structure):
     _fields_ = [("ms_total", C.c_double), ("ms_uf", C.c_double), ("ms_mie", C.c_double),
                 ("ms_lut", C.c_double), ("ms_us", C.c_double), ("ms_detector", C.c_double),
-                ("kernel_launches", C.c_int64), ("us_interactions", C.c_int64)]
+                ("kernel_launches", C.c_int64), ("us_interactions", C.c_int64),
+                ("lut_chunks_staged", C.c_int64), ("lut_chunks_total", C.c_int64)]
 
 
 def make_params(lam=1.0, amplitude=1.0, k_dir=(0.0, 0.0, 1.0), focus=(0.0, 0.0, 0.0),

@@ -163,6 +163,7 @@ struct bs_ctx {
     bool have = false;
 
     DevBuf d_sph, d_waves, d_kw4, d_ph, d_A, d_B, d_mie, d_tab, d_tabscr, d_legP, d_lut, d_uft, d_uftscr;
+    DevBuf d_cones, d_cnt;  // per-chunk wave cones; staged / total counters of the mixed LUT kernel
     DevBuf d_fields;  // [2][R*R] U then Uf
     DevBuf d_su, d_sv, d_mask, d_wx, d_wy, d_wix, d_wiy, d_f1, d_f2, d_g1, d_I, d_D, d_img;
     int legP_theta = 0, legP_L = 0;
@@ -213,7 +214,7 @@ bs_status bs_destroy(bs_ctx* c) {
     DevBuf* bufs[] = {&c->d_sph, &c->d_waves, &c->d_kw4, &c->d_ph, &c->d_A, &c->d_B, &c->d_mie, &c->d_tab,
                       &c->d_tabscr, &c->d_legP, &c->d_lut, &c->d_uft, &c->d_uftscr, &c->d_fields, &c->d_su,
                       &c->d_sv, &c->d_mask, &c->d_wx, &c->d_wy, &c->d_wix, &c->d_wiy, &c->d_f1, &c->d_f2,
-                      &c->d_g1, &c->d_I, &c->d_D, &c->d_img};
+                      &c->d_g1, &c->d_I, &c->d_D, &c->d_img, &c->d_cones, &c->d_cnt};
     for (DevBuf* b : bufs) b->release();
     for (auto& sl : c->slots) sl.release();
     c->d_texobj.release();
@@ -427,13 +428,19 @@ static bs_status run_detector(bs_ctx* c) {
 
 // Place each sphere's Usp and Uip patches in the LUT pool; spheres whose
 // tables together exceed the budget go to later chunks (each chunk is built
-// and applied before the next one overwrites the pool).
-static bs_status plan_luts(bs_ctx* c, size_t patch, std::vector<int>& chunk_start, size_t& pool, size_t& maxrows,
+// and applied before the next one overwrites the pool).  FP64: one
+// Patch<double> per entry.  Mixed: one float2 per entry in linear rows of
+// thetaR + 1 entries (the last column repeated, rounded up to an even count
+// for 16-byte rows), and a second copy of every entry in the texture planes,
+// which also counts against the budget.
+static bs_status plan_luts(bs_ctx* c, bool mixed, std::vector<int>& chunk_start, size_t& pool, size_t& maxrows,
                            size_t& maxL) {
+    const size_t patch = mixed ? sizeof(float2) : sizeof(Patch<double>);
+    const size_t copies = mixed ? 2 : 1;
     const int ns = (int)c->hs.size();
     size_t free_b = 0, total_b = 0;
     CK(cudaMemGetInfo(&free_b, &total_b));
-    size_t budget = c->budget ? c->budget : (size_t)(0.80 * (double)(free_b + c->d_lut.n));
+    size_t budget = c->budget ? c->budget : (size_t)(0.80 * (double)(free_b + c->d_lut.n * copies));
     chunk_start.clear();
     size_t acc = 0;
     pool = 0;
@@ -441,15 +448,17 @@ static bs_status plan_luts(bs_ctx* c, size_t patch, std::vector<int>& chunk_star
     maxL = 0;
     for (int i = 0; i < ns; i++) {
         Sphere& S = c->hs[i];
-        size_t need = (size_t)(S.dR + S.aR) * S.thetaR * patch;
-        if (need > budget)
-            return fail(BS_ERR_NOMEM, "LUT of sphere %d needs %zu bytes, over the budget of %zu", i + 1, need, budget);
-        if (i == 0 || acc + need > budget) {
+        S.lin_stride = mixed ? ((S.thetaR + 2) & ~1) : S.thetaR;
+        size_t need = (size_t)(S.dR + S.aR) * S.lin_stride * patch;
+        if (need * copies > budget)
+            return fail(BS_ERR_NOMEM, "LUT of sphere %d needs %zu bytes, over the budget of %zu", i + 1,
+                        need * copies, budget);
+        if (i == 0 || (acc + need) * copies > budget) {
             chunk_start.push_back(i);
             acc = 0;
         }
         S.usp_off = (int64_t)(acc / patch);
-        S.uip_off = S.usp_off + (int64_t)S.dR * S.thetaR;
+        S.uip_off = S.usp_off + (int64_t)S.dR * S.lin_stride;
         acc += need;
         pool = std::max(pool, acc);
         maxrows = std::max(maxrows, (size_t)(S.dR + S.aR));
@@ -514,6 +523,42 @@ static void sort_waves(std::vector<double>& w) {
     w.swap(out);
 }
 
+// Bounding cone (unit axis, half-angle in radians) of every WAVE_CHUNK
+// consecutive waves, with a small margin for single-precision rounding.  A
+// chunk holding a direction that is not a unit vector gets half-angle pi,
+// which turns the angular window off for it.
+static std::vector<float4> wave_cones(const std::vector<double>& w) {
+    size_t nk = w.size() / 3;
+    size_t nch = (nk + WAVE_CHUNK - 1) / WAVE_CHUNK;
+    std::vector<float4> out(nch);
+    for (size_t ch = 0; ch < nch; ch++) {
+        size_t a = ch * WAVE_CHUNK, b = std::min(nk, a + WAVE_CHUNK);
+        double m[3] = {0, 0, 0};
+        bool unit = true;
+        for (size_t i = a; i < b; i++) {
+            const double* k = &w[3 * i];
+            double kl = std::sqrt(k[0] * k[0] + k[1] * k[1] + k[2] * k[2]);
+            if (!(std::fabs(kl - 1.0) <= 1e-6)) unit = false;
+            for (int c = 0; c < 3; c++) m[c] += k[c];
+        }
+        double ml = std::sqrt(m[0] * m[0] + m[1] * m[1] + m[2] * m[2]);
+        double beta = 0;
+        if (ml > 1e-3 && unit) {
+            for (int c = 0; c < 3; c++) m[c] /= ml;
+            for (size_t i = a; i < b; i++) {
+                const double* k = &w[3 * i];
+                double cth = k[0] * m[0] + k[1] * m[1] + k[2] * m[2];
+                beta = std::max(beta, std::acos(std::min(1.0, std::max(-1.0, cth))));
+            }
+        } else {
+            m[0] = 0, m[1] = 0, m[2] = 1;
+            beta = TRUE_PI;
+        }
+        out[ch] = make_float4((float)m[0], (float)m[1], (float)m[2], (float)(beta + 1e-4));
+    }
+    return out;
+}
+
 // ---------------------------------------------------------------------------
 // The near field
 // ---------------------------------------------------------------------------
@@ -550,7 +595,7 @@ static bs_status run_nearfield(bs_ctx* c) {
     std::vector<int> chunk_start;
     size_t pool = 0, maxrows = 0, maxL = 0;
     if (p.scalar && p.lut_us && ns > 0) {
-        bs_status pst = plan_luts(c, fp64 ? sizeof(Patch<double>) : 2 * sizeof(float), chunk_start, pool, maxrows, maxL);
+        bs_status pst = plan_luts(c, !fp64, chunk_start, pool, maxrows, maxL);
         if (pst != BS_OK) return pst;
     }
 
@@ -594,7 +639,7 @@ static bs_status run_nearfield(bs_ctx* c) {
     } else {
         int thetaR = ns > 0 ? c->hs[0].thetaR : 1000;
         if (ns > 0) {
-            if (fp64) CK(c->d_lut.ensure(pool));
+            CK(c->d_lut.ensure(pool));
             CK(c->d_tab.ensure(maxrows * maxL * sizeof(zd)));
             CK(c->d_tabscr.ensure(maxrows * 2 * maxL * sizeof(double)));
             if (c->legP_theta != thetaR || c->legP_L < c->Lmax) {
@@ -611,6 +656,12 @@ static bs_status run_nearfield(bs_ctx* c) {
         if (!fp64 && ns > 0) {
             if ((int)c->slots.size() < max_chunk) c->slots.resize(max_chunk);
             CK(c->d_texobj.ensure((size_t)4 * max_chunk * sizeof(unsigned long long)));
+            std::vector<float4> cones = wave_cones(w);
+            CK(c->d_cones.ensure(cones.size() * sizeof(float4)));
+            CK(cudaMemcpyAsync(c->d_cones.p, cones.data(), cones.size() * sizeof(float4), cudaMemcpyHostToDevice,
+                               c->st));
+            CK(c->d_cnt.ensure(2 * sizeof(unsigned long long)));
+            CK(cudaMemsetAsync(c->d_cnt.p, 0, 2 * sizeof(unsigned long long), c->st));
         }
         bool first_build = true;
         for (int ci = 0; ci < std::max(1, nchunks); ci++) {
@@ -635,11 +686,13 @@ static bs_status run_nearfield(bs_ctx* c) {
                     // one spare row repeats the last, so a gather at the last row clamps as the texture would
                     const int rows[4] = {S.dR, S.dR, S.aR, S.aR};
                     for (int k = 0; k < 4; k++) CK(sl.ensure(k, S.thetaR, rows[k] + 1));
+                    float2* lin = c->d_lut.as<float2>();
                     launch_lut_build_tex(c->d_tab.as<zd>(), S.dR + 1, L, c->d_legP.as<double>(), c->legP_L, S.thetaR,
-                                         sl.surf[0], sl.surf[1], c->st);
+                                         sl.surf[0], sl.surf[1], lin + S.usp_off, S.lin_stride, c->st);
                     LAUNCHED(c);
                     launch_lut_build_tex(c->d_tab.as<zd>() + (size_t)S.dR * L, S.aR + 1, L, c->d_legP.as<double>(),
-                                         c->legP_L, S.thetaR, sl.surf[2], sl.surf[3], c->st);
+                                         c->legP_L, S.thetaR, sl.surf[2], sl.surf[3], lin + S.uip_off, S.lin_stride,
+                                         c->st);
                     LAUNCHED(c);
                     for (int k = 0; k < 4; k++) handles.push_back(sl.tex[k]);
                 }
@@ -657,8 +710,9 @@ static bs_status run_nearfield(bs_ctx* c) {
                                   c->d_ph.as<zd>(), c->d_lut.as<Patch<double>>(), (const zd*)Uf, (zd*)U, c->st);
             } else {
                 launch_us_lut_tex(sc, c->d_sph.as<Sphere>(), s0, s1, ci > 0, finalize, c->d_kw4.as<float4>(),
-                                  c->d_ph.as<cpx<float>>(), c->d_texobj.as<unsigned long long>(),
-                                  (const cpx<float>*)Uf, (cpx<float>*)U, c->st);
+                                  c->d_cones.as<float4>(), c->d_ph.as<cpx<float>>(),
+                                  c->d_texobj.as<unsigned long long>(), c->d_lut.as<float2>(), (const cpx<float>*)Uf,
+                                  (cpx<float>*)U, ns > 0 ? c->d_cnt.as<unsigned long long>() : nullptr, c->st);
             }
             LAUNCHED(c);
             // the handle list and the table slots are reused by the next chunk
@@ -699,6 +753,13 @@ bs_status bs_simulate(bs_ctx* c, bs_precision prec) {
     c->stats.ms_total = tot;
     c->stats.kernel_launches = c->launches - l0;
     c->stats.us_interactions = c->interactions;
+    c->stats.lut_chunks_staged = c->stats.lut_chunks_total = 0;
+    if (prec == BS_PREC_MIXED && c->prm.scalar && c->prm.lut_us && !c->hs.empty()) {
+        unsigned long long cnt[2] = {0, 0};
+        CK(cudaMemcpy(cnt, c->d_cnt.p, sizeof(cnt), cudaMemcpyDeviceToHost));
+        c->stats.lut_chunks_staged = (int64_t)cnt[0];
+        c->stats.lut_chunks_total = (int64_t)cnt[1];
+    }
     c->have = true;
     return BS_OK;
 }
@@ -795,7 +856,7 @@ bs_status bs_get_info(bs_ctx* c, bs_info* out) {
     const DevBuf* bufs[] = {&c->d_sph, &c->d_waves, &c->d_kw4, &c->d_ph, &c->d_A, &c->d_B, &c->d_mie, &c->d_tab,
                             &c->d_tabscr, &c->d_legP, &c->d_lut, &c->d_uft, &c->d_uftscr, &c->d_fields, &c->d_su,
                             &c->d_sv, &c->d_mask, &c->d_wx, &c->d_wy, &c->d_wix, &c->d_wiy, &c->d_f1, &c->d_f2,
-                            &c->d_g1, &c->d_I, &c->d_D, &c->d_img};
+                            &c->d_g1, &c->d_I, &c->d_D, &c->d_img, &c->d_cones, &c->d_cnt};
     int64_t tot = 0;
     for (const DevBuf* b : bufs) tot += (int64_t)b->n;
     for (const auto& sl : c->slots)

@@ -52,7 +52,7 @@ struct Sphere {
     int64_t usp_off;         // first patch of Usp in the LUT pool
     int64_t uip_off;         // first patch of Uip in the LUT pool
     int coef_off;            // first order of this sphere in the coefficient arrays
-    int tab_off;             // unused padding for alignment
+    int lin_stride;          // mixed path: row stride of the linear float2 tables (thetaR + 1, even)
 };
 
 // Host helpers (bs_host.cpp).

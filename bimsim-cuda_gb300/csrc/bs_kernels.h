@@ -9,6 +9,10 @@
 
 namespace bs {
 
+// Plane waves are processed in chunks of this many (after a Hilbert-curve
+// sort); the host supplies one bounding cone per chunk.
+constexpr int WAVE_CHUNK = 64;
+
 template <class T>
 struct cpx;
 using zd = cpx<double>;
@@ -37,11 +41,17 @@ void launch_us_lut_f64(const Scene& sc, const Sphere* sph, int s0, int s1, int a
                        cudaStream_t st);
 // mixed path: tex holds, for sphere s0 + j, the texture objects of
 // {Usp re, Usp im, Uip re, Uip im} at [4 j .. 4 j + 3]
+// lin: linear float2 tables (Sphere::usp_off / uip_off in float2 units, rows
+// of Sphere::lin_stride entries);
+// cones: one {axis, half-angle} per WAVE_CHUNK waves; counters[0..1] receive
+// the staged and total (sphere, chunk) counts of every block (may be null)
 void launch_us_lut_tex(const Scene& sc, const Sphere* sph, int s0, int s1, int accumulate, int finalize,
-                       const float4* kw4, const cpx<float>* ph, const unsigned long long* tex, const cpx<float>* Uf,
-                       cpx<float>* U, cudaStream_t st);
+                       const float4* kw4, const float4* cones, const cpx<float>* ph, const unsigned long long* tex,
+                       const float2* lin, const cpx<float>* Uf, cpx<float>* U, unsigned long long* counters,
+                       cudaStream_t st);
 void launch_lut_build_tex(const zd* tab, int rows, int L, const double* P, int Pstride, int thetaR,
-                          cudaSurfaceObject_t sre, cudaSurfaceObject_t sim, cudaStream_t st);
+                          cudaSurfaceObject_t sre, cudaSurfaceObject_t sim, float2* lin, int lin_stride,
+                          cudaStream_t st);
 template <class T>
 void launch_us_direct(const Scene& sc, const Sphere* sph, int lstride, const zd* A, const zd* B, const double* waves,
                       const cpx<T>* ph, const cpx<T>* Uf, cpx<T>* U, cudaStream_t st);

@@ -4,6 +4,8 @@
 // into the epilogue.
 #include <cuda_runtime.h>
 
+#include <climits>
+
 #include "bs_kernels.h"
 #include "bs_math.cuh"
 
@@ -384,87 +386,231 @@ __global__ void __launch_bounds__(128) us_lut_f64_kernel(Scene sc, const Sphere*
 // Mixed precision: per-(pixel, sphere) geometry in double, per-wave work in
 // float, per-chunk partial sums combined with Kahan compensation.
 //
-// The tables live in CUDA arrays (block-linear layout, separate real and
-// imaginary float planes, x = angle, y = radius) so that the gather of a
-// bilinear cell goes through the texture path, whose 2-D tiled layout keeps
-// the scattered lookups of neighbouring pixels in few cache lines.
-// tex2Dgather returns the four texels of the cell, (i, j+1), (i+1, j+1),
-// (i+1, j), (i, j) in x, y, z, w; the interpolation is done here with exact
-// single-precision weights, and clamp addressing reproduces the edge
-// behaviour of the reference's texture fetch.
-constexpr int UST_BLOCK = 256;  // 16 x 16 pixel tile
-constexpr int UST_CHUNK = 256;  // waves staged in shared memory at a time
+// A block owns a 16 x 16 pixel tile, one pixel per thread.  The waves arrive
+// sorted along a Hilbert curve and are processed in chunks of UST_CHUNK; the
+// host gives each chunk a bounding cone (axis c_k, half-angle beta_k).  For a
+// tile whose pixels all lie outside the sphere and see it within an angle
+// gamma of the tile-centre direction r_c, every lookup angle of a chunk lies
+// in angle(c_k, r_c) +- (beta_k + gamma) (triangle inequality on the sphere of
+// directions).  The table values of the tile's rows times that angular window
+// (float2, at most UST_STAGE of them) are copied to shared memory once per
+// chunk and the bilinear cells are read from there.  Chunks whose window does
+// not fit, and tiles touching or containing the sphere, read the cells through
+// the texture path instead: the tables also live in CUDA arrays (block-linear
+// layout, real and imaginary float planes, x = angle, y = radius) and
+// tex2Dgather returns the cell's four texels, (i, j+1), (i+1, j+1), (i+1, j),
+// (i, j) in x, y, z, w.  Both paths interpolate with the same single-precision
+// formula, so they give the same bits; edge cells clamp like the reference's
+// texture fetch.
+constexpr int UST_BLOCK = 256;      // 16 x 16 pixel tile
 
-__global__ void __launch_bounds__(UST_BLOCK, 3) us_lut_tex_kernel(Scene sc, const Sphere* __restrict__ sph, int s0, int s1,
-                                                                 int accumulate, int finalize,
-                                                                 const float4* __restrict__ kw4,
-                                                                 const cpx<float>* __restrict__ ph,
-                                                                 const unsigned long long* __restrict__ tex,
-                                                                 const cpx<float>* __restrict__ Uf,
-                                                                 cpx<float>* __restrict__ U) {
+// Fractional LUT angle index t = acos(c) tsc for c in [-1, 1] (c is clamped),
+// tsc = (thetaR - 1) / PI_REF, tscpi = tsc * pi.  acos(x) = sqrt(1 - x) g(x)
+// on [0, 1] with g analytic there (the square-root factorisation of acos at
+// x = 1, as in Abramowitz & Stegun 4.4.45-46), and acos(-x) = pi - acos(x).
+// g is our own degree-7 least-squares fit on 4000 Chebyshev nodes of [0, 1],
+// weighted for absolute error; evaluated in single precision the angle is
+// within 3.5e-7 rad of acos over [-1, 1] (about 1e-4 of one table column at
+// thetaR = 1024).
+__device__ __forceinline__ float theta_index(float c, float tsc, float tscpi) {
+    const float ax = fminf(fabsf(c), 1.f);
+    float s;
+    asm("sqrt.approx.f32 %0, %1;" : "=f"(s) : "f"(1.f - ax));
+    float g = -1.411853940e-03f;
+    g = fmaf(g, ax, 7.149144541e-03f);
+    g = fmaf(g, ax, -1.768672466e-02f);
+    g = fmaf(g, ax, 3.125903755e-02f);
+    g = fmaf(g, ax, -5.028845742e-02f);
+    g = fmaf(g, ax, 8.899561316e-02f);
+    g = fmaf(g, ax, -2.145996839e-01f);
+    g = fmaf(g, ax, 1.570796371e+00f);
+    const float v = (s * tsc) * g;
+    return c < 0.f ? tscpi - v : v;
+}
+
+// 8-byte global -> shared copy that does not go through registers (cp.async)
+__device__ __forceinline__ void copy_async8(float2* dst, const float2* src) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src) : "memory");
+}
+
+__device__ __forceinline__ void copy_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+constexpr int UST_CHUNK = WAVE_CHUNK;
+constexpr int UST_STAGE = 5400;     // float2 table values staged per chunk (43 KB; 4 blocks per SM)
+constexpr float UST_MARGIN = 2e-3f;  // radians added to the angular bounds
+
+__global__ void __launch_bounds__(UST_BLOCK, 4) us_lut_tex_kernel(Scene sc, const Sphere* __restrict__ sph, int s0, int s1,
+                                                                    int accumulate, int finalize,
+                                                                    const float4* __restrict__ kw4,
+                                                                    const float4* __restrict__ cones,
+                                                                    const cpx<float>* __restrict__ ph,
+                                                                    const unsigned long long* __restrict__ tex,
+                                                                    const float2* __restrict__ lin,
+                                                                    const cpx<float>* __restrict__ Uf,
+                                                                    cpx<float>* __restrict__ U,
+                                                                    unsigned long long* __restrict__ counters) {
+    extern __shared__ float2 s_stage[];
     __shared__ float4 s_k[UST_CHUNK];
     __shared__ float2 s_p[UST_CHUNK];
+    __shared__ int s_red[4][UST_BLOCK / 32];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     // each warp covers an 8 x 4 pixel block of the 16 x 16 tile
     const int tiles_u = (sc.R + 15) / 16;
-    const int iu = (blockIdx.x % tiles_u) * 16 + (lane & 7) + 8 * (warp & 1);
-    const int iv = (blockIdx.x / tiles_u) * 16 + (lane >> 3) + 4 * (warp >> 1);
+    const int tu = (blockIdx.x % tiles_u) * 16, tv = (blockIdx.x / tiles_u) * 16;
+    const int iu = tu + (lane & 7) + 8 * (warp & 1);
+    const int iv = tv + (lane >> 3) + 4 * (warp >> 1);
     const bool valid = iu < sc.R && iv < sc.R;
     const int idx = iv * sc.R + iu;
     double p[3];
     pixel_pos(sc, min(iu, sc.R - 1), min(iv, sc.R - 1), p);
+    // tile centre in single precision (bounds only, covered by the margins)
+    float pc[3];
+    {
+        const float u = ((float)tu + 7.5f) / (float)sc.R, v = ((float)tv + 7.5f) / (float)sc.R;
+#pragma unroll
+        for (int c = 0; c < 3; c++) pc[c] = (float)sc.A[c] + (float)sc.X[c] * u + (float)sc.Y[c] * v;
+    }
     float tot_r = 0.f, tot_i = 0.f, cmp_r = 0.f, cmp_i = 0.f;  // Kahan sum over chunk partials
     if (accumulate && valid) {
         tot_r = U[idx].re;
         tot_i = U[idx].im;
     }
+    const int nchunks = (sc.nk + UST_CHUNK - 1) / UST_CHUNK;
+    unsigned staged_chunks = 0;
     for (int s = s0; s < s1; s++) {
         const Sphere& S = sph[s];
         double r[3];
-        double d = dist_exact(p, S.p, r);
-        TableSel ts = select_table(S, d);
-        int ir = (int)floor(ts.x);
+        const double d = dist_exact(p, S.p, r);
+        const TableSel ts = select_table(S, d);
+        const int ir = (int)floor(ts.x);
         const float al = (float)(ts.x - ir);
         const float y = (float)ir + 1.0f;  // gather footprint rows ir, ir + 1
         const int k = 4 * (s - s0) + (d < S.a ? 2 : 0);
         const cudaTextureObject_t tre = tex[k], tim = tex[k + 1];
         float rx = 0.f, ry = 0.f, rz = 0.f, cb = 1.f;  // d == 0: cos(theta) := 1
         if (d != 0) {
-            double inv = 1.0 / d;
+            const double inv = 1.0 / d;
             rx = (float)(r[0] * inv);
             ry = (float)(r[1] * inv);
             rz = (float)(r[2] * inv);
             cb = 0.f;
         }
+        // ---- tile bounds: table rows and angular radius gamma ----
+        float cx = pc[0] - (float)S.p[0], cy = pc[1] - (float)S.p[1], cz = pc[2] - (float)S.p[2];
+        const float cl = sqrtf(cx * cx + cy * cy + cz * cz);
+        bool far_ok = valid ? (d >= S.a && d != 0) : true;
+        float gam = 0.f;
+        if (cl > 0.f) {
+            cx /= cl;
+            cy /= cl;
+            cz /= cl;
+            if (valid) gam = acosf(fminf(fmaxf(rx * cx + ry * cy + rz * cz, -1.f), 1.f));
+        } else {
+            far_ok = false;
+        }
+        int rlo = valid ? ir : INT_MAX, rhi = valid ? ir : INT_MIN;
+        rlo = __reduce_min_sync(0xffffffffu, rlo);
+        rhi = __reduce_max_sync(0xffffffffu, rhi);
+        int gbits = (int)__reduce_max_sync(0xffffffffu, (unsigned)__float_as_int(gam));
+        int ok = __all_sync(0xffffffffu, far_ok);
+        __syncthreads();  // s_red is reused for every sphere
+        if (lane == 0) {
+            s_red[0][warp] = rlo;
+            s_red[1][warp] = rhi;
+            s_red[2][warp] = gbits;
+            s_red[3][warp] = ok;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int w = 0; w < UST_BLOCK / 32; w++) {
+            rlo = min(rlo, s_red[0][w]);
+            rhi = max(rhi, s_red[1][w]);
+            gbits = max(gbits, s_red[2][w]);
+            ok = ok && s_red[3][w];
+        }
+        const float gam_all = __int_as_float(gbits) + UST_MARGIN;
+        // staged rows: [rlo, rhi + 1] clamped to the table
+        const int nrows = ok ? min(rhi + 1, ts.rows - 1) - rlo + 1 : 0;
+        const bool tile_staged = ok && nrows >= 1;
+        const int lr0 = min(max(ir - rlo, 0), max(nrows, 1) - 1);
+        const int lr1 = min(max(min(ir + 1, ts.rows - 1) - rlo, 0), max(nrows, 1) - 1);
+        const float2* table = lin + ts.off;
         const float tmax = (float)(S.thetaR - 1);
         const float tsc = (float)((S.thetaR - 1) / PI_REF);
+        const float tscpi = (float)((S.thetaR - 1) / PI_REF * TRUE_PI);
         const cpx<float>* phs = ph + (size_t)s * sc.nk;
-        for (int w0 = 0; w0 < sc.nk; w0 += UST_CHUNK) {
+        for (int ch = 0; ch < nchunks; ch++) {
+            const int w0 = ch * UST_CHUNK;
             const int nw = min(UST_CHUNK, sc.nk - w0);
-            __syncthreads();
+            int t_lo = 0, W = 1;
+            bool staged = false;
+            if (tile_staged) {
+                const float4 cone = cones[ch];
+                const float thc = acosf(fminf(fmaxf(cone.x * cx + cone.y * cy + cone.z * cz, -1.f), 1.f));
+                // columns up to thetaR: the linear rows carry a copy of the last column there
+                t_lo = max(0, (int)floorf((thc - cone.w - gam_all) * tsc) - 1);
+                const int t_hi = min(S.thetaR, (int)floorf((thc + cone.w + gam_all) * tsc) + 2);
+                W = t_hi - t_lo + 1;
+                staged = W >= 2 && nrows * W <= UST_STAGE;
+            }
+            __syncthreads();  // the previous chunk's readers are done
             if (threadIdx.x < nw) {
                 s_k[threadIdx.x] = kw4[w0 + threadIdx.x];
                 s_p[threadIdx.x] = make_float2(phs[w0 + threadIdx.x].re, phs[w0 + threadIdx.x].im);
             }
+            if (staged) {
+                // asynchronous copies, one table row per warp at a time, all in flight together
+                for (int rr = warp; rr < nrows; rr += UST_BLOCK / 32) {
+                    const float2* src = table + (size_t)(rlo + rr) * S.lin_stride + t_lo;
+                    float2* dst = s_stage + rr * W;
+                    for (int tt = lane; tt < W; tt += 32) copy_async8(dst + tt, src + tt);
+                }
+                copy_async_wait_all();
+            }
             __syncthreads();
             float ar = 0.f, ai = 0.f;
+            if (staged) {
+                staged_chunks++;
+                const float2* row0 = s_stage + lr0 * W;
+                const int drow = (lr1 - lr0) * W;
+                const unsigned lt_max = (unsigned)(W - 2);
 #pragma unroll 2
-            for (int w = 0; w < nw; w++) {
-                const float4 kk = s_k[w];
-                float c = fmaf(kk.x, rx, fmaf(kk.y, ry, fmaf(kk.z, rz, cb)));
-                c = fminf(fmaxf(c, -1.f), 1.f);
-                const float t = fminf(acosf(c) * tsc, tmax);
-                const float tf = floorf(t);
-                const float be = t - tf;
-                const float4 gr = tex2Dgather<float4>(tre, tf + 1.0f, y, 0);
-                const float4 gi = tex2Dgather<float4>(tim, tf + 1.0f, y, 0);
-                const float ar0 = fmaf(be, gr.z - gr.w, gr.w), ar1 = fmaf(be, gr.y - gr.x, gr.x);
-                const float ai0 = fmaf(be, gi.z - gi.w, gi.w), ai1 = fmaf(be, gi.y - gi.x, gi.x);
-                const float vr = fmaf(al, ar1 - ar0, ar0);
-                const float vi = fmaf(al, ai1 - ai0, ai0);
-                const float2 pw = s_p[w];
-                ar = fmaf(pw.x, vr, fmaf(-pw.y, vi, ar));
-                ai = fmaf(pw.x, vi, fmaf(pw.y, vr, ai));
+                for (int w = 0; w < nw; w++) {
+                    const float4 kk = s_k[w];
+                    const float c = fmaf(kk.x, rx, fmaf(kk.y, ry, kk.z * rz));  // cb = 0: every d > 0 here
+                    const float t = fminf(theta_index(c, tsc, tscpi), tmax);
+                    const float tf = floorf(t);
+                    const float be = t - tf;
+                    // in the window by construction; the unsigned clamp only keeps a bad bound in bounds
+                    const unsigned lt = min((unsigned)((int)tf - t_lo), lt_max);
+                    const float2* q = row0 + lt;
+                    const float2 e00 = q[0], e01 = q[1], e10 = q[drow], e11 = q[drow + 1];
+                    const float ar0 = fmaf(be, e01.x - e00.x, e00.x), ar1 = fmaf(be, e11.x - e10.x, e10.x);
+                    const float ai0 = fmaf(be, e01.y - e00.y, e00.y), ai1 = fmaf(be, e11.y - e10.y, e10.y);
+                    const float vr = fmaf(al, ar1 - ar0, ar0);
+                    const float vi = fmaf(al, ai1 - ai0, ai0);
+                    const float2 pw = s_p[w];
+                    ar = fmaf(pw.x, vr, fmaf(-pw.y, vi, ar));
+                    ai = fmaf(pw.x, vi, fmaf(pw.y, vr, ai));
+                }
+            } else {
+#pragma unroll 2
+                for (int w = 0; w < nw; w++) {
+                    const float4 kk = s_k[w];
+                    const float c = fmaf(kk.x, rx, fmaf(kk.y, ry, fmaf(kk.z, rz, cb)));
+                    const float t = fminf(theta_index(c, tsc, tscpi), tmax);
+                    const float tf = floorf(t);
+                    const float be = t - tf;
+                    const float4 gr = tex2Dgather<float4>(tre, tf + 1.0f, y, 0);
+                    const float4 gi = tex2Dgather<float4>(tim, tf + 1.0f, y, 0);
+                    const float ar0 = fmaf(be, gr.z - gr.w, gr.w), ar1 = fmaf(be, gr.y - gr.x, gr.x);
+                    const float ai0 = fmaf(be, gi.z - gi.w, gi.w), ai1 = fmaf(be, gi.y - gi.x, gi.x);
+                    const float vr = fmaf(al, ar1 - ar0, ar0);
+                    const float vi = fmaf(al, ai1 - ai0, ai0);
+                    const float2 pw = s_p[w];
+                    ar = fmaf(pw.x, vr, fmaf(-pw.y, vi, ar));
+                    ai = fmaf(pw.x, vi, fmaf(pw.y, vr, ai));
+                }
             }
             // Kahan: add the chunk partial to the running total
             const float yr = ar - cmp_r, yi = ai - cmp_i;
@@ -474,6 +620,10 @@ __global__ void __launch_bounds__(UST_BLOCK, 3) us_lut_tex_kernel(Scene sc, cons
             tot_r = tr;
             tot_i = ti;
         }
+    }
+    if (threadIdx.x == 0 && counters) {
+        atomicAdd(counters, (unsigned long long)staged_chunks);
+        atomicAdd(counters + 1, (unsigned long long)(s1 - s0) * nchunks);
     }
     if (!valid) return;
     if (finalize) {
@@ -492,11 +642,13 @@ __global__ void __launch_bounds__(UST_BLOCK, 3) us_lut_tex_kernel(Scene sc, cons
 }
 
 // LUT build into the real and imaginary planes of a CUDA array pair (same
-// sums as lut_build_kernel, written through surfaces).  `rows` counts one
-// spare row that repeats the last table row.
+// sums as lut_build_kernel, written through surfaces) and into the linear
+// float2 table used for staging.  `rows` counts one spare row of the planes
+// that repeats the last table row.
 __global__ void __launch_bounds__(256) lut_build_tex_kernel(const zd* __restrict__ tab, int rows, int L,
                                                               const double* __restrict__ P, int Pstride, int thetaR,
-                                                              cudaSurfaceObject_t sre, cudaSurfaceObject_t sim) {
+                                                              cudaSurfaceObject_t sre, cudaSurfaceObject_t sim,
+                                                              float2* __restrict__ lin, int lin_stride) {
     const int t = blockIdx.x * 32 + (threadIdx.x & 31);
     const int r = blockIdx.y * 8 + (threadIdx.x >> 5);
     if (t >= thetaR || r >= rows) return;
@@ -506,6 +658,11 @@ __global__ void __launch_bounds__(256) lut_build_tex_kernel(const zd* __restrict
     for (int l = 0; l < L; l++) acc = acc + c[l] * pl[l];
     surf2Dwrite((float)acc.re, sre, t * (int)sizeof(float), r);
     surf2Dwrite((float)acc.im, sim, t * (int)sizeof(float), r);
+    if (r < rows - 1) {
+        const float2 v = make_float2((float)acc.re, (float)acc.im);
+        lin[(size_t)r * lin_stride + t] = v;
+        if (t == thetaR - 1) lin[(size_t)r * lin_stride + thetaR] = v;  // clamped neighbour of the last column
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -699,17 +856,22 @@ void launch_us_lut_f64(const Scene& sc, const Sphere* sph, int s0, int s1, int a
 }
 
 void launch_us_lut_tex(const Scene& sc, const Sphere* sph, int s0, int s1, int accumulate, int finalize,
-                       const float4* kw4, const cpx<float>* ph, const unsigned long long* tex, const cpx<float>* Uf,
-                       cpx<float>* U, cudaStream_t st) {
+                       const float4* kw4, const float4* cones, const cpx<float>* ph, const unsigned long long* tex,
+                       const float2* lin, const cpx<float>* Uf, cpx<float>* U, unsigned long long* counters,
+                       cudaStream_t st) {
     int tiles = (sc.R + 15) / 16;
-    us_lut_tex_kernel<<<(unsigned)tiles * tiles, UST_BLOCK, 0, st>>>(sc, sph, s0, s1, accumulate, finalize, kw4, ph,
-                                                                      tex, Uf, U);
+    const int smem = UST_STAGE * (int)sizeof(float2);
+    // per device and cheap; a failure shows up as the launch error
+    cudaFuncSetAttribute(us_lut_tex_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    us_lut_tex_kernel<<<(unsigned)tiles * tiles, UST_BLOCK, smem, st>>>(sc, sph, s0, s1, accumulate, finalize, kw4,
+                                                                         cones, ph, tex, lin, Uf, U, counters);
 }
 
 void launch_lut_build_tex(const zd* tab, int rows, int L, const double* P, int Pstride, int thetaR,
-                          cudaSurfaceObject_t sre, cudaSurfaceObject_t sim, cudaStream_t st) {
+                          cudaSurfaceObject_t sre, cudaSurfaceObject_t sim, float2* lin, int lin_stride,
+                          cudaStream_t st) {
     dim3 grid(blocks_for(thetaR, 32), blocks_for(rows, 8));
-    lut_build_tex_kernel<<<grid, 256, 0, st>>>(tab, rows, L, P, Pstride, thetaR, sre, sim);
+    lut_build_tex_kernel<<<grid, 256, 0, st>>>(tab, rows, L, P, Pstride, thetaR, sre, sim, lin, lin_stride);
 }
 
 template <class T>

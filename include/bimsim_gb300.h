@@ -115,6 +115,10 @@ typedef struct bs_stats {
     double ms_detector;
     int64_t kernel_launches;
     int64_t us_interactions;  /* (pixel, sphere, wave) triples evaluated */
+    /* Mixed-precision LUT path: (pixel tile, sphere, wave chunk) units whose
+     * table window was staged in shared memory, and all such units. */
+    int64_t lut_chunks_staged;
+    int64_t lut_chunks_total;
 } bs_stats;
 
 typedef struct bs_ctx bs_ctx;

@@ -66,11 +66,18 @@ def scene(name):
                             us_lut_theta=128)
         assert p.supersample == 2
         return p, [(0.2, 0.1, 0.0, 1.0, 1.4, 0.05)], w(16, 0, 0.5, seed=9)
+    if name == "lut_staged":
+        # 64 x 64 pixels, 4 x 4 tiles of 16 x 16, most of them clear of both spheres: their LUT windows are
+        # staged in shared memory by the mixed kernel, the tiles touching a sphere use the texture path
+        p = abi.make_params(lam=2.5, condenser=(0, 0.5), objective=(0, 0.5), xy=(48, 0), resolution=64, padding=1,
+                            us_lut_r=100, us_lut_theta=300)
+        s = [(-6.0, 5.0, 0.0, 2.0, 1.4, 0.04), (9.0, -8.0, 1.0, 1.4, 1.5, 0.01)]
+        return p, s, w(256, 0, 0.5, seed=10)
     raise KeyError(name)
 
 
 ALL = ["lut", "lut_ufLUT", "direct_cfg1", "direct_multi", "plane_wave", "oblique_xz", "vector", "no_spheres",
-       "supersample"]
+       "supersample", "lut_staged"]
 _oracle_cache = {}
 
 
@@ -117,6 +124,19 @@ def test_mixed_matches_oracle(name):
     fld = {"U": rel(g["U"], U), "Uf": rel(g["Uf"], Uf)}
     assert max(img.values()) <= TOL_MIXED_IMG, (img, fld)
     assert max(fld.values()) <= TOL_MIXED_FIELD, (img, fld)
+
+
+def test_mixed_lut_kernel_uses_both_table_paths():
+    """The staged (shared-memory) and texture paths of the mixed LUT kernel both run in the
+    lut_staged scene; the parity tests above cover their values."""
+    g = run_gpu("lut_staged", BS_PREC_MIXED)
+    st = g["stats"]
+    tiles = (oracle_lib.geom(scene("lut_staged")[0]).R + 15) // 16
+    # tiles of 16 x 16 near-field pixels x 2 spheres x 4 wave chunks of 64
+    assert st.lut_chunks_total == tiles * tiles * 2 * 4
+    assert 0 < st.lut_chunks_staged < st.lut_chunks_total, (st.lut_chunks_staged, st.lut_chunks_total)
+    g64 = run_gpu("lut_staged", BS_PREC_FP64)
+    assert g64["stats"].lut_chunks_total == 0
 
 
 def test_images_are_derived_consistently():
@@ -177,6 +197,18 @@ def test_chunked_tables_match_single_pass():
     chunked = run_gpu("lut", BS_PREC_FP64, budget=one)
     assert rel(chunked["U"], full["U"]) <= 1e-14
     assert rel(chunked["D"], full["D"]) <= 1e-14
+
+
+def test_chunked_lut_budget_mixed():
+    """Mixed path, one sphere's tables at a time: 8-byte entries in linear rows of thetaR + 1 entries rounded
+    up to even (302 here), plus the texture planes, which count as a second copy."""
+    full = run_gpu("lut_staged", BS_PREC_MIXED)
+    p, s, _ = scene("lut_staged")
+    one = max((g.dR + g.aR) for g in (oracle_lib.sphere_geom(p, abi.Sphere(*sp)) for sp in s)) * 302 * 8 * 2
+    chunked = run_gpu("lut_staged", BS_PREC_MIXED, budget=one)
+    assert chunked["stats"].lut_chunks_total == full["stats"].lut_chunks_total
+    assert rel(chunked["U"], full["U"]) <= 1e-6
+    assert rel(chunked["D"], full["D"]) <= 1e-6
 
 
 def test_repeatable():
