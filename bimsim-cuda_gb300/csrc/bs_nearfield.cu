@@ -439,6 +439,18 @@ constexpr int UST_CHUNK = WAVE_CHUNK;
 constexpr int UST_STAGE = 5400;     // float2 table values staged per chunk (43 KB; 4 blocks per SM)
 constexpr float UST_MARGIN = 2e-3f;  // radians added to the angular bounds
 
+// Block-uniform values of one (tile, sphere) pair, kept in shared memory so
+// that they are re-read per chunk instead of holding registers through the
+// wave loops.
+struct TileSphere {
+    float cx, cy, cz;  // unit direction from the sphere to the tile centre
+    float gam;         // angular radius of the tile seen from the sphere, plus margin
+    float tsc, tscpi, tmax;
+    int rlo, nrows;    // staged table rows [rlo, rlo + nrows); nrows = 0: texture path only
+    int thetaR, lin_stride;
+    long long off;     // first entry of the table in the linear pool
+};
+
 __global__ void __launch_bounds__(UST_BLOCK, 4) us_lut_tex_kernel(Scene sc, const Sphere* __restrict__ sph, int s0, int s1,
                                                                     int accumulate, int finalize,
                                                                     const float4* __restrict__ kw4,
@@ -453,6 +465,7 @@ __global__ void __launch_bounds__(UST_BLOCK, 4) us_lut_tex_kernel(Scene sc, cons
     __shared__ float4 s_k[UST_CHUNK];
     __shared__ float2 s_p[UST_CHUNK];
     __shared__ int s_red[4][UST_BLOCK / 32];
+    __shared__ TileSphere s_ts;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     // each warp covers an 8 x 4 pixel block of the 16 x 16 tile
     const int tiles_u = (sc.R + 15) / 16;
@@ -460,26 +473,17 @@ __global__ void __launch_bounds__(UST_BLOCK, 4) us_lut_tex_kernel(Scene sc, cons
     const int iu = tu + (lane & 7) + 8 * (warp & 1);
     const int iv = tv + (lane >> 3) + 4 * (warp >> 1);
     const bool valid = iu < sc.R && iv < sc.R;
-    const int idx = iv * sc.R + iu;
-    double p[3];
-    pixel_pos(sc, min(iu, sc.R - 1), min(iv, sc.R - 1), p);
-    // tile centre in single precision (bounds only, covered by the margins)
-    float pc[3];
-    {
-        const float u = ((float)tu + 7.5f) / (float)sc.R, v = ((float)tv + 7.5f) / (float)sc.R;
-#pragma unroll
-        for (int c = 0; c < 3; c++) pc[c] = (float)sc.A[c] + (float)sc.X[c] * u + (float)sc.Y[c] * v;
-    }
     float tot_r = 0.f, tot_i = 0.f, cmp_r = 0.f, cmp_i = 0.f;  // Kahan sum over chunk partials
     if (accumulate && valid) {
-        tot_r = U[idx].re;
-        tot_i = U[idx].im;
+        tot_r = U[iv * sc.R + iu].re;
+        tot_i = U[iv * sc.R + iu].im;
     }
     const int nchunks = (sc.nk + UST_CHUNK - 1) / UST_CHUNK;
     unsigned staged_chunks = 0;
     for (int s = s0; s < s1; s++) {
         const Sphere& S = sph[s];
-        double r[3];
+        double p[3], r[3];
+        pixel_pos(sc, min(iu, sc.R - 1), min(iv, sc.R - 1), p);
         const double d = dist_exact(p, S.p, r);
         const TableSel ts = select_table(S, d);
         const int ir = (int)floor(ts.x);
@@ -496,85 +500,107 @@ __global__ void __launch_bounds__(UST_BLOCK, 4) us_lut_tex_kernel(Scene sc, cons
             cb = 0.f;
         }
         // ---- tile bounds: table rows and angular radius gamma ----
-        float cx = pc[0] - (float)S.p[0], cy = pc[1] - (float)S.p[1], cz = pc[2] - (float)S.p[2];
-        const float cl = sqrtf(cx * cx + cy * cy + cz * cz);
-        bool far_ok = valid ? (d >= S.a && d != 0) : true;
-        float gam = 0.f;
-        if (cl > 0.f) {
-            cx /= cl;
-            cy /= cl;
-            cz /= cl;
-            if (valid) gam = acosf(fminf(fmaxf(rx * cx + ry * cy + rz * cz, -1.f), 1.f));
-        } else {
-            far_ok = false;
-        }
-        int rlo = valid ? ir : INT_MAX, rhi = valid ? ir : INT_MIN;
-        rlo = __reduce_min_sync(0xffffffffu, rlo);
-        rhi = __reduce_max_sync(0xffffffffu, rhi);
-        int gbits = (int)__reduce_max_sync(0xffffffffu, (unsigned)__float_as_int(gam));
-        int ok = __all_sync(0xffffffffu, far_ok);
-        __syncthreads();  // s_red is reused for every sphere
-        if (lane == 0) {
-            s_red[0][warp] = rlo;
-            s_red[1][warp] = rhi;
-            s_red[2][warp] = gbits;
-            s_red[3][warp] = ok;
-        }
-        __syncthreads();
+        int rlo, rhi, ok;
+        {
+            // tile centre in single precision (bounds only, covered by the margins)
+            const float u = ((float)tu + 7.5f) / (float)sc.R, v = ((float)tv + 7.5f) / (float)sc.R;
+            float cx = (float)sc.A[0] + (float)sc.X[0] * u + (float)sc.Y[0] * v - (float)S.p[0];
+            float cy = (float)sc.A[1] + (float)sc.X[1] * u + (float)sc.Y[1] * v - (float)S.p[1];
+            float cz = (float)sc.A[2] + (float)sc.X[2] * u + (float)sc.Y[2] * v - (float)S.p[2];
+            const float cl = sqrtf(cx * cx + cy * cy + cz * cz);
+            bool far_ok = valid ? (d >= S.a && d != 0) : true;
+            float gam = 0.f;
+            if (cl > 0.f) {
+                cx /= cl;
+                cy /= cl;
+                cz /= cl;
+                if (valid) gam = acosf(fminf(fmaxf(rx * cx + ry * cy + rz * cz, -1.f), 1.f));
+            } else {
+                far_ok = false;
+            }
+            rlo = valid ? ir : INT_MAX;
+            rhi = valid ? ir : INT_MIN;
+            rlo = __reduce_min_sync(0xffffffffu, rlo);
+            rhi = __reduce_max_sync(0xffffffffu, rhi);
+            int gbits = (int)__reduce_max_sync(0xffffffffu, (unsigned)__float_as_int(gam));
+            ok = __all_sync(0xffffffffu, far_ok);
+            __syncthreads();  // s_red and s_ts are reused for every sphere
+            if (lane == 0) {
+                s_red[0][warp] = rlo;
+                s_red[1][warp] = rhi;
+                s_red[2][warp] = gbits;
+                s_red[3][warp] = ok;
+            }
+            __syncthreads();
 #pragma unroll
-        for (int w = 0; w < UST_BLOCK / 32; w++) {
-            rlo = min(rlo, s_red[0][w]);
-            rhi = max(rhi, s_red[1][w]);
-            gbits = max(gbits, s_red[2][w]);
-            ok = ok && s_red[3][w];
+            for (int w = 0; w < UST_BLOCK / 32; w++) {
+                rlo = min(rlo, s_red[0][w]);
+                rhi = max(rhi, s_red[1][w]);
+                gbits = max(gbits, s_red[2][w]);
+                ok = ok && s_red[3][w];
+            }
+            if (threadIdx.x == 0) {
+                s_ts.cx = cx;
+                s_ts.cy = cy;
+                s_ts.cz = cz;
+                s_ts.gam = __int_as_float(gbits) + UST_MARGIN;
+                s_ts.tsc = (float)((S.thetaR - 1) / PI_REF);
+                s_ts.tscpi = (float)((S.thetaR - 1) / PI_REF * TRUE_PI);
+                s_ts.tmax = (float)(S.thetaR - 1);
+                // staged rows: [rlo, rhi + 1] clamped to the table
+                s_ts.rlo = rlo;
+                s_ts.nrows = ok ? min(rhi + 1, ts.rows - 1) - rlo + 1 : 0;
+                s_ts.thetaR = S.thetaR;
+                s_ts.lin_stride = S.lin_stride;
+                s_ts.off = ts.off;
+            }
         }
-        const float gam_all = __int_as_float(gbits) + UST_MARGIN;
-        // staged rows: [rlo, rhi + 1] clamped to the table
-        const int nrows = ok ? min(rhi + 1, ts.rows - 1) - rlo + 1 : 0;
-        const bool tile_staged = ok && nrows >= 1;
-        const int lr0 = min(max(ir - rlo, 0), max(nrows, 1) - 1);
-        const int lr1 = min(max(min(ir + 1, ts.rows - 1) - rlo, 0), max(nrows, 1) - 1);
-        const float2* table = lin + ts.off;
-        const float tmax = (float)(S.thetaR - 1);
-        const float tsc = (float)((S.thetaR - 1) / PI_REF);
-        const float tscpi = (float)((S.thetaR - 1) / PI_REF * TRUE_PI);
-        const cpx<float>* phs = ph + (size_t)s * sc.nk;
+        // local rows of this pixel in the staged block (clamped, so always in bounds)
+        const int nrows_b = ok ? min(rhi + 1, ts.rows - 1) - rlo + 1 : 1;
+        const int lr0 = min(max(ir - rlo, 0), max(nrows_b, 1) - 1);
+        const int lr1 = min(max(min(ir + 1, ts.rows - 1) - rlo, 0), max(nrows_b, 1) - 1);
         for (int ch = 0; ch < nchunks; ch++) {
             const int w0 = ch * UST_CHUNK;
             const int nw = min(UST_CHUNK, sc.nk - w0);
+            __syncthreads();  // the previous chunk's readers are done; s_ts is written
+            const int nrows = s_ts.nrows;
             int t_lo = 0, W = 1;
             bool staged = false;
-            if (tile_staged) {
+            if (nrows > 0) {
                 const float4 cone = cones[ch];
-                const float thc = acosf(fminf(fmaxf(cone.x * cx + cone.y * cy + cone.z * cz, -1.f), 1.f));
+                const float tsc = s_ts.tsc, gam = s_ts.gam;
+                const float thc = acosf(fminf(fmaxf(cone.x * s_ts.cx + cone.y * s_ts.cy + cone.z * s_ts.cz, -1.f), 1.f));
                 // columns up to thetaR: the linear rows carry a copy of the last column there
-                t_lo = max(0, (int)floorf((thc - cone.w - gam_all) * tsc) - 1);
-                const int t_hi = min(S.thetaR, (int)floorf((thc + cone.w + gam_all) * tsc) + 2);
+                t_lo = max(0, (int)floorf((thc - cone.w - gam) * tsc) - 1);
+                const int t_hi = min(s_ts.thetaR, (int)floorf((thc + cone.w + gam) * tsc) + 2);
                 W = t_hi - t_lo + 1;
                 staged = W >= 2 && nrows * W <= UST_STAGE;
             }
-            __syncthreads();  // the previous chunk's readers are done
             if (threadIdx.x < nw) {
+                const cpx<float> pv = ph[(size_t)s * sc.nk + w0 + threadIdx.x];
                 s_k[threadIdx.x] = kw4[w0 + threadIdx.x];
-                s_p[threadIdx.x] = make_float2(phs[w0 + threadIdx.x].re, phs[w0 + threadIdx.x].im);
+                s_p[threadIdx.x] = make_float2(pv.re, pv.im);
             }
             if (staged) {
                 // asynchronous copies, one table row per warp at a time, all in flight together
+                const float2* table = lin + s_ts.off + (size_t)s_ts.rlo * s_ts.lin_stride + t_lo;
+                const int ls = s_ts.lin_stride;
                 for (int rr = warp; rr < nrows; rr += UST_BLOCK / 32) {
-                    const float2* src = table + (size_t)(rlo + rr) * S.lin_stride + t_lo;
+                    const float2* src = table + (size_t)rr * ls;
                     float2* dst = s_stage + rr * W;
                     for (int tt = lane; tt < W; tt += 32) copy_async8(dst + tt, src + tt);
                 }
                 copy_async_wait_all();
             }
             __syncthreads();
+            const float tsc = s_ts.tsc, tscpi = s_ts.tscpi, tmax = s_ts.tmax;
             float ar = 0.f, ai = 0.f;
             if (staged) {
                 staged_chunks++;
                 const float2* row0 = s_stage + lr0 * W;
                 const int drow = (lr1 - lr0) * W;
                 const unsigned lt_max = (unsigned)(W - 2);
-#pragma unroll 2
+#pragma unroll 1
                 for (int w = 0; w < nw; w++) {
                     const float4 kk = s_k[w];
                     const float c = fmaf(kk.x, rx, fmaf(kk.y, ry, kk.z * rz));  // cb = 0: every d > 0 here
@@ -594,7 +620,7 @@ __global__ void __launch_bounds__(UST_BLOCK, 4) us_lut_tex_kernel(Scene sc, cons
                     ai = fmaf(pw.x, vi, fmaf(pw.y, vr, ai));
                 }
             } else {
-#pragma unroll 2
+#pragma unroll 1
                 for (int w = 0; w < nw; w++) {
                     const float4 kk = s_k[w];
                     const float c = fmaf(kk.x, rx, fmaf(kk.y, ry, fmaf(kk.z, rz, cb)));
@@ -626,7 +652,10 @@ __global__ void __launch_bounds__(UST_BLOCK, 4) us_lut_tex_kernel(Scene sc, cons
         atomicAdd(counters + 1, (unsigned long long)(s1 - s0) * nchunks);
     }
     if (!valid) return;
+    const int idx = iv * sc.R + iu;
     if (finalize) {
+        double p[3];
+        pixel_pos(sc, iu, iv, p);
         bool outside = true;
         for (int s = 0; s < sc.ns; s++) {
             const Sphere& S = sph[s];
