@@ -130,6 +130,38 @@ def cpu_reference(p, spheres, waves, rows, threads):
     return time.perf_counter() - t0, R
 
 
+def run_served(args):
+    """Served workload: Poisson arrivals of seeded requests (see scenes.served_trace)
+    into the serving front end; latencies are submit -> image ready."""
+    from bimsim_gb300 import BS_PREC_MIXED, Server, scenes
+    trace = scenes.served_trace(args.serve_requests, seed=4, resolutions=(128, 256, 512, 1024),
+                                rate_hz=args.serve_rate)
+    lookups = sum((p.resolution * p.supersample * 3) ** 2 * len(s) * len(w) for _, p, s, w in trace)
+    with Server(workers=args.serve_workers) as srv:
+        t0 = time.perf_counter()
+        tickets = []
+        for t_arr, p, s, w in trace:
+            dt = t_arr - (time.perf_counter() - t0)
+            if dt > 0:
+                time.sleep(dt)
+            tickets.append(srv.submit(p, s, waves=w, precision=BS_PREC_MIXED))
+        gpu_ms = 0.0
+        for t in tickets:
+            srv.wait(t, 600.0)
+            _, info = srv.fetch(t)
+            gpu_ms += info.ms_gpu
+        wall = time.perf_counter() - t0
+        st = srv.stats()
+    return {"p50_ms": st.p50_ms, "p99_ms": st.p99_ms, "mean_ms": st.mean_ms, "max_ms": st.max_ms,
+            "requests": st.completed, "failed": st.failed, "lut_reuses": st.lut_reuses,
+            "workers": args.serve_workers, "arrival_rate_hz": args.serve_rate, "wall_s": wall,
+            "requests_per_s": st.completed / wall, "lookups": lookups, "sum_gpu_ms": gpu_ms,
+            "peak_bytes": st.bytes_peak, "budget_bytes": st.hbm_budget,
+            "trace": "Poisson arrivals; res in {128,256,512,1024}^2 (2048^2 left out of the default run), "
+                     "S ~ U{1..200}, lambda ~ U(2.5,12.5) um, nk in {200,1000,2000}, config-2 scene family, "
+                     "25% repeat an earlier scene with new directions; mixed precision"}
+
+
 def run_reference(args):
     ws, rank, _ = dist_env()
     if rank != 0:
@@ -255,6 +287,8 @@ def run_gb300(args):
         c2.simulate(BS_PREC_MIXED)
         mix = c2.image(BS_IMG_INTENSITY, f64=True)
     rel = float(np.linalg.norm(mix - ref) / np.linalg.norm(ref))
+    # ---- served latency (after the timed regions) ----
+    served = None if args.no_serve or ws > 1 else run_served(args)
     # ---- CPU baseline (oracle on a bounded band of rows) ----
     cpu = None
     if not args.no_cpu:
@@ -287,6 +321,7 @@ def run_gb300(args):
                                  "case": "intensity image, same scene family at 256^2, 8 spheres, 200 waves"},
         "clocks": clocks,
         "cpu_baseline": cpu,
+        "served": served,
     }
     print(json.dumps(line))
 
@@ -299,6 +334,10 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--ref-rows", type=int, default=int(os.environ.get("BS_REF_ROWS", "12")))
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--serve-requests", type=int, default=32)
+    ap.add_argument("--serve-rate", type=float, default=1.0)
+    ap.add_argument("--serve-workers", type=int, default=4)
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

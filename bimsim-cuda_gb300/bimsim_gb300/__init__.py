@@ -8,8 +8,8 @@ is missing.
 from .abi import (BS_FIELD_INCIDENT, BS_FIELD_TOTAL, BS_IMG_ABSORBANCE, BS_IMG_INCIDENT, BS_IMG_INTENSITY,
                   BS_IMG_TRANSMITTANCE, BS_PREC_FP64, BS_PREC_MIXED, Info, Params, Sphere, Stats, make_params,
                   sphere_array)
-from .lib import BimsimError, Context, library, library_path
+from .lib import BimsimError, Context, Server, estimate_bytes, library, library_path
 
 __all__ = ["BS_FIELD_INCIDENT", "BS_FIELD_TOTAL", "BS_IMG_ABSORBANCE", "BS_IMG_INCIDENT", "BS_IMG_INTENSITY",
            "BS_IMG_TRANSMITTANCE", "BS_PREC_FP64", "BS_PREC_MIXED", "BimsimError", "Context", "Info", "Params",
-           "Sphere", "Stats", "library", "library_path", "make_params", "sphere_array"]
+           "Server", "Sphere", "Stats", "estimate_bytes", "library", "library_path", "make_params", "sphere_array"]

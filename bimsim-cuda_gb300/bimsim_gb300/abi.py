@@ -56,7 +56,29 @@ class Stats(C.Structure):
     _fields_ = [("ms_total", C.c_double), ("ms_uf", C.c_double), ("ms_mie", C.c_double),
                 ("ms_lut", C.c_double), ("ms_us", C.c_double), ("ms_detector", C.c_double),
                 ("kernel_launches", C.c_int64), ("us_interactions", C.c_int64),
-                ("lut_chunks_staged", C.c_int64), ("lut_chunks_total", C.c_int64)]
+                ("lut_chunks_staged", C.c_int64), ("lut_chunks_total", C.c_int64),
+                ("lut_tables_built", C.c_int64), ("reserved", C.c_int64)]
+
+
+class ServerConfig(C.Structure):
+    _fields_ = [("workers", C.c_int32), ("dry_run", C.c_int32), ("hbm_budget", C.c_uint64)]
+
+
+class Request(C.Structure):
+    _fields_ = [("params", Params), ("spheres", C.c_void_p), ("n_spheres", C.c_int32), ("n_waves", C.c_int32),
+                ("waves", C.c_void_p), ("precision", C.c_int32), ("image", C.c_int32)]
+
+
+class ResultInfo(C.Structure):
+    _fields_ = [("ms_queued", C.c_double), ("ms_total", C.c_double), ("ms_gpu", C.c_double),
+                ("status", C.c_int32), ("lut_reused", C.c_int32), ("worker", C.c_int32), ("reserved", C.c_int32)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("submitted", C.c_int64), ("completed", C.c_int64), ("failed", C.c_int64), ("queued", C.c_int64),
+                ("running", C.c_int64), ("lut_reuses", C.c_int64), ("p50_ms", C.c_double), ("p99_ms", C.c_double),
+                ("mean_ms", C.c_double), ("max_ms", C.c_double), ("bytes_in_use", C.c_uint64),
+                ("bytes_peak", C.c_uint64), ("hbm_budget", C.c_uint64)]
 
 
 def make_params(lam=1.0, amplitude=1.0, k_dir=(0.0, 0.0, 1.0), focus=(0.0, 0.0, 0.0),

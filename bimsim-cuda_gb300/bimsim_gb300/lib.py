@@ -51,6 +51,17 @@ def library():
         "bs_get_lut": ([vp, i32, i32, vp, sz], C.c_int),
         "bs_measure_fma_peak": ([vp, vp], C.c_int),
         "bs_mie_noalloc": ([vp, i32, i32, C.c_double, vp, vp, vp], C.c_int),
+        "bs_set_params": ([vp, vp], C.c_int),
+        "bs_set_lut_reuse": ([vp, i32], C.c_int),
+        "bs_release_buffers": ([vp], C.c_int),
+        "bs_estimate_bytes": ([vp, vp, i32, i32, C.c_int, C.c_uint64, C.POINTER(C.c_uint64)], C.c_int),
+        "bs_server_create": ([vp, C.POINTER(vp)], C.c_int),
+        "bs_server_destroy": ([vp], C.c_int),
+        "bs_submit": ([vp, vp, C.POINTER(C.c_uint64)], C.c_int),
+        "bs_poll": ([vp, C.c_uint64, C.POINTER(i32)], C.c_int),
+        "bs_wait": ([vp, C.c_uint64, C.c_double], C.c_int),
+        "bs_fetch": ([vp, C.c_uint64, vp, sz, vp], C.c_int),
+        "bs_server_get_stats": ([vp, vp], C.c_int),
     }
     for name, (args, res) in proto.items():
         f = getattr(lib, name)
@@ -161,3 +172,102 @@ class Context:
 
     def write_envi(self, kind, path, append, band_value):
         self._check(self.lib.bs_write_envi(self.h, kind, path.encode(), 1 if append else 0, band_value))
+
+    def set_params(self, params):
+        self._check(self.lib.bs_set_params(self.h, C.byref(params)))
+        self.params = params
+
+    def set_lut_reuse(self, enable):
+        self._check(self.lib.bs_set_lut_reuse(self.h, 1 if enable else 0))
+
+    def release_buffers(self):
+        self._check(self.lib.bs_release_buffers(self.h))
+
+
+def estimate_bytes(params, spheres, n_waves, precision=abi.BS_PREC_MIXED, lut_budget=0):
+    """Device bytes a context holds after simulating this scene (host-only estimate)."""
+    lib = library()
+    arr, n = abi.sphere_array(spheres)
+    out = C.c_uint64()
+    st = lib.bs_estimate_bytes(C.byref(params), C.cast(arr, C.c_void_p), n, n_waves, precision, lut_budget,
+                               C.byref(out))
+    if st != 0:
+        raise BimsimError(st, lib.bs_last_error().decode())
+    return out.value
+
+
+class Server:
+    """Serving front end: submit slice requests, poll or wait, fetch images."""
+
+    def __init__(self, workers=4, hbm_budget=0, dry_run=False):
+        self.lib = library()
+        cfg = abi.ServerConfig(workers, 1 if dry_run else 0, hbm_budget)
+        h = C.c_void_p()
+        self._check(self.lib.bs_server_create(C.byref(cfg), C.byref(h)))
+        self.h = h
+        self._res = {}
+
+    def _check(self, st):
+        if st != 0:
+            raise BimsimError(st, self.lib.bs_last_error().decode())
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.bs_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def submit(self, params, spheres, waves=None, n_waves=None, precision=abi.BS_PREC_MIXED,
+               image=abi.BS_IMG_INTENSITY):
+        """waves: (nk, 3) unit directions, or None with n_waves for the compat sampler."""
+        arr, n = abi.sphere_array(spheres)
+        q = abi.Request()
+        q.params = params
+        q.spheres = C.cast(arr, C.c_void_p)
+        q.n_spheres = n
+        keep = None
+        if waves is not None:
+            keep = np.ascontiguousarray(waves, dtype=np.float64).reshape(-1)
+            q.waves = _p(keep)
+            q.n_waves = keep.size // 3
+        else:
+            q.waves = None
+            q.n_waves = n_waves or 0
+        q.precision = precision
+        q.image = image
+        t = C.c_uint64()
+        self._check(self.lib.bs_submit(self.h, C.byref(q), C.byref(t)))
+        self._res[t.value] = params.resolution
+        return t.value
+
+    def poll(self, ticket):
+        d = C.c_int32()
+        self._check(self.lib.bs_poll(self.h, ticket, C.byref(d)))
+        return bool(d.value)
+
+    def wait(self, ticket, timeout=-1.0):
+        self._check(self.lib.bs_wait(self.h, ticket, timeout))
+
+    def fetch(self, ticket):
+        """(image float32 res x res, ResultInfo); raises if the run failed."""
+        res = self._res.pop(ticket)
+        out = np.zeros(res * res, dtype=np.float32)
+        info = abi.ResultInfo()
+        self._check(self.lib.bs_fetch(self.h, ticket, _p(out), out.size, C.byref(info)))
+        return out.reshape(res, res), info
+
+    def stats(self):
+        s = abi.ServerStats()
+        self._check(self.lib.bs_server_get_stats(self.h, C.byref(s)))
+        return s

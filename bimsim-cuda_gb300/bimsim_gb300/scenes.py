@@ -91,3 +91,32 @@ def config5(resolution=4096, n_spheres=1000, samples=2000):
                         us_lut_r=4096, us_lut_theta=1024, uf_lut_r=4096)
     spheres = random_spheres(n_spheres, 400.0, 2.0, 20.0, seed=5, z_slab=60.0)
     return p, spheres, mc_waves(samples, 0.0, 0.5, seed=5)
+
+
+def served_trace(n, seed=4, resolutions=(128, 256, 512, 1024, 2048), rate_hz=1.0, repeat_frac=0.25):
+    """Requests of the served workload: Poisson arrivals at rate_hz, res from
+    `resolutions`, S ~ U{1..200} spheres as in config 2 (100 um field, a ~ U(1, 5),
+    n ~ U(1.2, 1.6) + i U(0, 0.05); a slab |z| < 30 um once the plane is too
+    crowded), lambda ~ U(2.5, 12.5) um, nk from {200, 1000, 2000}, LUTs of 4096 x
+    1024; a fraction repeat_frac of the requests re-images an earlier scene
+    with new directions.  Returns [(t_arrival_s, params, spheres, waves)]."""
+    g = rng(seed)
+    out = []
+    t = 0.0
+    for i in range(n):
+        t += g.exponential(1.0 / rate_hz)
+        if out and g.uniform() < repeat_frac:
+            _, p, s, w = out[int(g.integers(0, len(out)))]
+            w = mc_waves(len(w), 0.0, 0.5, seed=seed * 100003 + i)
+            out.append((t, p, s, w))
+            continue
+        res = int(g.choice(resolutions))
+        ns = int(g.integers(1, 201))
+        lam = float(g.uniform(2.5, 12.5))
+        nk = int(g.choice([200, 1000, 2000]))
+        p = abi.make_params(lam=lam, condenser=(0.0, 0.5), objective=(0.0, 0.5), xy=(100.0, 0.0),
+                            resolution=res, padding=1, field_order=10, lut_us=True, lut_uf=True,
+                            us_lut_r=4096, us_lut_theta=1024, uf_lut_r=4096)
+        s = random_spheres(ns, 100.0, 1.0, 5.0, seed=seed * 1009 + i, z_slab=0.0 if ns <= 60 else 30.0)
+        out.append((t, p, s, mc_waves(nk, 0.0, 0.5, seed=seed * 7919 + i)))
+    return out

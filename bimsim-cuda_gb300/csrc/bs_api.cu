@@ -7,6 +7,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <memory>
 #include <string>
 #include <type_traits>
 #include <vector>
@@ -172,7 +173,28 @@ struct bs_ctx {
     int64_t launches = 0;
     int64_t interactions = 0;
     bs_stats stats{};
+    // table reuse between runs (bs_set_lut_reuse)
+    bool reuse = false;
+    bool lut_valid = false;
+    std::vector<double> lut_key;
 };
+
+// Every linear device buffer of a context.
+static std::vector<DevBuf*> ctx_bufs(bs_ctx* c) {
+    return {&c->d_sph, &c->d_waves, &c->d_kw4, &c->d_ph, &c->d_A, &c->d_B, &c->d_mie, &c->d_tab,
+            &c->d_tabscr, &c->d_legP, &c->d_lut, &c->d_uft, &c->d_uftscr, &c->d_fields, &c->d_su,
+            &c->d_sv, &c->d_mask, &c->d_wx, &c->d_wy, &c->d_wix, &c->d_wiy, &c->d_f1, &c->d_f2,
+            &c->d_g1, &c->d_I, &c->d_D, &c->d_img, &c->d_cones, &c->d_cnt};
+}
+
+static void release_all(bs_ctx* c) {
+    for (DevBuf* b : ctx_bufs(c)) b->release();
+    for (auto& sl : c->slots) sl.release();
+    c->d_texobj.release();
+    c->legP_theta = c->legP_L = 0;
+    c->lut_valid = false;
+    c->have = false;
+}
 
 static size_t elem_r(int prec) { return prec == BS_PREC_FP64 ? sizeof(double) : sizeof(float); }
 
@@ -211,17 +233,20 @@ bs_status bs_create(const bs_params* params, bs_ctx** out) {
 bs_status bs_destroy(bs_ctx* c) {
     if (!c) return BS_OK;
     if (c->st) cudaStreamSynchronize(c->st);
-    DevBuf* bufs[] = {&c->d_sph, &c->d_waves, &c->d_kw4, &c->d_ph, &c->d_A, &c->d_B, &c->d_mie, &c->d_tab,
-                      &c->d_tabscr, &c->d_legP, &c->d_lut, &c->d_uft, &c->d_uftscr, &c->d_fields, &c->d_su,
-                      &c->d_sv, &c->d_mask, &c->d_wx, &c->d_wy, &c->d_wix, &c->d_wiy, &c->d_f1, &c->d_f2,
-                      &c->d_g1, &c->d_I, &c->d_D, &c->d_img, &c->d_cones, &c->d_cnt};
-    for (DevBuf* b : bufs) b->release();
-    for (auto& sl : c->slots) sl.release();
-    c->d_texobj.release();
+    release_all(c);
     for (int i = 0; i < 6; i++)
         if (c->ev[i]) cudaEventDestroy(c->ev[i]);
     if (c->st) cudaStreamDestroy(c->st);
     delete c;
+    return BS_OK;
+}
+
+bs_status bs_set_params(bs_ctx* c, const bs_params* params) {
+    if (!c || !params) return fail(BS_ERR_ARG, "bs_set_params: null argument");
+    std::string why;
+    if (!valid_params(params, why)) return fail(BS_ERR_ARG, "bs_set_params: %s", why.c_str());
+    c->prm = *params;
+    c->have = false;
     return BS_OK;
 }
 
@@ -345,21 +370,34 @@ static bs_status derive(bs_ctx* c) {
 // ---------------------------------------------------------------------------
 // The band-limited detector (microscope.cu:495-526, 608-662)
 // ---------------------------------------------------------------------------
+// Frequency of FFT bin i as the reference's bandpass kernel assigns it (note
+// -(R-1-i) rather than -(R-i) on the negative side).
+static double bin_freq(int i, int R, double step) { return (i <= R / 2) ? i * step : -(double)(R - 1 - i) * step; }
+
+// Bins along u and v inside the objective's outer NA (the only ones the
+// band-pass keeps), with the frequency steps.
+static void passbands(const bs_ctx* c, std::vector<int>& su, std::vector<int>& sv, double& du, double& dv) {
+    const int R = c->R;
+    du = 1.0 / std::sqrt(c->sc.X[0] * c->sc.X[0] + c->sc.X[1] * c->sc.X[1] + c->sc.X[2] * c->sc.X[2]);
+    dv = 1.0 / std::sqrt(c->sc.Y[0] * c->sc.Y[0] + c->sc.Y[1] * c->sc.Y[1] + c->sc.Y[2] * c->sc.Y[2]);
+    const double hi = c->prm.objective[1] / c->prm.lambda;
+    su.clear();
+    sv.clear();
+    for (int i = 0; i < R; i++) {
+        if (std::fabs(bin_freq(i, R, du)) <= hi) su.push_back(i);
+        if (std::fabs(bin_freq(i, R, dv)) <= hi) sv.push_back(i);
+    }
+}
+
 template <class T>
 static bs_status run_detector(bs_ctx* c) {
     const bs_params& p = c->prm;
     const int R = c->R;
-    double du = 1.0 / std::sqrt(c->sc.X[0] * c->sc.X[0] + c->sc.X[1] * c->sc.X[1] + c->sc.X[2] * c->sc.X[2]);
-    double dv = 1.0 / std::sqrt(c->sc.Y[0] * c->sc.Y[0] + c->sc.Y[1] * c->sc.Y[1] + c->sc.Y[2] * c->sc.Y[2]);
-    double lo = p.objective[0] / p.lambda, hi = p.objective[1] / p.lambda;
-    // frequency of bin i as the reference's bandpass kernel assigns it (note
-    // -(R-1-i) rather than -(R-i) on the negative side)
-    auto freq = [R](int i, double step) { return (i <= R / 2) ? i * step : -(double)(R - 1 - i) * step; };
+    double du, dv;
     std::vector<int> su, sv;
-    for (int i = 0; i < R; i++) {
-        if (std::fabs(freq(i, du)) <= hi) su.push_back(i);
-        if (std::fabs(freq(i, dv)) <= hi) sv.push_back(i);
-    }
+    passbands(c, su, sv, du, dv);
+    double lo = p.objective[0] / p.lambda, hi = p.objective[1] / p.lambda;
+    auto freq = [R](int i, double step) { return bin_freq(i, R, step); };
     const int Nu = (int)su.size(), Nv = (int)sv.size(), C = c->crop, res = c->res;
     CK(c->d_D.ensure(2 * (size_t)res * res * sizeof(T)));
     if (Nu == 0 || Nv == 0) {
@@ -433,21 +471,18 @@ static bs_status run_detector(bs_ctx* c) {
 // thetaR + 1 entries (the last column repeated, rounded up to an even count
 // for 16-byte rows), and a second copy of every entry in the texture planes,
 // which also counts against the budget.
-static bs_status plan_luts(bs_ctx* c, bool mixed, std::vector<int>& chunk_start, size_t& pool, size_t& maxrows,
-                           size_t& maxL) {
+static bs_status plan_tables(std::vector<Sphere>& hs, bool mixed, size_t budget, std::vector<int>& chunk_start,
+                             size_t& pool, size_t& maxrows, size_t& maxL) {
     const size_t patch = mixed ? sizeof(float2) : sizeof(Patch<double>);
     const size_t copies = mixed ? 2 : 1;
-    const int ns = (int)c->hs.size();
-    size_t free_b = 0, total_b = 0;
-    CK(cudaMemGetInfo(&free_b, &total_b));
-    size_t budget = c->budget ? c->budget : (size_t)(0.80 * (double)(free_b + c->d_lut.n * copies));
+    const int ns = (int)hs.size();
     chunk_start.clear();
     size_t acc = 0;
     pool = 0;
     maxrows = 0;
     maxL = 0;
     for (int i = 0; i < ns; i++) {
-        Sphere& S = c->hs[i];
+        Sphere& S = hs[i];
         S.lin_stride = mixed ? ((S.thetaR + 2) & ~1) : S.thetaR;
         size_t need = (size_t)(S.dR + S.aR) * S.lin_stride * patch;
         if (need * copies > budget)
@@ -466,6 +501,17 @@ static bs_status plan_luts(bs_ctx* c, bool mixed, std::vector<int>& chunk_start,
     }
     chunk_start.push_back(ns);
     return BS_OK;
+}
+
+static bs_status plan_luts(bs_ctx* c, bool mixed, std::vector<int>& chunk_start, size_t& pool, size_t& maxrows,
+                           size_t& maxL) {
+    size_t budget = c->budget;
+    if (!budget) {
+        size_t free_b = 0, total_b = 0;
+        CK(cudaMemGetInfo(&free_b, &total_b));
+        budget = (size_t)(0.80 * (double)(free_b + c->d_lut.n * (mixed ? 2 : 1)));
+    }
+    return plan_tables(c->hs, mixed, budget, chunk_start, pool, maxrows, maxL);
 }
 
 // Order plane waves along a Hilbert curve of their projection on the plane
@@ -653,6 +699,20 @@ static bs_status run_nearfield(bs_ctx* c) {
         const int nchunks = (int)chunk_start.size() - 1;
         int max_chunk = 0;
         for (int ci = 0; ci < nchunks; ci++) max_chunk = std::max(max_chunk, chunk_start[ci + 1] - chunk_start[ci]);
+        // tables of the previous run still in the pool and in the texture slots?
+        std::vector<double> key;
+        if (c->reuse && nchunks == 1) {
+            key = {fp64 ? 1.0 : 0.0, sc.kmag, (double)c->Lmax, (double)ns};
+            for (const Sphere& S : c->hs) {
+                const double v[] = {S.p[0], S.p[1], S.p[2], S.a, S.n_re, S.n_im, S.dmin, S.dmax, S.r0,
+                                    (double)S.Nl, (double)S.aR, (double)S.dR, (double)S.thetaR,
+                                    (double)S.lin_stride, (double)S.usp_off, (double)S.uip_off};
+                key.insert(key.end(), v, v + sizeof(v) / sizeof(v[0]));
+            }
+        }
+        const bool reuse_now = !key.empty() && c->lut_valid && key == c->lut_key;
+        c->lut_valid = false;  // set again below once this run's tables are complete
+        c->stats.lut_tables_built = reuse_now ? 0 : ns;
         if (!fp64 && ns > 0) {
             if ((int)c->slots.size() < max_chunk) c->slots.resize(max_chunk);
             CK(c->d_texobj.ensure((size_t)4 * max_chunk * sizeof(unsigned long long)));
@@ -670,6 +730,11 @@ static bs_status run_nearfield(bs_ctx* c) {
             for (int i = s0; i < s1; i++) {
                 const Sphere& S = c->hs[i];
                 const int L = S.Nl + 1;
+                if (reuse_now) {
+                    if (!fp64)
+                        for (int k = 0; k < 4; k++) handles.push_back(c->slots[i - s0].tex[k]);
+                    continue;
+                }
                 launch_coef_rows(S, sc.kmag, c->d_A.as<zd>(), c->d_B.as<zd>(), c->d_tab.as<zd>(),
                                  c->d_tabscr.as<double>(), c->st);
                 LAUNCHED(c);
@@ -718,13 +783,115 @@ static bs_status run_nearfield(bs_ctx* c) {
             // the handle list and the table slots are reused by the next chunk
             if (!fp64 && ci + 1 < std::max(1, nchunks)) CK(cudaStreamSynchronize(c->st));
         }
+        if (!key.empty()) {
+            c->lut_key.swap(key);
+            c->lut_valid = true;
+        }
         c->interactions = (long long)R * R * ns * nk;
     }
     cudaEventRecord(c->ev[4], c->st);
     return BS_OK;
 }
 
+// Device bytes the buffers of run_nearfield and run_detector reach for the
+// derived scene of `c` (each DevBuf at least 256 bytes; texture planes as
+// width x height floats, as bs_get_info counts them).  0 if the tables do not
+// fit lut_budget.
+static size_t estimate_bytes(bs_ctx* c, bool fp64, size_t lut_budget) {
+    const bs_params& p = c->prm;
+    const Scene& sc = c->sc;
+    const size_t R = c->R, ns = sc.ns, nk = sc.nk, C = c->crop, res = c->res;
+    const size_t cT = fp64 ? sizeof(cpx<double>) : sizeof(cpx<float>), rT = fp64 ? sizeof(double) : sizeof(float);
+    auto B = [](size_t n) { return std::max<size_t>(n, 256); };
+    size_t b = 0;
+    b += B(2 * R * R * cT);                                   // U, Uf
+    b += B(std::max<size_t>(1, ns) * sizeof(Sphere));
+    b += B((p.plane_wave ? 1 : nk) * 3 * sizeof(double));     // directions
+    if (p.lut_uf && !p.plane_wave && p.scalar) b += 2 * B((size_t)sc.uf_dR * (sc.m + 1) * sizeof(double));
+    if (p.scalar && ns > 0) {
+        size_t ncoef = 0;
+        for (const Sphere& S : c->hs) ncoef += S.Nl + 1;
+        b += 2 * B(ncoef * sizeof(zd)) + B(ns * 6 * (size_t)c->Lmax * sizeof(zd));
+        b += B(ns * nk * cT) + B(nk * sizeof(float4));        // phases, float directions
+    }
+    if (p.scalar && p.lut_us && ns > 0) {
+        std::vector<Sphere> hs = c->hs;
+        std::vector<int> cs;
+        size_t pool = 0, maxrows = 0, maxL = 0;
+        if (plan_tables(hs, !fp64, lut_budget ? lut_budget : SIZE_MAX / 4, cs, pool, maxrows, maxL) != BS_OK)
+            return 0;
+        const size_t thetaR = hs[0].thetaR;
+        b += B(pool) + B(maxrows * maxL * sizeof(zd)) + B(maxrows * 2 * maxL * sizeof(double));
+        b += B(thetaR * (size_t)c->Lmax * sizeof(double));    // Legendre table
+        if (!fp64) {
+            // slot k holds the k-th sphere of every chunk: the largest of those tables, plus a spare row each
+            size_t max_chunk = 0;
+            for (size_t ci = 0; ci + 1 < cs.size(); ci++) max_chunk = std::max(max_chunk, (size_t)(cs[ci + 1] - cs[ci]));
+            for (size_t k = 0; k < max_chunk; k++) {
+                size_t hd = 0, ha = 0;
+                for (size_t ci = 0; ci + 1 < cs.size(); ci++) {
+                    const size_t i = cs[ci] + k;
+                    if (i < (size_t)cs[ci + 1]) {
+                        hd = std::max(hd, (size_t)hs[i].dR + 1);
+                        ha = std::max(ha, (size_t)hs[i].aR + 1);
+                    }
+                }
+                b += 2 * thetaR * (hd + ha) * sizeof(float);
+            }
+            b += B(4 * max_chunk * sizeof(unsigned long long)) + B((nk + WAVE_CHUNK - 1) / WAVE_CHUNK * sizeof(float4)) +
+                 B(2 * sizeof(unsigned long long));
+        }
+    }
+    std::vector<int> su, sv;
+    double du, dv;
+    passbands(c, su, sv, du, dv);
+    const size_t Nu = su.size(), Nv = sv.size();
+    b += B(2 * res * res * rT);                               // D, Di
+    if (Nu && Nv) {
+        b += B(Nu * sizeof(int)) + B(Nv * sizeof(int)) + B(Nv * Nu * sizeof(float));
+        b += B(R * Nu * cT) + B(Nv * R * cT) + B(Nu * C * cT) + B(C * Nv * cT);
+        b += B(2 * R * Nu * cT) + B(2 * Nv * Nu * cT) + B(2 * Nv * C * cT) + B(2 * C * C * rT);
+    }
+    b += B(res * res * rT);                                   // image staging
+    return b;
+}
+
 extern "C" {
+
+bs_status bs_set_lut_reuse(bs_ctx* c, int32_t enable) {
+    if (!c) return fail(BS_ERR_ARG, "bs_set_lut_reuse: null context");
+    c->reuse = enable != 0;
+    if (!c->reuse) c->lut_valid = false;
+    return BS_OK;
+}
+
+bs_status bs_release_buffers(bs_ctx* c) {
+    if (!c) return fail(BS_ERR_ARG, "bs_release_buffers: null context");
+    CK(cudaStreamSynchronize(c->st));
+    release_all(c);
+    return BS_OK;
+}
+
+bs_status bs_estimate_bytes(const bs_params* params, const bs_sphere* spheres, int32_t ns, int32_t nk,
+                            bs_precision prec, uint64_t lut_budget, uint64_t* bytes) {
+    if (!params || !bytes || ns < 0 || nk < 0 || (ns > 0 && !spheres))
+        return fail(BS_ERR_ARG, "bs_estimate_bytes: bad arguments");
+    if (prec != BS_PREC_FP64 && prec != BS_PREC_MIXED) return fail(BS_ERR_ARG, "bs_estimate_bytes: unknown precision");
+    std::string why;
+    if (!valid_params(params, why)) return fail(BS_ERR_ARG, "bs_estimate_bytes: %s", why.c_str());
+    std::unique_ptr<bs_ctx> c(new bs_ctx());  // host state only: no stream, no device memory
+    c->prm = *params;
+    c->spheres.assign(spheres, spheres + ns);
+    c->waves.assign(3 * (size_t)std::max(nk, 1), 0.0);
+    c->waves_set = true;
+    bs_status st = derive(c.get());
+    if (st != BS_OK) return st;
+    size_t b = estimate_bytes(c.get(), prec == BS_PREC_FP64, (size_t)lut_budget);
+    if (!b) return fail(BS_ERR_NOMEM, "bs_estimate_bytes: a sphere's tables exceed the LUT budget of %llu bytes",
+                        (unsigned long long)lut_budget);
+    *bytes = b;
+    return BS_OK;
+}
 
 bs_status bs_simulate(bs_ctx* c, bs_precision prec) {
     if (!c) return fail(BS_ERR_ARG, "bs_simulate: null context");
@@ -733,6 +900,7 @@ bs_status bs_simulate(bs_ctx* c, bs_precision prec) {
     bs_status st = derive(c);
     if (st != BS_OK) return st;
     c->prec = prec;
+    c->stats.lut_tables_built = 0;
     int64_t l0 = c->launches;
     st = (prec == BS_PREC_FP64) ? run_nearfield<double>(c) : run_nearfield<float>(c);
     if (st != BS_OK) return st;
@@ -853,12 +1021,8 @@ bs_status bs_get_info(bs_ctx* c, bs_info* out) {
     out->n_waves = p.plane_wave ? 1 : (int)(c->waves.size() / 3);
     out->uf_lut_r = p.uf_lut_r > 0 ? p.uf_lut_r : 2 * R;
     out->us_lut_theta = p.us_lut_theta > 0 ? p.us_lut_theta : 1000;
-    const DevBuf* bufs[] = {&c->d_sph, &c->d_waves, &c->d_kw4, &c->d_ph, &c->d_A, &c->d_B, &c->d_mie, &c->d_tab,
-                            &c->d_tabscr, &c->d_legP, &c->d_lut, &c->d_uft, &c->d_uftscr, &c->d_fields, &c->d_su,
-                            &c->d_sv, &c->d_mask, &c->d_wx, &c->d_wy, &c->d_wix, &c->d_wiy, &c->d_f1, &c->d_f2,
-                            &c->d_g1, &c->d_I, &c->d_D, &c->d_img, &c->d_cones, &c->d_cnt};
     int64_t tot = 0;
-    for (const DevBuf* b : bufs) tot += (int64_t)b->n;
+    for (const DevBuf* b : ctx_bufs(c)) tot += (int64_t)b->n;
     for (const auto& sl : c->slots)
         for (int k = 0; k < 4; k++) tot += (int64_t)sl.w * sl.h[k] * (int64_t)sizeof(float);
     out->device_bytes = tot;

@@ -119,6 +119,8 @@ typedef struct bs_stats {
      * table window was staged in shared memory, and all such units. */
     int64_t lut_chunks_staged;
     int64_t lut_chunks_total;
+    int64_t lut_tables_built;  /* sphere tables (Usp + Uip) built; 0 when reused */
+    int64_t reserved;
 } bs_stats;
 
 typedef struct bs_ctx bs_ctx;
@@ -136,6 +138,11 @@ bs_status bs_create(const bs_params* params, bs_ctx** out);
 
 /* Free everything the context holds (microscopeStruct::destroy). */
 bs_status bs_destroy(bs_ctx* ctx);
+
+/* Replace the parameters of an existing context (a new LoadParameters pass,
+ * arguments.h:564-593, without reallocating); results of the last run are
+ * dropped. */
+bs_status bs_set_params(bs_ctx* ctx, const bs_params* params);
 
 /* Sphere list (lSpheres arguments.h:193-320, with the material resolved). */
 bs_status bs_set_spheres(bs_ctx* ctx, const bs_sphere* spheres, int32_t n);
@@ -193,6 +200,86 @@ bs_status bs_get_lut(bs_ctx* ctx, int32_t sphere, int32_t which, double* host, s
  * CUDA events.  The denominator of the scattered-field kernels' roofline.
  * No reference counterpart. */
 bs_status bs_measure_fma_peak(double* fp32_tflops, double* fp64_tflops);
+
+/* Keep the lookup tables of the last run and skip rebuilding them when the
+ * next bs_simulate on this context has the same tables: same spheres (centre,
+ * radius, index), wavelength, plane, table sizes and precision, and all
+ * tables fitting the LUT budget at once.  Off by default (every simulate then
+ * does the whole path, as the reference does); the serving front end turns it
+ * on for its contexts.  No reference counterpart. */
+bs_status bs_set_lut_reuse(bs_ctx* ctx, int32_t enable);
+
+/* Return every device buffer of the context to the CUDA allocator (results of
+ * the last run are dropped).  No reference counterpart. */
+bs_status bs_release_buffers(bs_ctx* ctx);
+
+/* Device bytes a context would hold after bs_simulate of this scene: near
+ * fields, detector transform, tables (capped by lut_budget when it is > 0, as
+ * bs_set_lut_budget does) and the per-sphere and per-wave arrays.  Host-only;
+ * the serving front end admits requests with it.  No reference counterpart. */
+bs_status bs_estimate_bytes(const bs_params* params, const bs_sphere* spheres, int32_t n_spheres, int32_t n_waves,
+                            bs_precision prec, uint64_t lut_budget, uint64_t* bytes);
+
+/* ------------------------------------------------------------------------
+ * Serving front end.  The reference runs one simulation per process; this
+ * queue runs many slices on one GPU: requests wait in arrival order, a pool
+ * of contexts (one CUDA stream each) runs as many as fit the device-memory
+ * budget at once (smaller requests may pass a head request that does not fit
+ * yet, each at most 8 times), a context keeps its tables for the next
+ * request with the same scene (requests are steered to it), and every result
+ * is what bs_simulate on a fresh context gives for the same inputs.
+ * ------------------------------------------------------------------------ */
+typedef struct bs_server bs_server;
+
+typedef struct bs_server_config {
+    int32_t workers;          /* requests in flight at once; 0 = 4                        */
+    int32_t dry_run;          /* 1: schedule without a GPU (capacity planning, tests):     */
+                              /*    a request "runs" for 1 ms and returns an image of      */
+                              /*    its ticket number                                      */
+    uint64_t hbm_budget;      /* device bytes for all contexts; 0 = 80 % of free memory    */
+} bs_server_config;
+
+typedef struct bs_request {
+    bs_params params;
+    const bs_sphere* spheres; /* copied at submit */
+    int32_t n_spheres;
+    int32_t n_waves;          /* directions in `waves`, or the count for the compat sampler */
+    const double* waves;      /* n_waves x 3 unit vectors, copied; NULL = bs_sample_waves_compat */
+    int32_t precision;        /* bs_precision                                             */
+    int32_t image;            /* bs_image_kind returned by bs_fetch                        */
+} bs_request;
+
+typedef struct bs_result_info {
+    double ms_queued;         /* submit -> start */
+    double ms_total;          /* submit -> done  */
+    double ms_gpu;            /* device time of the slice (bs_stats.ms_total)             */
+    int32_t status;           /* bs_status of the run                                      */
+    int32_t lut_reused;       /* 1 if the tables came from the previous request            */
+    int32_t worker;
+    int32_t reserved;
+} bs_result_info;
+
+typedef struct bs_server_stats {
+    int64_t submitted, completed, failed, queued, running;
+    int64_t lut_reuses;
+    double p50_ms, p99_ms, mean_ms, max_ms;  /* submit -> done, completed requests */
+    uint64_t bytes_in_use, bytes_peak, hbm_budget;
+} bs_server_stats;
+
+bs_status bs_server_create(const bs_server_config* cfg, bs_server** out);
+/* Stops accepting work, finishes what is running, drops what waits. */
+bs_status bs_server_destroy(bs_server* srv);
+/* BS_ERR_NOMEM when the request alone does not fit the budget. */
+bs_status bs_submit(bs_server* srv, const bs_request* req, uint64_t* ticket);
+/* *done = 1 once the request finished (successfully or not). */
+bs_status bs_poll(bs_server* srv, uint64_t ticket, int32_t* done);
+/* Blocks up to timeout_s seconds (< 0: no limit); BS_ERR_TIMEOUT if unfinished. */
+bs_status bs_wait(bs_server* srv, uint64_t ticket, double timeout_s);
+/* Copies the image (res x res float32) and releases the ticket.  Returns the
+ * run's own status if it failed (message in bs_last_error()), BS_ERR_NOTREADY
+ * if it has not finished. */
+bs_status bs_fetch(bs_server* srv, uint64_t ticket, float* host, size_t count, bs_result_info* info);
+bs_status bs_server_get_stats(bs_server* srv, bs_server_stats* out);
 
 /* Mie coefficients without any device allocation, for callers that cannot
  * call cudaMalloc (code inside CUDA stream capture, serving loops that reserve

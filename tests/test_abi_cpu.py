@@ -47,8 +47,10 @@ def test_struct_layout_matches_c():
 #include <stddef.h>
 #include "bimsim_gb300.h"
 int main(void) {
-  printf("%zu %zu %zu %zu %zu %zu\n", sizeof(bs_params), sizeof(bs_sphere), sizeof(bs_info), sizeof(bs_stats),
-         offsetof(bs_params, resolution), offsetof(bs_params, reserved));
+  printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu\n", sizeof(bs_params), sizeof(bs_sphere), sizeof(bs_info),
+         sizeof(bs_stats), offsetof(bs_params, resolution), offsetof(bs_params, reserved),
+         sizeof(bs_server_config), sizeof(bs_request), offsetof(bs_request, waves), sizeof(bs_result_info),
+         sizeof(bs_server_stats));
   return 0;
 }'''
     with tempfile.TemporaryDirectory() as td:
@@ -58,7 +60,9 @@ int main(void) {
         subprocess.check_call(["gcc", "-I", os.path.join(REPO, "include"), c, "-o", exe])
         vals = list(map(int, subprocess.check_output([exe]).split()))
     assert vals == [C.sizeof(abi.Params), C.sizeof(abi.Sphere), C.sizeof(abi.Info), C.sizeof(abi.Stats),
-                    abi.Params.resolution.offset, abi.Params.reserved.offset]
+                    abi.Params.resolution.offset, abi.Params.reserved.offset, C.sizeof(abi.ServerConfig),
+                    C.sizeof(abi.Request), abi.Request.waves.offset, C.sizeof(abi.ResultInfo),
+                    C.sizeof(abi.ServerStats)]
 
 
 def test_version_and_error_strings(so):
