@@ -326,6 +326,73 @@ def run_gb300(args):
     print(json.dumps(line))
 
 
+def run_workload(args):
+    """Secondary workloads, one JSON line each (not the headline line):
+      sweep    config 3: 512^2 config-2 scene, 50 spheres (3 Lorentzian materials), 1000 waves,
+               --sweep-bands wavelengths evenly spaced in 2.5-12.5 um through bs_sweep
+      config1  the plain method: 256^2 over 20 um, padding 2, one sphere a = 5 um, 400 waves,
+               direct order sums, FP64
+    Steps: --warmup untimed and --steps timed runs of the whole workload, L2 flushed between."""
+    import numpy as np
+    import torch
+
+    from bimsim_gb300 import BS_IMG_INTENSITY, BS_PREC_FP64, BS_PREC_MIXED, Context, scenes
+    torch.cuda.set_device(0)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    if args.workload == "sweep":
+        p, s, w, lambdas, table = scenes.config3(n_lambda=512)
+        idx = np.linspace(0, 511, args.sweep_bands).round().astype(int)
+        lambdas, table = lambdas[idx], table[idx]
+        prec = BS_PREC_MIXED
+        work = f"config3: 512^2 detector over 100 um (near field 1536^2), 50 spheres, 1000 waves, " \
+               f"{len(lambdas)} of the 512 wavelengths in 2.5-12.5 um, LUT 4096x1024"
+    else:
+        p, s, w = scenes.config1()
+        lambdas = table = None
+        prec = BS_PREC_FP64
+        work = "config1: 256^2 over 20 um, padding 2 (near field 1280^2), one sphere a=5 um n=1.4+0.05i, " \
+               "lambda 2.5 um, 400 waves, direct order sums (--recursive)"
+    ctx = Context(p)
+    ctx.set_spheres(s)
+    ctx.set_waves(w)
+    R = ctx.info().nf_res
+
+    def step():
+        if lambdas is not None:
+            ctx.sweep(lambdas, table, precision=prec, images=True)
+        else:
+            ctx.simulate(prec)
+            ctx.image(BS_IMG_INTENSITY)
+
+    for _ in range(args.warmup):
+        step()
+    sampler = ClockSampler(0)
+    sampler.start()
+    times = []
+    for _ in range(args.steps):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        step()
+        torch.cuda.synchronize()
+        times.append(time.perf_counter() - t0)
+    clocks = sampler.stop()
+    st = ctx.stats()
+    per = statistics.median(times)
+    nb = len(lambdas) if lambdas is not None else 1
+    line = {"metric": "sweep bands/s" if lambdas is not None else "field-slice pixels/s (plain FP64 direct)",
+            "value": nb / per if lambdas is not None else R * R / per,
+            "unit": "bands/s" if lambdas is not None else "pixels/s",
+            "field_slice_pixels_per_s": nb * R * R / per, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": per * 1e3, "higher_is_better": True,
+            "dtype": "f32 (FP64 tables and geometry)" if prec == BS_PREC_MIXED else "f64",
+            "data": "synthetic (seeded)", "config": {"workload": work, "l2": "flushed between steps"},
+            "last_band_stats": {"ms_us": st.ms_us, "ms_lut": st.ms_lut, "ms_uf": st.ms_uf, "ms_detector": st.ms_detector,
+                                "ms_total": st.ms_total, "interactions": st.us_interactions},
+            "clocks": clocks}
+    print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -338,9 +405,13 @@ def main():
     ap.add_argument("--serve-requests", type=int, default=32)
     ap.add_argument("--serve-rate", type=float, default=1.0)
     ap.add_argument("--serve-workers", type=int, default=4)
+    ap.add_argument("--workload", default="slice", choices=["slice", "sweep", "config1"])
+    ap.add_argument("--sweep-bands", type=int, default=64)
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload != "slice":
+        run_workload(args)
     else:
         run_gb300(args)
 

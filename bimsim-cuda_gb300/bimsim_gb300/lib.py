@@ -52,6 +52,7 @@ def library():
         "bs_measure_fma_peak": ([vp, vp], C.c_int),
         "bs_mie_noalloc": ([vp, i32, i32, C.c_double, vp, vp, vp], C.c_int),
         "bs_set_params": ([vp, vp], C.c_int),
+        "bs_sweep": ([vp, vp, i32, vp, C.c_int, C.c_int, vp, C.c_char_p, i32], C.c_int),
         "bs_set_lut_reuse": ([vp, i32], C.c_int),
         "bs_release_buffers": ([vp], C.c_int),
         "bs_estimate_bytes": ([vp, vp, i32, i32, C.c_int, C.c_uint64, C.POINTER(C.c_uint64)], C.c_int),
@@ -172,6 +173,18 @@ class Context:
 
     def write_envi(self, kind, path, append, band_value):
         self._check(self.lib.bs_write_envi(self.h, kind, path.encode(), 1 if append else 0, band_value))
+
+    def sweep(self, lambdas, n_table, precision=abi.BS_PREC_MIXED, kind=abi.BS_IMG_INTENSITY, envi_path=None,
+              band_as_nu=False, images=True):
+        """Images (nl, res, res) float32 of a spectral sweep; n_table: (nl, ns) complex indices."""
+        lam = np.ascontiguousarray(lambdas, dtype=np.float64)
+        nt = np.ascontiguousarray(np.asarray(n_table, dtype=np.complex128)).view(np.float64)
+        res = self.params.resolution
+        out = np.zeros((len(lam), res, res), dtype=np.float32) if images else None
+        self._check(self.lib.bs_sweep(self.h, _p(lam), len(lam), _p(nt) if nt.size else None, precision, kind,
+                                      _p(out) if out is not None else None,
+                                      envi_path.encode() if envi_path else None, 1 if band_as_nu else 0))
+        return out
 
     def set_params(self, params):
         self._check(self.lib.bs_set_params(self.h, C.byref(params)))

@@ -120,3 +120,56 @@ def served_trace(n, seed=4, resolutions=(128, 256, 512, 1024, 2048), rate_hz=1.0
         s = random_spheres(ns, 100.0, 1.0, 5.0, seed=seed * 1009 + i, z_slab=0.0 if ns <= 60 else 30.0)
         out.append((t, p, s, mc_waves(nk, 0.0, 0.5, seed=seed * 7919 + i)))
     return out
+
+
+def lorentz_kappa(nu, centres_um, widths_um, peaks):
+    """Absorption index: Lorentzian bands in wavenumber nu (1/um), each centred
+    at 1/centre with half width (width/2)/centre^2 (so FWHM ~ width in
+    wavelength) and the given peak."""
+    nu = np.asarray(nu, dtype=np.float64)
+    k = np.zeros_like(nu)
+    for c, w, pk in zip(centres_um, widths_um, peaks):
+        nc, g = 1.0 / c, 0.5 * w / (c * c)
+        k += pk * g * g / ((nu - nc) ** 2 + g * g)
+    return k
+
+
+def hilbert_dn(nu_grid, kappa):
+    """Kramers-Kronig refractive-index change of an absorption band on a
+    uniform wavenumber grid: dn = -H[kappa], H the discrete Hilbert transform
+    (FFT, response -i sign(f), zero-padded 4x against wrap-around).  For a
+    Lorentzian kappa = p g^2 / ((nu - nc)^2 + g^2) this is
+    -p g (nu - nc) / ((nu - nc)^2 + g^2): normal dispersion below the band."""
+    n = len(kappa)
+    m = 4 * n
+    f = np.fft.fft(np.concatenate([kappa, np.zeros(m - n)]))
+    freq = np.fft.fftfreq(m)
+    h = np.real(np.fft.ifft(-1j * np.sign(freq) * f))[:n]
+    return -h
+
+
+def lorentz_material(lambdas, seed=3, n0=1.45, bands=3):
+    """n(lambda) = n0 + dn(lambda) + i kappa(lambda) with `bands` seeded
+    Lorentzian absorption bands (centres in 2.5-12.5 um, widths 0.05-0.2 um,
+    peaks <= 0.1) and dn from the discrete Hilbert transform of kappa."""
+    g = rng(seed)
+    centres = g.uniform(2.5, 12.5, bands)
+    widths = g.uniform(0.05, 0.2, bands)
+    peaks = g.uniform(0.02, 0.1, bands)
+    nu_grid = np.linspace(1.0 / 40.0, 1.0 / 1.0, 1 << 16)
+    kap = lorentz_kappa(nu_grid, centres, widths, peaks)
+    dn = hilbert_dn(nu_grid, kap)
+    nu = 1.0 / np.asarray(lambdas, dtype=np.float64)
+    return n0 + np.interp(nu, nu_grid, dn) + 1j * lorentz_kappa(nu, centres, widths, peaks)
+
+
+def config3(n_lambda=512, resolution=512, n_spheres=50, samples=1000, n_materials=3):
+    """Spectral sweep: the config-2 scene family at `resolution` over 512
+    wavelengths evenly spaced in 2.5-12.5 um; sphere i is made of material
+    i % n_materials, each a lorentz_material with its own seed.  Returns
+    (params, spheres, waves, lambdas, n_table[n_lambda, n_spheres])."""
+    p, spheres, waves = config2(resolution=resolution, n_spheres=n_spheres, samples=samples, seed=3)
+    lambdas = np.linspace(2.5, 12.5, n_lambda)
+    mats = [lorentz_material(lambdas, seed=30 + j) for j in range(n_materials)]
+    table = np.stack([mats[i % n_materials] for i in range(len(spheres))], axis=1)
+    return p, spheres, waves, lambdas, table

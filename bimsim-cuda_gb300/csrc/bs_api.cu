@@ -1011,6 +1011,34 @@ bs_status bs_write_envi(bs_ctx* c, bs_image_kind kind, const char* path, int32_t
     return BS_OK;
 }
 
+bs_status bs_sweep(bs_ctx* c, const double* lambdas, int32_t nl, const double* n_table, bs_precision prec,
+                   bs_image_kind kind, float* images, const char* envi_path, int32_t band_as_nu) {
+    if (!c || !lambdas || nl < 1) return fail(BS_ERR_ARG, "bs_sweep: need at least one wavelength");
+    const size_t ns = c->spheres.size();
+    if (ns > 0 && !n_table) return fail(BS_ERR_ARG, "bs_sweep: need the refractive-index table");
+    for (int32_t l = 0; l < nl; l++)
+        if (!(lambdas[l] > 0)) return fail(BS_ERR_ARG, "bs_sweep: wavelength %d is not positive", l + 1);
+    const bs_params saved_p = c->prm;
+    const std::vector<bs_sphere> saved_s = c->spheres;
+    const size_t npix = (size_t)c->prm.resolution * c->prm.resolution;
+    bs_status st = BS_OK;
+    for (int32_t l = 0; l < nl && st == BS_OK; l++) {
+        c->prm.lambda = lambdas[l];
+        for (size_t i = 0; i < ns; i++) {
+            c->spheres[i].n_re = n_table[2 * ((size_t)l * ns + i)];
+            c->spheres[i].n_im = n_table[2 * ((size_t)l * ns + i) + 1];
+        }
+        st = bs_simulate(c, prec);
+        if (st == BS_OK && images) st = bs_get_image(c, kind, images + (size_t)l * npix, npix);
+        if (st == BS_OK && envi_path)
+            st = bs_write_envi(c, kind, envi_path, l > 0, band_as_nu ? 1e4 / lambdas[l] : lambdas[l]);
+    }
+    c->prm = saved_p;
+    c->spheres = saved_s;
+    c->have = false;
+    return st;
+}
+
 bs_status bs_get_info(bs_ctx* c, bs_info* out) {
     if (!c || !out) return fail(BS_ERR_ARG, "bs_get_info: null argument");
     const bs_params& p = c->prm;

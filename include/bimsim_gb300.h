@@ -201,6 +201,18 @@ bs_status bs_get_lut(bs_ctx* ctx, int32_t sphere, int32_t which, double* host, s
  * No reference counterpart. */
 bs_status bs_measure_fma_peak(double* fp32_tflops, double* fp64_tflops);
 
+/* Spectral sweep: the reference's per-wavelength runs (one `bimsim --lambda
+ * ... --append` process per band, runBimSim.py:80-86 and specimage.py) in one
+ * call.  For wavelength l of nl, every sphere s takes the index
+ * n_table[2*(l*ns + s)] + i n_table[2*(l*ns + s) + 1]; the slice is computed
+ * as bs_simulate would and image `kind` goes to images + l*res*res (float32,
+ * may be NULL) and, when envi_path is given, to band l of that ENVI file
+ * (band value lambda, or 1e4/lambda when band_as_nu).  The context's own
+ * wavelength and indices are restored afterwards; results of the last
+ * band are dropped. */
+bs_status bs_sweep(bs_ctx* ctx, const double* lambdas, int32_t nl, const double* n_table, bs_precision prec,
+                   bs_image_kind kind, float* images, const char* envi_path, int32_t band_as_nu);
+
 /* Keep the lookup tables of the last run and skip rebuilding them when the
  * next bs_simulate on this context has the same tables: same spheres (centre,
  * radius, index), wavelength, plane, table sizes and precision, and all
