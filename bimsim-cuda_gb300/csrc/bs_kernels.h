@@ -13,6 +13,13 @@ namespace bs {
 // sort); the host supplies one bounding cone per chunk.
 constexpr int WAVE_CHUNK = 64;
 
+// Mixed LUT kernel staging: float2 table values a 16 x 16 pixel tile stages
+// per wave chunk (43 KB of shared memory, 4 blocks per SM), and the angle
+// margin (radians) added to its window bounds.
+constexpr int LUT_TILE = 16;
+constexpr int LUT_STAGE_ENTRIES = 5400;
+constexpr float LUT_STAGE_MARGIN = 2e-3f;
+
 template <class T>
 struct cpx;
 using zd = cpx<double>;
@@ -44,11 +51,12 @@ void launch_us_lut_f64(const Scene& sc, const Sphere* sph, int s0, int s1, int a
 // lin: linear float2 tables (Sphere::usp_off / uip_off in float2 units, rows
 // of Sphere::lin_stride entries);
 // cones: one {axis, half-angle} per WAVE_CHUNK waves; counters[0..1] receive
-// the staged and total (sphere, chunk) counts of every block (may be null)
+// the staged and total (sphere, chunk) counts of every block (may be null);
+// stage = false runs the texture-only variant
 void launch_us_lut_tex(const Scene& sc, const Sphere* sph, int s0, int s1, int accumulate, int finalize,
                        const float4* kw4, const float4* cones, const cpx<float>* ph, const unsigned long long* tex,
                        const float2* lin, const cpx<float>* Uf, cpx<float>* U, unsigned long long* counters,
-                       cudaStream_t st);
+                       bool stage, cudaStream_t st);
 void launch_lut_build_tex(const zd* tab, int rows, int L, const double* P, int Pstride, int thetaR,
                           cudaSurfaceObject_t sre, cudaSurfaceObject_t sim, float2* lin, int lin_stride,
                           cudaStream_t st);

@@ -436,8 +436,8 @@ __device__ __forceinline__ void copy_async8(float2* dst, const float2* src) {
 
 __device__ __forceinline__ void copy_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 constexpr int UST_CHUNK = WAVE_CHUNK;
-constexpr int UST_STAGE = 5400;     // float2 table values staged per chunk (43 KB; 4 blocks per SM)
-constexpr float UST_MARGIN = 2e-3f;  // radians added to the angular bounds
+constexpr int UST_STAGE = LUT_STAGE_ENTRIES;
+constexpr float UST_MARGIN = LUT_STAGE_MARGIN;
 
 // Block-uniform values of one (tile, sphere) pair, kept in shared memory so
 // that they are re-read per chunk instead of holding registers through the
@@ -451,7 +451,10 @@ struct TileSphere {
     long long off;     // first entry of the table in the linear pool
 };
 
-__global__ void __launch_bounds__(UST_BLOCK, 4) us_lut_tex_kernel(Scene sc, const Sphere* __restrict__ sph, int s0, int s1,
+// STAGE = false: texture path only, no dynamic shared memory (the L1 keeps
+// its full size for the texture cache) and 6 blocks per SM.
+template <bool STAGE>
+__global__ void __launch_bounds__(UST_BLOCK, STAGE ? 4 : 6) us_lut_tex_kernel(Scene sc, const Sphere* __restrict__ sph, int s0, int s1,
                                                                     int accumulate, int finalize,
                                                                     const float4* __restrict__ kw4,
                                                                     const float4* __restrict__ cones,
@@ -500,8 +503,16 @@ __global__ void __launch_bounds__(UST_BLOCK, 4) us_lut_tex_kernel(Scene sc, cons
             cb = 0.f;
         }
         // ---- tile bounds: table rows and angular radius gamma ----
-        int rlo, rhi, ok;
-        {
+        int rlo = 0, rhi = 0, ok = 0;
+        if (!STAGE) {
+            __syncthreads();  // s_ts is reused for every sphere
+            if (threadIdx.x == 0) {
+                s_ts.tsc = (float)((S.thetaR - 1) / PI_REF);
+                s_ts.tscpi = (float)((S.thetaR - 1) / PI_REF * TRUE_PI);
+                s_ts.tmax = (float)(S.thetaR - 1);
+                s_ts.nrows = 0;
+            }
+        } else {
             // tile centre in single precision (bounds only, covered by the margins)
             const float u = ((float)tu + 7.5f) / (float)sc.R, v = ((float)tv + 7.5f) / (float)sc.R;
             float cx = (float)sc.A[0] + (float)sc.X[0] * u + (float)sc.Y[0] * v - (float)S.p[0];
@@ -566,7 +577,7 @@ __global__ void __launch_bounds__(UST_BLOCK, 4) us_lut_tex_kernel(Scene sc, cons
             const int nrows = s_ts.nrows;
             int t_lo = 0, W = 1;
             bool staged = false;
-            if (nrows > 0) {
+            if (STAGE && nrows > 0) {
                 const float4 cone = cones[ch];
                 const float tsc = s_ts.tsc, gam = s_ts.gam;
                 const float thc = acosf(fminf(fmaxf(cone.x * s_ts.cx + cone.y * s_ts.cy + cone.z * s_ts.cz, -1.f), 1.f));
@@ -581,7 +592,7 @@ __global__ void __launch_bounds__(UST_BLOCK, 4) us_lut_tex_kernel(Scene sc, cons
                 s_k[threadIdx.x] = kw4[w0 + threadIdx.x];
                 s_p[threadIdx.x] = make_float2(pv.re, pv.im);
             }
-            if (staged) {
+            if (STAGE && staged) {
                 // asynchronous copies, one table row per warp at a time, all in flight together
                 const float2* table = lin + s_ts.off + (size_t)s_ts.rlo * s_ts.lin_stride + t_lo;
                 const int ls = s_ts.lin_stride;
@@ -595,7 +606,7 @@ __global__ void __launch_bounds__(UST_BLOCK, 4) us_lut_tex_kernel(Scene sc, cons
             __syncthreads();
             const float tsc = s_ts.tsc, tscpi = s_ts.tscpi, tmax = s_ts.tmax;
             float ar = 0.f, ai = 0.f;
-            if (staged) {
+            if (STAGE && staged) {
                 staged_chunks++;
                 const float2* row0 = s_stage + lr0 * W;
                 const int drow = (lr1 - lr0) * W;
@@ -887,13 +898,20 @@ void launch_us_lut_f64(const Scene& sc, const Sphere* sph, int s0, int s1, int a
 void launch_us_lut_tex(const Scene& sc, const Sphere* sph, int s0, int s1, int accumulate, int finalize,
                        const float4* kw4, const float4* cones, const cpx<float>* ph, const unsigned long long* tex,
                        const float2* lin, const cpx<float>* Uf, cpx<float>* U, unsigned long long* counters,
-                       cudaStream_t st) {
+                       bool stage, cudaStream_t st) {
     int tiles = (sc.R + 15) / 16;
+    if (!stage) {
+        us_lut_tex_kernel<false><<<(unsigned)tiles * tiles, UST_BLOCK, 0, st>>>(sc, sph, s0, s1, accumulate, finalize,
+                                                                                 kw4, cones, ph, tex, lin, Uf, U,
+                                                                                 counters);
+        return;
+    }
     const int smem = UST_STAGE * (int)sizeof(float2);
     // per device and cheap; a failure shows up as the launch error
-    cudaFuncSetAttribute(us_lut_tex_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    us_lut_tex_kernel<<<(unsigned)tiles * tiles, UST_BLOCK, smem, st>>>(sc, sph, s0, s1, accumulate, finalize, kw4,
-                                                                         cones, ph, tex, lin, Uf, U, counters);
+    cudaFuncSetAttribute(us_lut_tex_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    us_lut_tex_kernel<true><<<(unsigned)tiles * tiles, UST_BLOCK, smem, st>>>(sc, sph, s0, s1, accumulate, finalize,
+                                                                               kw4, cones, ph, tex, lin, Uf, U,
+                                                                               counters);
 }
 
 void launch_lut_build_tex(const zd* tab, int rows, int L, const double* P, int Pstride, int thetaR,

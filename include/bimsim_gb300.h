@@ -120,7 +120,7 @@ typedef struct bs_stats {
     int64_t lut_chunks_staged;
     int64_t lut_chunks_total;
     int64_t lut_tables_built;  /* sphere tables (Usp + Uip) built; 0 when reused */
-    int64_t reserved;
+    double lut_staged_predicted;  /* the kernel choice's model of lut_chunks_staged / total */
 } bs_stats;
 
 typedef struct bs_ctx bs_ctx;
@@ -212,6 +212,12 @@ bs_status bs_measure_fma_peak(double* fp32_tflops, double* fp64_tflops);
  * band are dropped. */
 bs_status bs_sweep(bs_ctx* ctx, const double* lambdas, int32_t nl, const double* n_table, bs_precision prec,
                    bs_image_kind kind, float* images, const char* envi_path, int32_t band_as_nu);
+
+/* Kernel of the mixed-precision LUT stage: 0 (default) chooses from a model
+ * of how many table windows fit in shared memory, 1 always stages windows in
+ * shared memory (texture gathers where a window does not fit), 2 uses texture
+ * gathers only.  All three give the same bits.  No reference counterpart. */
+bs_status bs_set_lut_staging(bs_ctx* ctx, int32_t mode);
 
 /* Keep the lookup tables of the last run and skip rebuilding them when the
  * next bs_simulate on this context has the same tables: same spheres (centre,

@@ -90,7 +90,7 @@ def oracle_result(name):
     return _oracle_cache[name]
 
 
-def run_gpu(name, prec, budget=0):
+def run_gpu(name, prec, budget=0, staging=0):
     p, s, waves = scene(name)
     ctx = Context(p)
     ctx.set_spheres(s)
@@ -98,6 +98,8 @@ def run_gpu(name, prec, budget=0):
         ctx.set_waves(waves)
     if budget:
         ctx.set_lut_budget(budget)
+    if staging:
+        ctx.set_lut_staging(staging)
     ctx.simulate(prec)
     out = dict(U=ctx.field(BS_FIELD_TOTAL), Uf=ctx.field(BS_FIELD_INCIDENT),
                D=ctx.image(BS_IMG_INTENSITY, f64=True), Di=ctx.image(BS_IMG_INCIDENT, f64=True),
@@ -129,7 +131,7 @@ def test_mixed_matches_oracle(name):
 def test_mixed_lut_kernel_uses_both_table_paths():
     """The staged (shared-memory) and texture paths of the mixed LUT kernel both run in the
     lut_staged scene; the parity tests above cover their values."""
-    g = run_gpu("lut_staged", BS_PREC_MIXED)
+    g = run_gpu("lut_staged", BS_PREC_MIXED, staging=1)
     st = g["stats"]
     tiles = (oracle_lib.geom(scene("lut_staged")[0]).R + 15) // 16
     # tiles of 16 x 16 near-field pixels x 2 spheres x 4 wave chunks of 64
@@ -137,6 +139,24 @@ def test_mixed_lut_kernel_uses_both_table_paths():
     assert 0 < st.lut_chunks_staged < st.lut_chunks_total, (st.lut_chunks_staged, st.lut_chunks_total)
     g64 = run_gpu("lut_staged", BS_PREC_FP64)
     assert g64["stats"].lut_chunks_total == 0
+
+
+@pytest.mark.parametrize("name", ["lut", "lut_ufLUT", "lut_staged", "oblique_xz", "supersample"])
+def test_staged_and_texture_kernels_give_identical_bits(name):
+    a = run_gpu(name, BS_PREC_MIXED, staging=1)
+    b = run_gpu(name, BS_PREC_MIXED, staging=2)
+    assert b["stats"].lut_chunks_staged == 0
+    assert np.array_equal(a["U"], b["U"]) and np.array_equal(a["D"], b["D"])
+
+
+def test_kernel_choice_model_tracks_the_staged_fraction():
+    """The host model that picks the staged kernel predicts the fraction the kernel then stages."""
+    g = run_gpu("lut_staged", BS_PREC_MIXED, staging=1)
+    st = g["stats"]
+    measured = st.lut_chunks_staged / st.lut_chunks_total
+    assert abs(st.lut_staged_predicted - measured) < 0.2, (st.lut_staged_predicted, measured)
+    auto = run_gpu("lut_staged", BS_PREC_MIXED)["stats"]
+    assert (auto.lut_chunks_staged > 0) == (auto.lut_staged_predicted >= 0.25)
 
 
 def test_images_are_derived_consistently():
