@@ -208,7 +208,11 @@ def run_gb300(args):
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
 
-    p, spheres, waves = scenes.config2()
+    if args.small:
+        # profiling case: the same pixel density and table sampling per micrometre at 256^2 (near field 768^2)
+        p, spheres, waves = scenes.config2(resolution=256, fov=25.0, n_spheres=10, samples=1000, lut_r=1024)
+    else:
+        p, spheres, waves = scenes.config2()
     ctx = Context(p)
     ctx.set_spheres(spheres)
     ctx.set_waves(waves)
@@ -288,10 +292,10 @@ def run_gb300(args):
         mix = c2.image(BS_IMG_INTENSITY, f64=True)
     rel = float(np.linalg.norm(mix - ref) / np.linalg.norm(ref))
     # ---- served latency (after the timed regions) ----
-    served = None if args.no_serve or ws > 1 else run_served(args)
+    served = None if args.no_serve or args.small or ws > 1 else run_served(args)
     # ---- CPU baseline (oracle on a bounded band of rows) ----
     cpu = None
-    if not args.no_cpu:
+    if not args.no_cpu and not args.small:
         rows = args.ref_rows
         dt, Rr = cpu_reference(p, spheres, waves, rows, os.cpu_count() or 1)
         cpu = {"value": Rr * Rr / (dt * Rr / rows), "unit": "pixels/s", "cores": os.cpu_count() or 1,
@@ -304,8 +308,10 @@ def run_gb300(args):
         "warmup": args.warmup, "ms_per_step": total / args.steps * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32 (FP64 tables and geometry)",
         "data": "synthetic (seeded Philox scene and waves)",
-        "config": {"workload": "config2: 1024^2 detector over 100 um, 50 spheres a~U(1,5) n~U(1.2,1.6)+iU(0,.05), "
-                               "lambda 3 um, 1000 MC waves, scalar LUT + Uf LUT, LUT 4096x1024, near field 3072^2",
+        "config": {"workload": ("PROFILING CASE (not the benchmark): 256^2 over 25 um, 10 spheres, LUT 1024x1024, "
+                                "near field 768^2" if args.small else
+                                "config2: 1024^2 detector over 100 um, 50 spheres a~U(1,5) n~U(1.2,1.6)+iU(0,.05), "
+                                "lambda 3 um, 1000 MC waves, scalar LUT + Uf LUT, LUT 4096x1024, near field 3072^2"),
                    "precision": "mixed", "l2": "flushed between timed steps (256 MB write); LUTs 1.6 GB > L2",
                    "parallelism": f"replicas x{ws}"},
         "e2e": {"value": e2e_value, "unit": "pixels/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
@@ -402,6 +408,8 @@ def main():
     ap.add_argument("--ref-rows", type=int, default=int(os.environ.get("BS_REF_ROWS", "12")))
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--small", action="store_true",
+                    help="profiling case: config-2 scene family at 256^2 over 25 um, 10 spheres, LUT 1024 x 1024")
     ap.add_argument("--serve-requests", type=int, default=32)
     ap.add_argument("--serve-rate", type=float, default=1.0)
     ap.add_argument("--serve-workers", type=int, default=4)
