@@ -53,6 +53,9 @@ def library():
         "bs_mie_noalloc": ([vp, i32, i32, C.c_double, vp, vp, vp], C.c_int),
         "bs_set_params": ([vp, vp], C.c_int),
         "bs_sweep": ([vp, vp, i32, vp, C.c_int, C.c_int, vp, C.c_char_p, i32], C.c_int),
+        "bs_simulate_sources": ([vp, vp, i32, C.c_int], C.c_int),
+        "bs_plane_point": ([vp, C.c_double, C.c_double, vp], C.c_int),
+        "bs_get_far_field": ([vp, C.c_int, vp, sz], C.c_int),
         "bs_set_lut_reuse": ([vp, i32], C.c_int),
         "bs_set_lut_staging": ([vp, i32], C.c_int),
         "bs_release_buffers": ([vp], C.c_int),
@@ -161,6 +164,13 @@ class Context:
         self._check(self.lib.bs_get_field(self.h, kind, _p(out), R * R))
         return out.view(np.complex128).reshape(R, R)
 
+    def far_field(self, kind=abi.BS_FIELD_TOTAL):
+        """Band-passed, cropped far field (res*ss)^2 complex of the last run."""
+        n = self.params.resolution * self.params.supersample
+        out = np.zeros(2 * n * n, dtype=np.float64)
+        self._check(self.lib.bs_get_far_field(self.h, kind, _p(out), n * n))
+        return out.view(np.complex128).reshape(n, n)
+
     def mie(self, sphere, nl):
         A = np.zeros(2 * (nl + 1))
         B = np.zeros(2 * (nl + 1))
@@ -187,6 +197,11 @@ class Context:
                                       envi_path.encode() if envi_path else None, 1 if band_as_nu else 0))
         return out
 
+    def simulate_sources(self, sources, precision=abi.BS_PREC_MIXED):
+        """sources: (n, 4) rows of focus x, y, z and amplitude; detector images sum over them."""
+        a = np.ascontiguousarray(sources, dtype=np.float64).reshape(-1, 4)
+        self._check(self.lib.bs_simulate_sources(self.h, _p(a), len(a), precision))
+
     def set_params(self, params):
         self._check(self.lib.bs_set_params(self.h, C.byref(params)))
         self.params = params
@@ -200,6 +215,16 @@ class Context:
 
     def release_buffers(self):
         self._check(self.lib.bs_release_buffers(self.h))
+
+
+def plane_point(params, u, v):
+    """Point A + u X + v Y of the detector plane (microscopeStruct::pos)."""
+    lib = library()
+    out = np.zeros(3)
+    st = lib.bs_plane_point(C.byref(params), u, v, _p(out))
+    if st != 0:
+        raise BimsimError(st, lib.bs_last_error().decode())
+    return out
 
 
 def estimate_bytes(params, spheres, n_waves, precision=abi.BS_PREC_MIXED, lut_budget=0):

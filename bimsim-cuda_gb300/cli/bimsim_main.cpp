@@ -22,6 +22,7 @@
 #include <vector>
 
 #include "bimsim_gb300.h"
+#include "image_io.h"
 
 namespace {
 
@@ -428,8 +429,28 @@ int main(int argc, char** argv) {
     if (args("uf-lut-res")) p.uf_lut_r = args.i("uf-lut-res", 0);
     std::string prec = args.text("precision");
     bs_precision precision = (prec == "fp64") ? BS_PREC_FP64 : BS_PREC_MIXED;
-    if (args("extended-source") || args.i("interpolate") != -1)
-        return fail("BIMSim Error: extended sources and point-source interpolation are not part of this build");
+    // extended source (LoadExtendedSource, microscope.cu:1257-1296): one point
+    // source per non-zero pixel at pos(x/width, y/height) of the detector plane,
+    // amplitude pixel/255; x outer, y inner
+    std::vector<double> sources;
+    if (args("extended-source")) {
+        int w = 0, h = 0;
+        std::vector<unsigned char> px;
+        std::string err;
+        if (!bsio::read_channel0(args.text("extended-source"), w, h, px, err)) return fail("BIMSim Error: " + err);
+        for (int x = 0; x < w; x++)
+            for (int y = 0; y < h; y++) {
+                unsigned char v = px[(size_t)y * w + x];
+                if (v == 0) continue;
+                float u = (float)x / (float)w, vv = (float)y / (float)h;
+                double f[3];
+                if (check(bs_plane_point(&p, u, vv, f))) return 1;
+                sources.insert(sources.end(), {f[0], f[1], f[2], (double)((float)v / 255)});
+            }
+        if (verbose) std::cout << "Number of point sources: " << sources.size() / 4 << std::endl;
+    } else if (args.i("interpolate") != -1) {
+        return fail("BIMSim Error: point-source interpolation (--interpolate 0-3) is not part of this build");
+    }
 
     // spheres with their refractive index at lambda (material n + i k, rts/optics/material.h:434-446)
     std::vector<bs_sphere> spheres;
@@ -440,6 +461,16 @@ int main(int argc, char** argv) {
     std::string intFile = args.text("intensity"), incFile = args.text("incident"), absFile = args.text("absorbance"),
                 absSpecFile = args.text("absorbance-spec"), transFile;
     if (args("transmittance")) transFile = args.text("transmittance");
+    std::string nearFile = args.text("near-field"), farFile = args.text("far-field");
+    std::string fieldStr = args.text("output-type");
+    bsio::Colormap cmap = bsio::CM_BREWER;
+    {
+        std::string cm = args.text("colormap");
+        if (cm == "gray")
+            cmap = bsio::CM_GRAY;
+        else if (cm != "brewer")
+            std::cout << "color-map value not recognized (using default): " << cm << std::endl;
+    }
 
     if (args("dry-run")) {
         std::printf("{\"lambda\": %.9g, \"amplitude\": %.9g, \"k\": [%.9g, %.9g, %.9g], \"focus\": [%.9g, %.9g, %.9g], "
@@ -447,13 +478,15 @@ int main(int argc, char** argv) {
                     "\"plane_max\": [%.9g, %.9g, %.9g], \"normal\": [%.9g, %.9g, %.9g], \"resolution\": %d, "
                     "\"padding\": %d, \"supersample\": %d, \"field_order\": %d, \"samples\": %d, \"scalar\": %d, "
                     "\"plane_wave\": %d, \"lut_uf\": %d, \"lut_us\": %d, \"us_lut\": [%d, %d], \"uf_lut\": %d, "
-                    "\"precision\": \"%s\", \"wavenumber\": %d, \"append\": %d, \"spheres\": [",
+                    "\"precision\": \"%s\", \"wavenumber\": %d, \"append\": %d, \"point_sources\": %zu, "
+                    "\"spheres\": [",
                     p.lambda, p.amplitude, p.k_dir[0], p.k_dir[1], p.k_dir[2], p.focus[0], p.focus[1], p.focus[2],
                     p.condenser[0], p.condenser[1], p.objective[0], p.objective[1], p.plane_min[0], p.plane_min[1],
                     p.plane_min[2], p.plane_max[0], p.plane_max[1], p.plane_max[2], p.plane_normal[0],
                     p.plane_normal[1], p.plane_normal[2], p.resolution, p.padding, p.supersample, p.field_order, nk,
                     p.scalar, p.plane_wave, p.lut_uf, p.lut_us, p.us_lut_r, p.us_lut_theta, p.uf_lut_r,
-                    precision == BS_PREC_FP64 ? "fp64" : "mixed", wavenumber ? 1 : 0, append ? 1 : 0);
+                    precision == BS_PREC_FP64 ? "fp64" : "mixed", wavenumber ? 1 : 0, append ? 1 : 0,
+                    sources.size() / 4);
         for (size_t i = 0; i < spheres.size(); i++)
             std::printf("%s[%.9g, %.9g, %.9g, %.9g, %.9g, %.9g]", i ? ", " : "", spheres[i].x, spheres[i].y,
                         spheres[i].z, spheres[i].a, spheres[i].n_re, spheres[i].n_im);
@@ -480,7 +513,43 @@ int main(int argc, char** argv) {
             if (check(bs_sample_waves_compat(ctx, nk))) return 1;
         }
     }
-    if (check(bs_simulate(ctx, precision))) return 1;
+    if (sources.empty()) {
+        if (check(bs_simulate(ctx, precision))) return 1;
+        // fileoutStruct::saveNearField / saveFarField (fileout.cu:3-45): field images of
+        // the last source in the single-source path
+        auto field_image = [&](const std::string& file, bool far) -> int {
+            if (file.empty()) return 0;
+            bool mag = fieldStr == "magnitude", re = fieldStr == "real", im = fieldStr == "imaginary";
+            if (!mag && !re && !im) return 0;  // other output types write nothing here
+            if (is_binary(file)) {
+                std::cout << "\t\t field images need an image file name (.bmp or .png): " << file << std::endl;
+                return 0;
+            }
+            int n = 0;
+            std::vector<double> f;
+            if (far) {
+                n = p.resolution * p.supersample;
+                f.resize(2 * (size_t)n * n);
+                if (check(bs_get_far_field(ctx, BS_FIELD_TOTAL, f.data(), (size_t)n * n))) return 1;
+            } else {
+                bs_info inf{};
+                bs_get_info(ctx, &inf);
+                n = inf.nf_res;
+                f.resize(2 * (size_t)n * n);
+                if (check(bs_get_field(ctx, BS_FIELD_TOTAL, f.data(), (size_t)n * n))) return 1;
+            }
+            std::vector<double> v((size_t)n * n);
+            for (size_t i = 0; i < v.size(); i++)
+                v[i] = mag ? std::sqrt(f[2 * i] * f[2 * i] + f[2 * i + 1] * f[2 * i + 1]) : (re ? f[2 * i] : f[2 * i + 1]);
+            std::string err;
+            if (!bsio::write_scalar_image(file, n, n, v, mag, cmap, err)) return fail("BIMSim Error: " + err);
+            return 0;
+        };
+        if (field_image(nearFile, false) || field_image(farFile, true)) return 1;
+    } else {
+        // SimulateExtendedSource (microscope.cu:873-913): the detector sums the point sources
+        if (check(bs_simulate_sources(ctx, sources.data(), (int)(sources.size() / 4), precision))) return 1;
+    }
 
     // ---- fileoutStruct::saveDetector (fileout.cu:47-159) ----
     double band = wavenumber ? (double)(10000.0f / lambda) : (double)lambda;
@@ -492,8 +561,13 @@ int main(int argc, char** argv) {
         if (file.empty()) return 0;
         std::cout << "\t\t saving: " << file << std::endl;
         if (!is_binary(file)) {
-            std::cout << "\t\t image output is not part of this build (" << file
-                      << "); give a file name without an image extension to write ENVI" << std::endl;
+            // scalarslice::toImage(file) with its defaults: range [0, max], Brewer map
+            // (the --colormap flag reaches only the field images, fileout.cu:3-45)
+            std::vector<double> v((size_t)p.resolution * p.resolution);
+            if (check(bs_get_image_f64(ctx, kind, v.data(), v.size()))) return 1;
+            std::string err;
+            if (!bsio::write_scalar_image(file, p.resolution, p.resolution, v, true, bsio::CM_BREWER, err))
+                return fail("BIMSim Error: " + err);
             return 0;
         }
         return check(bs_write_envi(ctx, kind, file.c_str(), append ? 1 : 0, band));

@@ -165,6 +165,8 @@ struct bs_ctx {
 
     DevBuf d_sph, d_waves, d_kw4, d_ph, d_A, d_B, d_mie, d_tab, d_tabscr, d_legP, d_lut, d_uft, d_uftscr;
     DevBuf d_cones, d_cnt;  // per-chunk wave cones; staged / total counters of the mixed LUT kernel
+    DevBuf d_far;           // far fields Ud, Ufd on request (bs_get_far_field)
+    int det_Nv = 0;         // passband rows of the last detector run (0: no far field)
     DevBuf d_fields;  // [2][R*R] U then Uf
     DevBuf d_su, d_sv, d_mask, d_wx, d_wy, d_wix, d_wiy, d_f1, d_f2, d_g1, d_I, d_D, d_img;
     int legP_theta = 0, legP_L = 0;
@@ -185,7 +187,7 @@ static std::vector<DevBuf*> ctx_bufs(bs_ctx* c) {
     return {&c->d_sph, &c->d_waves, &c->d_kw4, &c->d_ph, &c->d_A, &c->d_B, &c->d_mie, &c->d_tab,
             &c->d_tabscr, &c->d_legP, &c->d_lut, &c->d_uft, &c->d_uftscr, &c->d_fields, &c->d_su,
             &c->d_sv, &c->d_mask, &c->d_wx, &c->d_wy, &c->d_wix, &c->d_wiy, &c->d_f1, &c->d_f2,
-            &c->d_g1, &c->d_I, &c->d_D, &c->d_img, &c->d_cones, &c->d_cnt};
+            &c->d_g1, &c->d_I, &c->d_D, &c->d_img, &c->d_cones, &c->d_cnt, &c->d_far};
 }
 
 static void release_all(bs_ctx* c) {
@@ -391,7 +393,7 @@ static void passbands(const bs_ctx* c, std::vector<int>& su, std::vector<int>& s
 }
 
 template <class T>
-static bs_status run_detector(bs_ctx* c) {
+static bs_status run_detector(bs_ctx* c, bool accumulate) {
     const bs_params& p = c->prm;
     const int R = c->R;
     double du, dv;
@@ -400,9 +402,10 @@ static bs_status run_detector(bs_ctx* c) {
     double lo = p.objective[0] / p.lambda, hi = p.objective[1] / p.lambda;
     auto freq = [R](int i, double step) { return bin_freq(i, R, step); };
     const int Nu = (int)su.size(), Nv = (int)sv.size(), C = c->crop, res = c->res;
+    c->det_Nv = (Nu == 0) ? 0 : Nv;
     CK(c->d_D.ensure(2 * (size_t)res * res * sizeof(T)));
     if (Nu == 0 || Nv == 0) {
-        CK(cudaMemsetAsync(c->d_D.p, 0, 2 * (size_t)res * res * sizeof(T), c->st));
+        if (!accumulate) CK(cudaMemsetAsync(c->d_D.p, 0, 2 * (size_t)res * res * sizeof(T), c->st));
         return BS_OK;
     }
     std::vector<float> mask((size_t)Nv * Nu);
@@ -460,7 +463,7 @@ static bs_status run_detector(bs_ctx* c) {
     launch_cgemm<T>(C, C, Nv, 2, wiy, Nv, 0, g1, C, (long long)Nv * C, nullptr, C, (long long)C * C, 2, nullptr,
                     scale, I, c->st);
     LAUNCHED(c);
-    launch_bin<T>(res, c->ss, 2, I, c->d_D.as<T>(), c->st);
+    launch_bin<T>(res, c->ss, 2, accumulate ? 1 : 0, I, c->d_D.as<T>(), c->st);
     LAUNCHED(c);
     return BS_OK;
 }
@@ -981,9 +984,11 @@ bs_status bs_estimate_bytes(const bs_params* params, const bs_sphere* spheres, i
     return BS_OK;
 }
 
-bs_status bs_simulate(bs_ctx* c, bs_precision prec) {
-    if (!c) return fail(BS_ERR_ARG, "bs_simulate: null context");
-    if (prec != BS_PREC_FP64 && prec != BS_PREC_MIXED) return fail(BS_ERR_ARG, "bs_simulate: unknown precision");
+}  // extern "C"
+
+// One slice; with accumulate the detector images add to those of the previous
+// slice on this context (same precision and detector size).
+static bs_status simulate_impl(bs_ctx* c, bs_precision prec, bool accumulate) {
     c->have = false;
     bs_status st = derive(c);
     if (st != BS_OK) return st;
@@ -993,7 +998,7 @@ bs_status bs_simulate(bs_ctx* c, bs_precision prec) {
     int64_t l0 = c->launches;
     st = (prec == BS_PREC_FP64) ? run_nearfield<double>(c) : run_nearfield<float>(c);
     if (st != BS_OK) return st;
-    st = (prec == BS_PREC_FP64) ? run_detector<double>(c) : run_detector<float>(c);
+    st = (prec == BS_PREC_FP64) ? run_detector<double>(c, accumulate) : run_detector<float>(c, accumulate);
     if (st != BS_OK) return st;
     cudaEventRecord(c->ev[5], c->st);
     CK(cudaStreamSynchronize(c->st));
@@ -1018,6 +1023,102 @@ bs_status bs_simulate(bs_ctx* c, bs_precision prec) {
         c->stats.lut_chunks_total = (int64_t)cnt[1];
     }
     c->have = true;
+    return BS_OK;
+}
+
+extern "C" {
+
+bs_status bs_simulate(bs_ctx* c, bs_precision prec) {
+    if (!c) return fail(BS_ERR_ARG, "bs_simulate: null context");
+    if (prec != BS_PREC_FP64 && prec != BS_PREC_MIXED) return fail(BS_ERR_ARG, "bs_simulate: unknown precision");
+    return simulate_impl(c, prec, false);
+}
+
+bs_status bs_simulate_sources(bs_ctx* c, const double* sources, int32_t n, bs_precision prec) {
+    if (!c || !sources || n < 1) return fail(BS_ERR_ARG, "bs_simulate_sources: need at least one source");
+    if (prec != BS_PREC_FP64 && prec != BS_PREC_MIXED)
+        return fail(BS_ERR_ARG, "bs_simulate_sources: unknown precision");
+    for (int32_t i = 0; i < n; i++)
+        for (int k = 0; k < 4; k++)
+            if (!std::isfinite(sources[4 * i + k]))
+                return fail(BS_ERR_ARG, "bs_simulate_sources: source %d is not finite", i + 1);
+    const bs_params saved = c->prm;
+    const bool saved_reuse = c->reuse;
+    c->reuse = true;  // the sphere tables do not depend on the focus or the amplitude
+    bs_stats sum{};
+    bs_status st = BS_OK;
+    for (int32_t i = 0; i < n && st == BS_OK; i++) {
+        for (int k = 0; k < 3; k++) c->prm.focus[k] = sources[4 * i + k];
+        c->prm.amplitude = sources[4 * i + 3];
+        st = simulate_impl(c, prec, i > 0);
+        if (st != BS_OK) break;
+        const bs_stats& s = c->stats;
+        sum.ms_total += s.ms_total;
+        sum.ms_uf += s.ms_uf;
+        sum.ms_mie += s.ms_mie;
+        sum.ms_lut += s.ms_lut;
+        sum.ms_us += s.ms_us;
+        sum.ms_detector += s.ms_detector;
+        sum.kernel_launches += s.kernel_launches;
+        sum.us_interactions += s.us_interactions;
+        sum.lut_chunks_staged += s.lut_chunks_staged;
+        sum.lut_chunks_total += s.lut_chunks_total;
+        sum.lut_tables_built += s.lut_tables_built;
+        sum.lut_staged_predicted = s.lut_staged_predicted;
+    }
+    c->reuse = saved_reuse;
+    if (!saved_reuse) c->lut_valid = false;
+    const bool have = c->have;
+    c->prm = saved;
+    c->have = have && st == BS_OK;  // images stay valid: they do not depend on prm after the run
+    if (st == BS_OK) c->stats = sum;
+    return st;
+}
+
+}  // extern "C"
+
+template <class T>
+static bs_status far_field(bs_ctx* c, int which, double* host) {
+    const int C = c->crop, Nv = c->det_Nv;
+    const size_t n = (size_t)C * C;
+    if (Nv == 0) {  // nothing passes the objective: the far field is zero
+        std::fill(host, host + 2 * n, 0.0);
+        return BS_OK;
+    }
+    CK(c->d_far.ensure(n * sizeof(cpx<T>)));
+    const T scale = (T)(1.0 / ((double)c->R * (double)c->R));
+    const cpx<T>* g1 = c->d_g1.as<cpx<T>>() + (size_t)which * Nv * C;
+    launch_cgemm<T>(C, C, Nv, 1, c->d_wiy.as<cpx<T>>(), Nv, 0, g1, C, 0, c->d_far.as<cpx<T>>(), C, 0, 3, nullptr,
+                    scale, nullptr, c->st);
+    LAUNCHED(c);
+    std::vector<cpx<T>> t(n);
+    CK(cudaMemcpyAsync(t.data(), c->d_far.p, n * sizeof(cpx<T>), cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    for (size_t i = 0; i < n; i++) {
+        host[2 * i] = (double)t[i].re;
+        host[2 * i + 1] = (double)t[i].im;
+    }
+    return BS_OK;
+}
+
+extern "C" {
+
+bs_status bs_get_far_field(bs_ctx* c, bs_field_kind kind, double* host, size_t count) {
+    if (!c || !host) return fail(BS_ERR_ARG, "bs_get_far_field: null argument");
+    if (!c->have) return fail(BS_ERR_STATE, "bs_get_far_field: no simulation result");
+    if (kind != BS_FIELD_TOTAL && kind != BS_FIELD_INCIDENT) return fail(BS_ERR_ARG, "bs_get_far_field: unknown field");
+    if (count < (size_t)c->crop * c->crop)
+        return fail(BS_ERR_ARG, "bs_get_far_field: need %zu complex values", (size_t)c->crop * c->crop);
+    const int which = kind == BS_FIELD_TOTAL ? 0 : 1;
+    return c->prec == BS_PREC_FP64 ? far_field<double>(c, which, host) : far_field<float>(c, which, host);
+}
+
+bs_status bs_plane_point(const bs_params* params, double u, double v, double* xyz) {
+    if (!params || !xyz) return fail(BS_ERR_ARG, "bs_plane_point: null argument");
+    Quad q = quad_from(params->plane_min, params->plane_max, params->plane_normal);
+    xyz[0] = q.A.x + q.X.x * u + q.Y.x * v;
+    xyz[1] = q.A.y + q.X.y * u + q.Y.y * v;
+    xyz[2] = q.A.z + q.X.z * u + q.Y.z * v;
     return BS_OK;
 }
 

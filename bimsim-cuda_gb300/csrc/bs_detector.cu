@@ -109,6 +109,8 @@ __global__ void __launch_bounds__(256) cgemm_kernel(int M, int N, int K, const c
                 vr *= scale;
                 vi *= scale;
                 I[o] = vr * vr + vi * vi;
+            } else if (epi == 3) {  // scaled field (the far field Ud, Ufd)
+                C[o] = mk(vr * scale, vi * scale);
             } else {
                 if (epi == 1) {
                     T mval = (T)mask[(long long)gm * N + gn];
@@ -121,7 +123,7 @@ __global__ void __launch_bounds__(256) cgemm_kernel(int M, int N, int K, const c
 }
 
 template <class T>
-__global__ void bin_kernel(int res, int ss, const T* __restrict__ I, T* __restrict__ D) {
+__global__ void bin_kernel(int res, int ss, int accumulate, const T* __restrict__ I, T* __restrict__ D) {
     int b = blockIdx.y;
     int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= res * res) return;
@@ -131,7 +133,9 @@ __global__ void bin_kernel(int res, int ss, const T* __restrict__ I, T* __restri
     T acc = 0;
     for (int ix = 0; ix < ss; ix++)
         for (int iy = 0; iy < ss; iy++) acc += Ib[(long long)(iv * ss + iy) * cw + iu * ss + ix];
-    D[(long long)b * res * res + e] = acc / (T)(ss * ss);
+    // accumulate: the detector sums over point sources (IntegrateAndResample adds, fieldslice.cu:71-108)
+    T* out = D + (long long)b * res * res + e;
+    *out = (accumulate ? *out : (T)0) + acc / (T)(ss * ss);
 }
 
 template <class T>
@@ -161,9 +165,9 @@ void launch_cgemm(int M, int N, int K, int batch, const cpx<T>* A, int lda, long
 }
 
 template <class T>
-void launch_bin(int res, int ss, int batch, const T* I, T* D, cudaStream_t st) {
+void launch_bin(int res, int ss, int batch, int accumulate, const T* I, T* D, cudaStream_t st) {
     dim3 grid((res * res + 255) / 256, batch);
-    bin_kernel<T><<<grid, 256, 0, st>>>(res, ss, I, D);
+    bin_kernel<T><<<grid, 256, 0, st>>>(res, ss, accumulate, I, D);
 }
 
 template <class T>
@@ -175,7 +179,7 @@ void launch_image(int n, int kind, const T* D, const T* Di, T* out, cudaStream_t
     template void launch_twiddle<T>(int, int, const int*, int, int, int, int, int, cpx<T>*, cudaStream_t);      \
     template void launch_cgemm<T>(int, int, int, int, const cpx<T>*, int, long long, const cpx<T>*, int,       \
                                   long long, cpx<T>*, int, long long, int, const float*, T, T*, cudaStream_t); \
-    template void launch_bin<T>(int, int, int, const T*, T*, cudaStream_t);                                    \
+    template void launch_bin<T>(int, int, int, int, const T*, T*, cudaStream_t);                                    \
     template void launch_image<T>(int, int, const T*, const T*, T*, cudaStream_t);
 BS_DET_INST(float)
 BS_DET_INST(double)

@@ -75,15 +75,16 @@ void launch_twiddle(int ni, int nj, const int* freq, int off_i, int R, int sign,
 // C[b] (M x N) = A[b] (M x K) * B[b] (K x N), complex, row-major, batch over
 // blockIdx.z with element strides sA, sB, sC (0 = shared operand).
 // epi 0: store; epi 1: multiply by mask[m*N + n]; epi 2: store |scale * c|^2
-// into the real array I[b] (M x N, batch stride sC).
+// into the real array I[b] (M x N, batch stride sC); epi 3: store scale * c.
 template <class T>
 void launch_cgemm(int M, int N, int K, int batch, const cpx<T>* A, int lda, long long sA, const cpx<T>* B, int ldb,
                   long long sB, cpx<T>* C, int ldc, long long sC, int epi, const float* mask, T scale, T* I,
                   cudaStream_t st);
 
-// D[b][iv][iu] = sum over the ss x ss block of I[b] / ss^2 (fieldslice.cu:71-108)
+// D[b][iv][iu] (+)= sum over the ss x ss block of I[b] / ss^2 (fieldslice.cu:71-108);
+// accumulate adds to D (the detector sums point sources)
 template <class T>
-void launch_bin(int res, int ss, int batch, const T* I, T* D, cudaStream_t st);
+void launch_bin(int res, int ss, int batch, int accumulate, const T* I, T* D, cudaStream_t st);
 
 // image kinds 2, 3: -log10(D/Di), D/Di (microscope.cu:722-775); 0, 1: copies
 template <class T>

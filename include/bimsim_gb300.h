@@ -170,6 +170,12 @@ bs_status bs_get_image_f64(bs_ctx* ctx, bs_image_kind kind, double* host, size_t
  * nf_res^2 complex values. */
 bs_status bs_get_field(bs_ctx* ctx, bs_field_kind kind, double* host, size_t count);
 
+/* Far field at the detector (microscopeStruct::Ud / Ufd after the objective
+ * band-pass and crop, microscope.cu:608-655, scaled by 1/R^2 like ScaleField):
+ * (res*ss)^2 interleaved (re, im) doubles of the last run (the last point
+ * source after bs_simulate_sources). */
+bs_status bs_get_far_field(bs_ctx* ctx, bs_field_kind kind, double* host, size_t count);
+
 /* Append or write one band to an ENVI file (scalarslice::toEnvi,
  * scalarslice.cu:146-166; rts/envi/envi.h:196-433).  band_value is the
  * header's wavelength entry (lambda, or 1e4/lambda for --nu). */
@@ -200,6 +206,22 @@ bs_status bs_get_lut(bs_ctx* ctx, int32_t sphere, int32_t which, double* host, s
  * CUDA events.  The denominator of the scattered-field kernels' roofline.
  * No reference counterpart. */
 bs_status bs_measure_fma_peak(double* fp32_tflops, double* fp64_tflops);
+
+/* Extended (point-source) illumination: microscopeStruct::SimulateExtendedSource
+ * (microscope.cu:873-913) over the point sources LoadExtendedSource makes from
+ * a source image (microscope.cu:1257-1296).  Source i has focus
+ * sources[4i .. 4i+2] and amplitude sources[4i+3]; each is simulated like
+ * bs_simulate and the detector images add up (D = sum D_i, Di = sum Di_i, as
+ * IntegrateAndResample accumulates, fieldslice.cu:71-108); absorbance and
+ * transmittance come from the sums.  The sphere tables do not depend on the
+ * focus or amplitude and are built once per call.  The context's own focus
+ * and amplitude are kept; bs_get_stats sums the per-source timings. */
+bs_status bs_simulate_sources(bs_ctx* ctx, const double* sources, int32_t n, bs_precision prec);
+
+/* Point pos(u, v) = A + u X + v Y of the detector plane quad (microscopeStruct::pos;
+ * the quad of arguments.h:340-407 built by rts/math/quad.h:55-84), e.g. for
+ * placing point sources at image pixels (u = x / width, v = y / height). */
+bs_status bs_plane_point(const bs_params* params, double u, double v, double* xyz);
 
 /* Spectral sweep: the reference's per-wavelength runs (one `bimsim --lambda
  * ... --append` process per band, runBimSim.py:80-86 and specimage.py) in one

@@ -999,7 +999,7 @@ void fft2(std::vector<cd>& f, int R, int sign) {
 
 // applyBandpass / bandpass / getFarField / integrateDetector
 // (microscope.cu:495-526, 608-662; fieldslice.cpp:25-94; fieldslice.cu:71-108,319-338)
-void detector(const bs_params& p, const Geom& g, const cd* U, double* D) {
+std::vector<cd> bandpassed(const bs_params& p, const Geom& g, const cd* U) {
     const int R = g.R;
     std::vector<cd> f(U, U + (size_t)R * R);
     fft2(f, R, -1);
@@ -1014,6 +1014,12 @@ void detector(const bs_params& p, const Geom& g, const cd* U, double* D) {
         }
     }
     fft2(f, R, +1);
+    return f;
+}
+
+void detector(const bs_params& p, const Geom& g, const cd* U, double* D) {
+    const int R = g.R;
+    std::vector<cd> f = bandpassed(p, g, U);
     double sc = 1.0 / ((double)R * R);
     int cr = g.crop_res, off = g.crop_off, ss = g.ss, res = g.res;
     for (int iv = 0; iv < res; iv++)
@@ -1340,6 +1346,20 @@ int bso_nearfield_rows(const bs_params* p, const bs_sphere* s, int ns, const dou
     Scene sc;
     scene_init(sc, *p, s, ns, waves, nk);
     nearfield_rows(sc, row0, row1, nthreads, reinterpret_cast<cd*>(U), nullptr);
+    return 0;
+}
+
+// the far field Ud: band-passed field on the crop, scaled by 1/R^2 (getFarField, microscope.cu:641-655)
+int bso_far_field(const bs_params* p, const double* U, double* out) {
+    Geom g = derive(*p);
+    std::vector<cd> f = bandpassed(*p, g, reinterpret_cast<const cd*>(U));
+    const double sc = 1.0 / ((double)g.R * g.R);
+    for (int v = 0; v < g.crop_res; v++)
+        for (int u = 0; u < g.crop_res; u++) {
+            cd val = f[(size_t)(g.crop_off + v) * g.R + (g.crop_off + u)] * sc;
+            out[2 * ((size_t)v * g.crop_res + u)] = val.real();
+            out[2 * ((size_t)v * g.crop_res + u) + 1] = val.imag();
+        }
     return 0;
 }
 

@@ -85,6 +85,8 @@ int bso_nearfield_rows(const bs_params* p, const bs_sphere* s, int ns,
 
 /* Detector chain on given near fields (microscope.cu:608-662, 722-814). */
 int bso_detector(const bs_params* p, const double* U, const double* Uf, double* D, double* Di);
+/* Far field Ud (crop_res^2 complex, interleaved): band-passed U on the crop, scaled by 1/R^2. */
+int bso_far_field(const bs_params* p, const double* U, double* out);
 
 /* Forward (sign=-1) or inverse (sign=+1, unnormalised) 1-D DFT of n complex. */
 int bso_fft(int n, int sign, double* data);

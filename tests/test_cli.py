@@ -1,8 +1,12 @@
-"""The `bimsim` command line: flag grammar and derived parameters (CPU), and an
-end-to-end run writing ENVI files (GPU)."""
+"""The `bimsim` command line: flag grammar and derived parameters, source-image
+reading and the image writers (CPU), and end-to-end runs writing ENVI and image
+files (GPU)."""
 import json
 import os
+import struct
 import subprocess
+import tempfile
+import zlib
 
 import numpy as np
 import pytest
@@ -13,11 +17,13 @@ from bimsim_gb300 import BS_IMG_ABSORBANCE, BS_IMG_INCIDENT, BS_IMG_INTENSITY, B
 EXE = os.path.join(os.path.dirname(lib.library_path()), "bimsim")
 
 
-def run(*args, check=True):
+def run(*args, check=True, cwd=None):
     if not os.path.exists(EXE):
         from bimsim_gb300 import build
         build.build()
-    r = subprocess.run([EXE] + [str(a) for a in args], capture_output=True, text=True)
+    # the reference's default outputs (out_*.bmp) land in cwd: keep them out of the repository
+    r = subprocess.run([EXE] + [str(a) for a in args], capture_output=True, text=True,
+                       cwd=cwd or tempfile.gettempdir())
     if check:
         assert r.returncode == 0, r.stdout + r.stderr
     return r
@@ -107,7 +113,7 @@ def test_cli_end_to_end_envi(tmp_path):
               "--precision", "fp64", "--lut-res", 96, 128]
     out = tmp_path / "I"
     absf = tmp_path / "A"
-    run(*common, "--intensity", out, "--absorbance", absf, "--incident", "", "--absorbance-spec", "")
+    run(*common, "--intensity", out, "--absorbance", absf, "--incident", "", "--absorbance-spec", "", cwd=tmp_path)
     I = np.fromfile(out, dtype=np.float32).reshape(16, 16)
     hdr = open(str(out) + ".hdr").read()
     assert "bands = 1" in hdr and "wavelength = {\n3}" in hdr
@@ -118,6 +124,191 @@ def test_cli_end_to_end_envi(tmp_path):
     assert np.linalg.norm(I - D) / np.linalg.norm(D) < 1e-6
     A = np.fromfile(absf, dtype=np.float32).reshape(16, 16)
     assert np.linalg.norm(A + np.log10(D / Di)) / np.linalg.norm(np.log10(D / Di)) < 1e-5
-    run(*common, "--intensity", out, "--absorbance", "", "--incident", "", "--absorbance-spec", "", "--append")
+    run(*common, "--intensity", out, "--absorbance", "", "--incident", "", "--absorbance-spec", "", "--append",
+        cwd=tmp_path)
     assert "bands = 2" in open(str(out) + ".hdr").read()
     assert np.fromfile(out, dtype=np.float32).size == 2 * 256
+
+
+# ---------------------------------------------------------------------------
+# source images (--extended-source) and image outputs
+# ---------------------------------------------------------------------------
+def write_bmp(path, rows, bpp):
+    """rows: list of lists of (r, g, b) (bpp 24) or palette indices (bpp 8, grey palette), top row first."""
+    h, w = len(rows), len(rows[0])
+    stride = (w * bpp // 8 + 3) & ~3
+    pal = b"".join(bytes((i, i, i, 0)) for i in range(256)) if bpp == 8 else b""
+    off = 54 + len(pal)
+    data = b""
+    for r in reversed(rows):
+        line = b"".join(bytes((px[2], px[1], px[0])) for px in r) if bpp == 24 else bytes(r)
+        data += line + b"\0" * (stride - len(line))
+    hdr = b"BM" + struct.pack("<IHHI", off + len(data), 0, 0, off)
+    hdr += struct.pack("<IiiHHIIiiII", 40, w, h, 1, bpp, 0, len(data), 2835, 2835, 256 if bpp == 8 else 0, 0)
+    open(path, "wb").write(hdr + pal + data)
+
+
+def test_extended_source_images_give_one_source_per_nonzero_pixel(tmp_path):
+    pgm = tmp_path / "s.pgm"
+    pgm.write_text("P2\n# comment\n3 2\n255\n0 128 255\n10 0 0\n")
+    assert dry("--extended-source", pgm, "--xy", 10, 0)["point_sources"] == 3
+    bmp24 = tmp_path / "s24.bmp"
+    write_bmp(bmp24, [[(0, 9, 9), (200, 0, 0)], [(1, 0, 0), (0, 0, 0)]], 24)  # first channel = red
+    assert dry("--extended-source", bmp24, "--xy", 10, 0)["point_sources"] == 2
+    bmp8 = tmp_path / "s8.bmp"
+    write_bmp(bmp8, [[0, 3, 0, 7], [5, 0, 0, 0]], 8)
+    assert dry("--extended-source", bmp8, "--xy", 10, 0)["point_sources"] == 3
+    r = run("--extended-source", tmp_path / "missing.pgm", "--dry-run", check=False)
+    assert r.returncode == 1 and "cannot open" in r.stdout
+    r = run("--interpolate", 1, "--dry-run", check=False)
+    assert r.returncode == 1
+
+
+def brewer_rgb(values, vmin, vmax):
+    """Restatement of the Brewer map (rts/visualization/colormap.h) in float32 arithmetic."""
+    ctrl = np.array([[49, 54, 149], [69, 117, 180], [116, 173, 209], [171, 217, 233], [224, 243, 248],
+                     [255, 255, 191], [254, 224, 144], [253, 174, 97], [244, 109, 67], [215, 48, 39],
+                     [165, 0, 38]], dtype=np.float64)
+    ctrl = (np.round(ctrl / 255.0 * 1e6) / 1e6).astype(np.float32)
+    a = ((np.asarray(values, np.float64) - vmin) / (vmax - vmin)).astype(np.float32)
+    x = np.float32(11) * a
+    fl = np.floor(x)
+    fr = (x - fl).astype(np.float32)
+    i0 = np.clip(fl.astype(int), 0, 10)
+    i1 = np.clip(fl.astype(int) + 1, 0, 10)
+    c = (np.float32(1) - fr)[:, None] * ctrl[i0] + fr[:, None] * ctrl[i1]
+    return (np.float32(255) * c.astype(np.float32)).astype(np.uint8)
+
+
+def read_bmp24(path):
+    b = open(path, "rb").read()
+    off, = struct.unpack("<I", b[10:14])
+    w, h = struct.unpack("<ii", b[18:26])
+    stride = (w * 3 + 3) & ~3
+    img = np.zeros((h, w, 3), np.uint8)
+    for y in range(h):
+        row = b[off + (h - 1 - y) * stride: off + (h - 1 - y) * stride + 3 * w]
+        img[y] = np.frombuffer(row, np.uint8).reshape(w, 3)[:, ::-1]
+    return img
+
+
+def read_png_rgb(path):
+    b = open(path, "rb").read()
+    assert b[:8] == bytes([137, 80, 78, 71, 13, 10, 26, 10])
+    pos, idat, w = 8, b"", 0
+    while pos < len(b):
+        n, = struct.unpack(">I", b[pos:pos + 4])
+        typ, data = b[pos + 4:pos + 8], b[pos + 8:pos + 8 + n]
+        crc, = struct.unpack(">I", b[pos + 8 + n:pos + 12 + n])
+        assert crc == zlib.crc32(typ + data) & 0xFFFFFFFF
+        if typ == b"IHDR":
+            w, h = struct.unpack(">II", data[:8])
+            assert data[8:10] == bytes([8, 2])
+        elif typ == b"IDAT":
+            idat += data
+        pos += 12 + n
+    raw = zlib.decompress(idat)
+    rows = [raw[y * (3 * w + 1): (y + 1) * (3 * w + 1)] for y in range(h)]
+    assert all(r[0] == 0 for r in rows)
+    return np.stack([np.frombuffer(r[1:], np.uint8).reshape(w, 3) for r in rows])
+
+
+@pytest.fixture(scope="module")
+def image_writer(tmp_path_factory):
+    """A small driver of cli/image_io.cpp: writes colour-mapped values read from stdin."""
+    d = tmp_path_factory.mktemp("imgw")
+    src = d / "drv.cpp"
+    src.write_text(r'''
+#include "image_io.h"
+#include <iostream>
+int main(int argc, char** argv) {
+    int w, h, pos, cm; std::cin >> w >> h >> pos >> cm;
+    std::vector<double> v((size_t)w * h);
+    for (auto& x : v) std::cin >> x;
+    std::string err;
+    if (!bsio::write_scalar_image(argv[1], w, h, v, pos != 0, (bsio::Colormap)cm, err)) { std::cout << err; return 1; }
+    return 0;
+}''')
+    cli = os.path.join(os.path.dirname(os.path.dirname(lib.library_path())), "cli")
+    exe = d / "drv"
+    subprocess.check_call(["g++", "-std=c++17", "-O2", "-I", cli, str(src), os.path.join(cli, "image_io.cpp"),
+                           "-o", str(exe)])
+
+    def write(path, vals, positive=True, cm=0):
+        h, w = vals.shape
+        inp = f"{w} {h} {int(positive)} {cm}\n" + " ".join(repr(float(x)) for x in vals.ravel())
+        r = subprocess.run([str(exe), str(path)], input=inp, capture_output=True, text=True)
+        return r
+    return write
+
+
+def test_brewer_bmp_and_png_match_the_reference_colormap(image_writer, tmp_path):
+    rng = np.random.default_rng(7)
+    vals = rng.uniform(0, 3, (5, 7))
+    vals[2, 3] = 3.5                                  # the maximum: range [0, 3.5]
+    for ext, reader in ((".bmp", read_bmp24), (".png", read_png_rgb)):
+        path = tmp_path / ("a" + ext)
+        assert image_writer(path, vals).returncode == 0
+        img = reader(path)
+        assert img.shape == (5, 7, 3)
+        exp = brewer_rgb(vals.ravel(), 0.0, 3.5).reshape(5, 7, 3)
+        assert np.array_equal(img, exp)
+    # the six-decimal control points: (69, 117, 180) of the second point render as (68, 117, 179)
+    ctrl = (np.round(np.array([69, 117, 180]) / 255.0 * 1e6) / 1e6).astype(np.float32)
+    assert (np.float32(255) * ctrl).astype(np.uint8).tolist() == [68, 117, 179]
+
+
+def test_gray_and_signed_range(image_writer, tmp_path):
+    vals = np.array([[-2.0, -1.0, 0.0, 1.0]])
+    path = tmp_path / "g.bmp"
+    assert image_writer(path, vals, positive=False, cm=1).returncode == 0
+    img = read_bmp24(path)
+    expect = (np.float32(255) * np.clip(((vals.ravel() + 2) / 4).astype(np.float32), 0, 1)).astype(np.uint8)
+    assert np.array_equal(img[0, :, 0], expect) and np.array_equal(img[0, :, 1], expect)
+    r = image_writer(tmp_path / "x.jpg", vals)
+    assert r.returncode == 1 and "not supported" in r.stdout
+
+
+@pytest.mark.gpu
+def test_cli_extended_source_and_image_outputs(tmp_path):
+    """--extended-source sums point sources exactly like bs_simulate_sources; image outputs are the
+    colour-mapped detector images; near- and far-field images are written by default."""
+    from bimsim_gb300 import BS_PREC_MIXED, lib as L, scenes
+    src = tmp_path / "s.pgm"
+    src.write_text("P2\n2 2\n255\n0 255\n128 0\n")
+    waves = scenes.mc_waves(24, 0, 0.5, seed=22)
+    wfile = tmp_path / "w.txt"
+    np.savetxt(wfile, waves)
+    common = ["--spheres", 0.5, 0, 0, 2, 0, "--materials", 1.4, 0.05, "--lambda", 3, "--condenser", 0, 0.5,
+              "--objective", 0, 0.5, "--resolution", 16, "--xy", 12, 0, "--waves-file", wfile, "--lut-res", 96, 128,
+              "--extended-source", src]
+    run(*common, "--intensity", tmp_path / "I", "--incident", "", "--absorbance", "", "--absorbance-spec", "",
+        cwd=tmp_path)
+    I = np.fromfile(tmp_path / "I", dtype=np.float32).reshape(16, 16)
+    p = abi.make_params(lam=3, condenser=(0, 0.5), objective=(0, 0.5), xy=(12, 0), resolution=16, us_lut_r=96,
+                        us_lut_theta=128)
+    srcs = []
+    for x, y, v in ((1, 0, 255), (0, 1, 128)):   # x outer, y inner, non-zero pixels only
+        f = L.plane_point(p, np.float32(x / 2), np.float32(y / 2))
+        srcs.append([*f, float(np.float32(v) / np.float32(255))])
+    with Context(p) as ctx:
+        ctx.set_spheres([(0.5, 0, 0, 2, float(np.float32(1.4)), float(np.float32(0.05)))])
+        ctx.set_waves(waves)
+        ctx.simulate_sources(np.array(srcs), BS_PREC_MIXED)
+        ref = ctx.image(BS_IMG_INTENSITY)
+    assert np.array_equal(I, ref)
+    # default outputs: detector images as BMP (Brewer), near and far field magnitude images
+    d2 = tmp_path / "run2"
+    d2.mkdir()
+    run(*common[:-2], "--absorbance-spec", "", cwd=d2)
+    for name, n in (("out_i.bmp", 16), ("out_inc.bmp", 16), ("out_a.bmp", 16), ("out_n.bmp", 48), ("out_f.bmp", 16)):
+        img = read_bmp24(d2 / name)
+        assert img.shape == (n, n, 3), name
+    run(*common[:-2], "--intensity", d2 / "I", "--absorbance-spec", "", "--near-field", "", "--far-field", "",
+        cwd=d2)
+    Ie = np.fromfile(d2 / "I", dtype=np.float32).astype(np.float64).reshape(16, 16)
+    img = read_bmp24(d2 / "out_i.bmp")
+    m = Ie.ravel()[np.argmax(np.abs(Ie.ravel()))]
+    exp = brewer_rgb(Ie.ravel(), 0.0, m).reshape(16, 16, 3)
+    # the image is mapped from the double image, the expectation from its float32 ENVI copy
+    assert np.mean(np.abs(img.astype(int) - exp.astype(int)) <= 1) == 1.0
