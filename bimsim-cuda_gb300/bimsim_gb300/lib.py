@@ -56,6 +56,7 @@ def library():
         "bs_simulate_sources": ([vp, vp, i32, C.c_int], C.c_int),
         "bs_plane_point": ([vp, C.c_double, C.c_double, vp], C.c_int),
         "bs_get_far_field": ([vp, C.c_int, vp, sz], C.c_int),
+        "bs_material_eval": ([C.c_char_p, vp, i32, vp], C.c_int),
         "bs_set_lut_reuse": ([vp, i32], C.c_int),
         "bs_set_lut_staging": ([vp, i32], C.c_int),
         "bs_release_buffers": ([vp], C.c_int),
@@ -215,6 +216,17 @@ class Context:
 
     def release_buffers(self):
         self._check(self.lib.bs_release_buffers(self.h))
+
+
+def material_eval(path, lambdas):
+    """Complex refractive index of a material file at each wavelength (um)."""
+    lib = library()
+    lam = np.ascontiguousarray(lambdas, dtype=np.float64).reshape(-1)
+    out = np.zeros(2 * lam.size)
+    st = lib.bs_material_eval(str(path).encode(), _p(lam), lam.size, _p(out))
+    if st != 0:
+        raise BimsimError(st, lib.bs_last_error().decode())
+    return out.view(np.complex128)
 
 
 def plane_point(params, u, v):

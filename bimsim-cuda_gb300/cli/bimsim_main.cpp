@@ -292,9 +292,14 @@ int main(int argc, char** argv) {
 
     // lMaterials (arguments.h:134-191)
     std::vector<Material> mats;
-    if (args("material-file"))
-        return fail("BIMSim Error: --material-file (dispersion tables, Kramers-Kronig) is not part of this build");
-    {
+    if (args("material-file")) {
+        // one material per file, evaluated at lambda (rts::material<float>(file).getN, nearfield.cpp:119-124)
+        for (int i = 0; i < args.nargs("material-file"); i++) {
+            double l = lambda, n[2];
+            if (check(bs_material_eval(args.text("material-file", i).c_str(), &l, 1, n))) return 1;
+            mats.push_back({(float)n[0], (float)n[1]});
+        }
+    } else {
         int nm = args.nargs("materials");
         if (nm == 1) {
             mats.push_back({args.f("materials"), 0});

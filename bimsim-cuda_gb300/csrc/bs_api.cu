@@ -7,6 +7,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <fstream>
 #include <memory>
 #include <string>
 #include <type_traits>
@@ -1111,6 +1112,23 @@ bs_status bs_get_far_field(bs_ctx* c, bs_field_kind kind, double* host, size_t c
         return fail(BS_ERR_ARG, "bs_get_far_field: need %zu complex values", (size_t)c->crop * c->crop);
     const int which = kind == BS_FIELD_TOTAL ? 0 : 1;
     return c->prec == BS_PREC_FP64 ? far_field<double>(c, which, host) : far_field<float>(c, which, host);
+}
+
+bs_status bs_material_eval(const char* path, const double* lambdas, int32_t n, double* out) {
+    if (!path || n < 0 || (n > 0 && (!lambdas || !out))) return fail(BS_ERR_ARG, "bs_material_eval: bad arguments");
+    std::ifstream f(path);
+    if (!f) return fail(BS_ERR_IO, "Material Error -- file not found: %s", path);
+    std::string text((std::istreambuf_iterator<char>(f)), std::istreambuf_iterator<char>());
+    std::vector<float> lam, re, im;
+    std::string err;
+    if (!material_load(text, lam, re, im, err)) return fail(BS_ERR_IO, "%s: %s", path, err.c_str());
+    for (int32_t i = 0; i < n; i++) {
+        float r, k;
+        material_eval(lam, re, im, (float)lambdas[i], r, k);
+        out[2 * i] = r;
+        out[2 * i + 1] = k;
+    }
+    return BS_OK;
 }
 
 bs_status bs_plane_point(const bs_params* params, double u, double v, double* xyz) {

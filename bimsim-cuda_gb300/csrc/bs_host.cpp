@@ -377,3 +377,120 @@ int envi_add_band(const char* path, const float* band, int samples, int lines, d
 }
 
 }  // namespace bs
+
+// ---------------------------------------------------------------------------
+// Material files (rts/optics/material.h:57-160, 434-540; rts/math/function.h).
+// Single precision throughout, as the reference's material<ptype = float>.
+// ---------------------------------------------------------------------------
+namespace bs {
+
+namespace {
+
+enum MatField { MF_MICRONS, MF_WAVENUMBER, MF_N, MF_K, MF_A, MF_IGNORE };
+
+struct MatPoint {
+    float lambda;
+    float n_re, n_im;
+};
+
+// "microns,n,k"-style column list (entryType, material.h:62-95)
+std::vector<MatField> parse_format(std::string f) {
+    std::vector<MatField> out;
+    for (;;) {
+        size_t e = f.find(',');
+        std::string t = f.substr(0, e);
+        out.push_back(t == "microns" ? MF_MICRONS
+                      : t == "wavenumber" ? MF_WAVENUMBER
+                      : t == "n" ? MF_N
+                      : t == "k" ? MF_K
+                      : t == "A" ? MF_A
+                      : MF_IGNORE);
+        if (e == std::string::npos) break;
+        f = f.substr(e + 1);
+    }
+    return out;
+}
+
+}  // namespace
+
+bool material_load(const std::string& text, std::vector<float>& lam, std::vector<float>& re, std::vector<float>& im,
+                   std::string& err) {
+    std::stringstream ss(text);
+    std::string line, format = "microns,n,k";
+    // an optional first comment line names the columns: "# ... [wavenumber,n,k]" (material.h:490-510)
+    if (ss.peek() == '#') {
+        std::getline(ss, line);
+        size_t a = line.find('['), b = line.find(']');
+        if (a != std::string::npos && b != std::string::npos) format = line.substr(a + 1, b - a - 1);
+    }
+    const std::vector<MatField> cols = parse_format(format);
+    std::vector<MatPoint> pts;
+    int lineno = 0;
+    while (std::getline(ss, line)) {
+        lineno++;
+        if (!line.empty() && line[0] == '#') continue;
+        if (line.find_first_not_of(" \t\r") == std::string::npos) continue;  // the reference loops forever here
+        // inputEntry (material.h:105-160): before each value skip every character
+        // that is not a digit (so signs are dropped: "-0.5" reads 0.5), then read a float
+        MatPoint p{0.f, 0.f, 0.f};
+        size_t pos = 0;
+        for (MatField c : cols) {
+            while (pos < line.size() && (line[pos] < '0' || line[pos] > '9')) pos++;
+            if (pos >= line.size()) {
+                err = "material line " + std::to_string(lineno) + " has fewer values than the format [" + format +
+                      "]";
+                return false;
+            }
+            size_t used = 0;
+            float v = std::stof(line.substr(pos), &used);
+            pos += used;
+            switch (c) {
+                case MF_MICRONS: p.lambda = v; break;
+                case MF_WAVENUMBER: p.lambda = 10000.0f / v; break;
+                case MF_N: p.n_re = v; break;
+                case MF_K: p.n_im = v; break;
+                case MF_A: p.n_im = (v * p.lambda) / (4 * (float)PI_REF); break;  // _A(), material.h:37-40
+                default: break;
+            }
+        }
+        // function::insert: before the first point with a larger wavelength (function.h:80-98)
+        auto it = std::upper_bound(pts.begin(), pts.end(), p,
+                                   [](const MatPoint& a, const MatPoint& b) { return a.lambda < b.lambda; });
+        pts.insert(it, p);
+    }
+    if (pts.empty()) {
+        err = "material file has no entries";
+        return false;
+    }
+    lam.clear();
+    re.clear();
+    im.clear();
+    for (auto& q : pts) {
+        lam.push_back(q.lambda);
+        re.push_back(q.n_re);
+        im.push_back(q.n_im);
+    }
+    return true;
+}
+
+// material::getN = function::linear(lambda) + n0 with n0 = 0 for files
+// (material.h:617-621, function.h:44-75): the first point with a larger
+// wavelength bounds the interval, ends clamp, and the weights are swapped as in
+// the reference: value = y_lo * a + y_hi * (1 - a), a = (l - l_lo) / (l_hi - l_lo).
+void material_eval(const std::vector<float>& lam, const std::vector<float>& re, const std::vector<float>& im,
+                   float l, float& n_re, float& n_im) {
+    size_t i = std::upper_bound(lam.begin(), lam.end(), l) - lam.begin();
+    if (i == lam.size()) {
+        n_re = re.back();
+        n_im = im.back();
+    } else if (i == 0) {
+        n_re = re.front();
+        n_im = im.front();
+    } else {
+        const float a = (l - lam[i - 1]) / (lam[i] - lam[i - 1]);
+        n_re = re[i - 1] * a + re[i] * (1.0f - a);
+        n_im = im[i - 1] * a + im[i] * (1.0f - a);
+    }
+}
+
+}  // namespace bs

@@ -4,6 +4,9 @@
 #include <stddef.h>
 #include <stdint.h>
 
+#include <string>
+#include <vector>
+
 namespace bs {
 
 // dataTypes.h:17 defines PI = 3.14159f; the kernels and sphere.cpp /
@@ -56,6 +59,12 @@ struct Sphere {
 };
 
 // Host helpers (bs_host.cpp).
+// Material files: parse (sorted by wavelength) and evaluate n + ik at lambda (um).
+bool material_load(const std::string& text, std::vector<float>& lam, std::vector<float>& re, std::vector<float>& im,
+                   std::string& err);
+void material_eval(const std::vector<float>& lam, const std::vector<float>& re, const std::vector<float>& im,
+                   float l, float& n_re, float& n_im);
+
 struct V3 {
     double x, y, z;
 };

@@ -218,6 +218,15 @@ bs_status bs_measure_fma_peak(double* fp32_tflops, double* fp64_tflops);
  * and amplitude are kept; bs_get_stats sums the per-source timings. */
 bs_status bs_simulate_sources(bs_ctx* ctx, const double* sources, int32_t n, bs_precision prec);
 
+/* Refractive index n + ik at each wavelength (um) from a material file
+ * (rts::material<float>(filename).getN(lambda), material.h:434-621): rows of
+ * "lambda n k" (default) or the columns named by a first comment line
+ * "# ... [wavenumber,n,k]" (also microns, A = absorbance); rows sorted by
+ * wavelength; linear interpolation between rows with the reference's swapped
+ * weights (rts/math/function.h:44-75), clamped at the ends; single precision.
+ * Blank lines are skipped (the reference's parser never returns on one). */
+bs_status bs_material_eval(const char* path, const double* lambdas, int32_t n, double* n_out);
+
 /* Point pos(u, v) = A + u X + v Y of the detector plane quad (microscopeStruct::pos;
  * the quad of arguments.h:340-407 built by rts/math/quad.h:55-84), e.g. for
  * placing point sources at image pixels (u = x / width, v = y / height). */

@@ -149,6 +149,17 @@ int ref_quad_dist(const float* pmin, const float* pmax, const float* nrm, float 
     return 0;
 }
 
+// rts::material<ptype>(filename).getN(lambda) (material.h:470-480, 617-621)
+int ref_material_eval(const char* path, int n, const double* lambdas, double* out) {
+    rts::material<ptype> m{std::string(path)};
+    for (int i = 0; i < n; i++) {
+        rts::complex<ptype> c = m.getN((ptype)lambdas[i]);
+        out[2 * i] = c.real();
+        out[2 * i + 1] = c.imag();
+    }
+    return 0;
+}
+
 // scalarslice::toEnvi's file handling (scalarslice.cu:146-166)
 int ref_envi_add_band(const char* path, const float* band, int samples, int lines, double wavelength, int append) {
     EnviFile f(path, append ? "a" : "w");

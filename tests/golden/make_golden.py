@@ -149,6 +149,26 @@ def main():
         env["dat_2"] = open(path, "rb").read().hex()
     out["envi"] = env
 
+    # material files (rts/optics/material.h, rts/math/function.h): parsing, sorting, the swapped
+    # interpolation weights, end clamping, wavenumber and absorbance columns, dropped signs
+    cases = {
+        "microns_unsorted": "4.0 1.50 0.02\n2.0 1.40 0.00\n3.0 1.45 0.10\n6.0 1.30 0.05\n",
+        "header_wavenumber": "# measured [wavenumber,n,k]\n2500 1.41 0.01\n2000 1.43 0.03\n1000 1.38 0.2\n",
+        "absorbance": "#[microns,n,A]\n2.5 1.42 0.3\n5.0 1.44 0.9\n10.0 1.40 0.1\n",
+        "comments_signs": "# plain file\n3.0 1.4 -0.05\n# a comment row\n5.0 1.6 0.07\n4.0 1.5 .5\n",
+        "duplicates": "3.0 1.4 0.01\n3.0 1.6 0.03\n5.0 1.5 0.02\n",
+    }
+    lams = np.array([1.0, 2.0, 2.5, 3.0, 3.25, 3.5, 4.0, 4.75, 5.0, 5.5, 7.0, 12.0], dtype=np.float64)
+    mats = {}
+    with tempfile.TemporaryDirectory() as td:
+        for name, text in cases.items():
+            path = os.path.join(td, name + ".txt")
+            open(path, "w").write(text)
+            res = np.zeros(2 * lams.size)
+            r.ref_material_eval(path.encode(), lams.size, P(lams), P(res))
+            mats[name] = {"text": text, "lambda": lams.tolist(), "n": res.tolist()}
+    out["material"] = mats
+
     for key, val in out.items():
         with open(os.path.join(HERE, key + ".json"), "w") as fh:
             json.dump(val, fh, separators=(",", ":"))

@@ -130,6 +130,21 @@ def test_cli_end_to_end_envi(tmp_path):
     assert np.fromfile(out, dtype=np.float32).size == 2 * 256
 
 
+def test_material_files_give_sphere_indices(tmp_path):
+    m1 = tmp_path / "m1.txt"
+    m1.write_text("2.0 1.40 0.00\n4.0 1.50 0.02\n")
+    m2 = tmp_path / "m2.txt"
+    m2.write_text("# [wavenumber,n,k]\n5000 1.30 0.1\n2000 1.60 0.3\n")
+    d = dry("--material-file", m1, m2, "--lambda", 2.5, "--spheres", 0, 0, 0, 1, 0, 3, 0, 0, 1, 1)
+    s0, s1 = d["spheres"]
+    # lambda 2.5 lies a quarter into [2, 4]: the reference weights give 1.40 * 0.25 + 1.50 * 0.75
+    assert s0[4] == pytest.approx(1.475, rel=1e-6) and s0[5] == pytest.approx(0.015, rel=1e-5)
+    n = lib.material_eval(m2, [np.float32(2.5)])[0]
+    assert s1[4] == pytest.approx(n.real, rel=1e-7) and s1[5] == pytest.approx(n.imag, rel=1e-6)
+    r = run("--material-file", tmp_path / "missing.txt", "--dry-run", check=False)
+    assert r.returncode == 1 and "not found" in r.stdout
+
+
 # ---------------------------------------------------------------------------
 # source images (--extended-source) and image outputs
 # ---------------------------------------------------------------------------
