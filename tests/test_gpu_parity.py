@@ -252,3 +252,22 @@ def test_compat_sampler_matches_reference_rule():
     arr, ns = abi.sphere_array(s)
     _, _, Do, _ = oracle_lib.simulate(p, arr, ns, w.reshape(-1, 3))
     assert rel(D, Do) <= TOL64
+
+
+def test_config1_full_size_fp64_matches_oracle():
+    """Config 1 at its full size (256^2 over 20 um, padding 2: near field 1280^2, 400 waves, direct order
+    sums, one sphere a = 5 um with ka = 12.57): FP64 GPU path vs the oracle on all host cores."""
+    p, s, w = scenes.config1()
+    arr, ns = abi.sphere_array(s)
+    U, Uf, D, Di = oracle_lib.simulate(p, arr, ns, w)
+    with Context(p) as ctx:
+        ctx.set_spheres(s)
+        ctx.set_waves(w)
+        ctx.simulate(BS_PREC_FP64)
+        errs = {"U": rel(ctx.field(BS_FIELD_TOTAL), U), "Uf": rel(ctx.field(BS_FIELD_INCIDENT), Uf),
+                "D": rel(ctx.image(BS_IMG_INTENSITY, f64=True), D),
+                "Di": rel(ctx.image(BS_IMG_INCIDENT, f64=True), Di)}
+        ctx.simulate(BS_PREC_MIXED)
+        mixed = {"D": rel(ctx.image(BS_IMG_INTENSITY, f64=True), D)}
+    assert max(errs.values()) <= TOL64, errs
+    assert mixed["D"] <= TOL_MIXED_IMG, mixed
