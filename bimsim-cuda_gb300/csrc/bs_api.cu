@@ -167,6 +167,7 @@ struct bs_ctx {
     DevBuf d_sph, d_waves, d_kw4, d_ph, d_A, d_B, d_mie, d_tab, d_tabscr, d_legP, d_lut, d_uft, d_uftscr;
     DevBuf d_cones, d_cnt;  // per-chunk wave cones; staged / total counters of the mixed LUT kernel
     DevBuf d_far;           // far fields Ud, Ufd on request (bs_get_far_field)
+    DevBuf d_starts;        // row / coefficient offsets of a coefficient batch
     int det_Nv = 0;         // passband rows of the last detector run (0: no far field)
     DevBuf d_fields;  // [2][R*R] U then Uf
     DevBuf d_su, d_sv, d_mask, d_wx, d_wy, d_wix, d_wiy, d_f1, d_f2, d_g1, d_I, d_D, d_img;
@@ -188,7 +189,8 @@ static std::vector<DevBuf*> ctx_bufs(bs_ctx* c) {
     return {&c->d_sph, &c->d_waves, &c->d_kw4, &c->d_ph, &c->d_A, &c->d_B, &c->d_mie, &c->d_tab,
             &c->d_tabscr, &c->d_legP, &c->d_lut, &c->d_uft, &c->d_uftscr, &c->d_fields, &c->d_su,
             &c->d_sv, &c->d_mask, &c->d_wx, &c->d_wy, &c->d_wix, &c->d_wiy, &c->d_f1, &c->d_f2,
-            &c->d_g1, &c->d_I, &c->d_D, &c->d_img, &c->d_cones, &c->d_cnt, &c->d_far};
+            &c->d_g1, &c->d_I, &c->d_D, &c->d_img, &c->d_cones, &c->d_cnt, &c->d_far,
+            &c->d_starts};
 }
 
 static void release_all(bs_ctx* c) {
@@ -508,6 +510,45 @@ static bs_status plan_tables(std::vector<Sphere>& hs, bool mixed, size_t budget,
     return BS_OK;
 }
 
+// Spheres whose coefficient rows are computed in one launch: consecutive
+// spheres of a table chunk, at most COEF_BATCH_ROWS rows together (a single
+// larger sphere forms its own batch).  starts: first global row of each sphere
+// and the total, then the first coefficient of each sphere.
+constexpr long long COEF_BATCH_ROWS = 1 << 19;
+
+struct CoefBatch {
+    int b0, b1;
+    long long rows, coefs;
+    std::vector<long long> starts;
+};
+
+static std::vector<CoefBatch> coef_batches(const std::vector<Sphere>& hs, const std::vector<int>& chunk_start) {
+    std::vector<CoefBatch> out;
+    for (size_t ci = 0; ci + 1 < chunk_start.size(); ci++) {
+        int b0 = chunk_start[ci];
+        const int s1 = chunk_start[ci + 1];
+        while (b0 < s1) {
+            CoefBatch b{b0, b0, 0, 0, {}};
+            std::vector<long long> cs;
+            while (b.b1 < s1) {
+                const Sphere& S = hs[b.b1];
+                const long long r = S.dR + S.aR;
+                if (b.b1 > b0 && b.rows + r > COEF_BATCH_ROWS) break;
+                b.starts.push_back(b.rows);
+                cs.push_back(b.coefs);
+                b.rows += r;
+                b.coefs += r * (S.Nl + 1);
+                b.b1++;
+            }
+            b.starts.push_back(b.rows);
+            b.starts.insert(b.starts.end(), cs.begin(), cs.end());
+            out.push_back(std::move(b));
+            b0 = out.back().b1;
+        }
+    }
+    return out;
+}
+
 static bs_status plan_luts(bs_ctx* c, bool mixed, std::vector<int>& chunk_start, size_t& pool, size_t& maxrows,
                            size_t& maxL) {
     size_t budget = c->budget;
@@ -720,10 +761,12 @@ static bs_status run_nearfield(bs_ctx* c) {
 
     // ---- LUT placement (before the sphere table goes to the device) ----
     std::vector<int> chunk_start;
+    std::vector<CoefBatch> batches;
     size_t pool = 0, maxrows = 0, maxL = 0;
     if (p.scalar && p.lut_us && ns > 0) {
         bs_status pst = plan_luts(c, !fp64, chunk_start, pool, maxrows, maxL);
         if (pst != BS_OK) return pst;
+        batches = coef_batches(c->hs, chunk_start);
     }
 
     // ---- Mie coefficients ----
@@ -767,8 +810,14 @@ static bs_status run_nearfield(bs_ctx* c) {
         int thetaR = ns > 0 ? c->hs[0].thetaR : 1000;
         if (ns > 0) {
             CK(c->d_lut.ensure(pool));
-            CK(c->d_tab.ensure(maxrows * maxL * sizeof(zd)));
-            CK(c->d_tabscr.ensure(maxrows * 2 * maxL * sizeof(double)));
+            long long maxcoef = 0, maxstarts = 0;
+            for (const CoefBatch& b : batches) {
+                maxcoef = std::max(maxcoef, b.coefs);
+                maxstarts = std::max(maxstarts, (long long)b.starts.size());
+            }
+            CK(c->d_tab.ensure((size_t)maxcoef * sizeof(zd)));
+            CK(c->d_tabscr.ensure((size_t)maxcoef * 2 * sizeof(double)));
+            CK(c->d_starts.ensure((size_t)maxstarts * sizeof(long long)));
             if (c->legP_theta != thetaR || c->legP_L < c->Lmax) {
                 CK(c->d_legP.ensure((size_t)thetaR * c->Lmax * sizeof(double)));
                 launch_legendre_table(thetaR, c->Lmax, c->d_legP.as<double>(), c->st);
@@ -796,6 +845,16 @@ static bs_status run_nearfield(bs_ctx* c) {
         c->lut_valid = false;  // set again below once this run's tables are complete
         c->stats.lut_tables_built = reuse_now ? 0 : ns;
         if (!fp64 && ns > 0) {
+            // the texture planes are gather-capable 2D CUDA arrays (thetaR wide, rows + 1 high)
+            int maxw = 0, maxh = 0;
+            CK(cudaDeviceGetAttribute(&maxw, cudaDevAttrMaxTexture2DGatherWidth, c->device));
+            CK(cudaDeviceGetAttribute(&maxh, cudaDevAttrMaxTexture2DGatherHeight, c->device));
+            for (const Sphere& S : c->hs)
+                if (S.thetaR > maxw || std::max(S.dR, S.aR) + 1 > maxh)
+                    return fail(BS_ERR_UNSUPPORTED,
+                                "mixed precision: a %d x %d lookup table exceeds the %d x %d texture limit of this GPU "
+                                "(use BS_PREC_FP64 or fewer table samples)",
+                                std::max(S.dR, S.aR), S.thetaR, maxh - 1, maxw);
             if ((int)c->slots.size() < max_chunk) c->slots.resize(max_chunk);
             CK(c->d_texobj.ensure((size_t)4 * max_chunk * sizeof(unsigned long long)));
             std::vector<float4> cones = wave_cones(w);
@@ -812,41 +871,44 @@ static bs_status run_nearfield(bs_ctx* c) {
         for (int ci = 0; ci < std::max(1, nchunks); ci++) {
             int s0 = ns > 0 ? chunk_start[ci] : 0, s1 = ns > 0 ? chunk_start[ci + 1] : 0;
             std::vector<unsigned long long> handles;
-            for (int i = s0; i < s1; i++) {
-                const Sphere& S = c->hs[i];
-                const int L = S.Nl + 1;
-                if (reuse_now) {
-                    if (!fp64)
-                        for (int k = 0; k < 4; k++) handles.push_back(c->slots[i - s0].tex[k]);
-                    continue;
-                }
-                launch_coef_rows(S, sc.kmag, c->d_A.as<zd>(), c->d_B.as<zd>(), c->d_tab.as<zd>(),
-                                 c->d_tabscr.as<double>(), c->st);
+            for (const CoefBatch& b : batches) {
+                if (reuse_now || b.b0 < s0 || b.b1 > s1) continue;
+                CK(cudaMemcpyAsync(c->d_starts.p, b.starts.data(), b.starts.size() * sizeof(long long),
+                                   cudaMemcpyHostToDevice, c->st));
+                launch_coef_rows_batch(c->d_sph.as<Sphere>(), b.b0, b.b1 - b.b0, c->d_starts.as<long long>(), b.rows,
+                                       sc.kmag, c->d_A.as<zd>(), c->d_B.as<zd>(), c->d_tab.as<zd>(),
+                                       c->d_tabscr.as<double>(), c->st);
                 LAUNCHED(c);
-                if (fp64) {
-                    Patch<double>* lut = c->d_lut.as<Patch<double>>();
-                    launch_lut_build<double>(c->d_tab.as<zd>(), S.dR, L, c->d_legP.as<double>(), c->legP_L, S.thetaR,
-                                             lut + S.usp_off, c->st);
-                    LAUNCHED(c);
-                    launch_lut_build<double>(c->d_tab.as<zd>() + (size_t)S.dR * L, S.aR, L, c->d_legP.as<double>(),
-                                             c->legP_L, S.thetaR, lut + S.uip_off, c->st);
-                    LAUNCHED(c);
-                } else {
-                    TexSlot& sl = c->slots[i - s0];
-                    // one spare row repeats the last, so a gather at the last row clamps as the texture would
-                    const int rows[4] = {S.dR, S.dR, S.aR, S.aR};
-                    for (int k = 0; k < 4; k++) CK(sl.ensure(k, S.thetaR, rows[k] + 1));
-                    float2* lin = c->d_lut.as<float2>();
-                    launch_lut_build_tex(c->d_tab.as<zd>(), S.dR + 1, L, c->d_legP.as<double>(), c->legP_L, S.thetaR,
-                                         sl.surf[0], sl.surf[1], lin + S.usp_off, S.lin_stride, c->st);
-                    LAUNCHED(c);
-                    launch_lut_build_tex(c->d_tab.as<zd>() + (size_t)S.dR * L, S.aR + 1, L, c->d_legP.as<double>(),
-                                         c->legP_L, S.thetaR, sl.surf[2], sl.surf[3], lin + S.uip_off, S.lin_stride,
-                                         c->st);
-                    LAUNCHED(c);
-                    for (int k = 0; k < 4; k++) handles.push_back(sl.tex[k]);
+                for (int i = b.b0; i < b.b1; i++) {
+                    const Sphere& S = c->hs[i];
+                    const int L = S.Nl + 1;
+                    const zd* tab = c->d_tab.as<zd>() + b.starts[(size_t)(b.b1 - b.b0) + 1 + (i - b.b0)];
+                    if (fp64) {
+                        Patch<double>* lut = c->d_lut.as<Patch<double>>();
+                        launch_lut_build<double>(tab, S.dR, L, c->d_legP.as<double>(), c->legP_L, S.thetaR,
+                                                 lut + S.usp_off, c->st);
+                        LAUNCHED(c);
+                        launch_lut_build<double>(tab + (size_t)S.dR * L, S.aR, L, c->d_legP.as<double>(), c->legP_L,
+                                                 S.thetaR, lut + S.uip_off, c->st);
+                        LAUNCHED(c);
+                    } else {
+                        TexSlot& sl = c->slots[i - s0];
+                        // one spare row repeats the last, so a gather at the last row clamps as the texture would
+                        const int rows[4] = {S.dR, S.dR, S.aR, S.aR};
+                        for (int k = 0; k < 4; k++) CK(sl.ensure(k, S.thetaR, rows[k] + 1));
+                        float2* lin = c->d_lut.as<float2>();
+                        launch_lut_build_tex(tab, S.dR + 1, L, c->d_legP.as<double>(), c->legP_L, S.thetaR,
+                                             sl.surf[0], sl.surf[1], lin + S.usp_off, S.lin_stride, c->st);
+                        LAUNCHED(c);
+                        launch_lut_build_tex(tab + (size_t)S.dR * L, S.aR + 1, L, c->d_legP.as<double>(), c->legP_L,
+                                             S.thetaR, sl.surf[2], sl.surf[3], lin + S.uip_off, S.lin_stride, c->st);
+                        LAUNCHED(c);
+                    }
                 }
             }
+            if (!fp64)
+                for (int i = s0; i < s1; i++)
+                    for (int k = 0; k < 4; k++) handles.push_back(c->slots[i - s0].tex[k]);
             if (!fp64 && !handles.empty())
                 CK(cudaMemcpyAsync(c->d_texobj.p, handles.data(), handles.size() * sizeof(unsigned long long),
                                    cudaMemcpyHostToDevice, c->st));
@@ -907,7 +969,13 @@ static size_t estimate_bytes(bs_ctx* c, bool fp64, size_t lut_budget) {
         if (plan_tables(hs, !fp64, lut_budget ? lut_budget : SIZE_MAX / 4, cs, pool, maxrows, maxL) != BS_OK)
             return 0;
         const size_t thetaR = hs[0].thetaR;
-        b += B(pool) + B(maxrows * maxL * sizeof(zd)) + B(maxrows * 2 * maxL * sizeof(double));
+        long long maxcoef = 0, maxstarts = 0;
+        for (const CoefBatch& cb : coef_batches(hs, cs)) {
+            maxcoef = std::max(maxcoef, cb.coefs);
+            maxstarts = std::max(maxstarts, (long long)cb.starts.size());
+        }
+        b += B(pool) + B((size_t)maxcoef * sizeof(zd)) + B((size_t)maxcoef * 2 * sizeof(double)) +
+             B((size_t)maxstarts * sizeof(long long));
         b += B(thetaR * (size_t)c->Lmax * sizeof(double));    // Legendre table
         if (!fp64) {
             // slot k holds the k-th sphere of every chunk: the largest of those tables, plus a spare row each
@@ -1228,7 +1296,15 @@ bs_status bs_sweep(bs_ctx* c, const double* lambdas, int32_t nl, const double* n
         if (!(lambdas[l] > 0)) return fail(BS_ERR_ARG, "bs_sweep: wavelength %d is not positive", l + 1);
     const bs_params saved_p = c->prm;
     const std::vector<bs_sphere> saved_s = c->spheres;
+    const int saved_staging = c->lut_staging;
     const size_t npix = (size_t)c->prm.resolution * c->prm.resolution;
+    // Empirical tuning of the mixed LUT kernel: with the choice left to the model
+    // and at least 4 bands, band 0 runs the staged kernel and band 1 the
+    // texture-only one; the faster serves the rest.  Both give the same bits, so
+    // the images do not depend on the choice.
+    const bool tune = saved_staging == 0 && prec == BS_PREC_MIXED && nl >= 4 && c->prm.scalar && c->prm.lut_us &&
+                      ns > 0;
+    float ms_stage = 0, ms_tex = 0;
     bs_status st = BS_OK;
     for (int32_t l = 0; l < nl && st == BS_OK; l++) {
         c->prm.lambda = lambdas[l];
@@ -1236,13 +1312,17 @@ bs_status bs_sweep(bs_ctx* c, const double* lambdas, int32_t nl, const double* n
             c->spheres[i].n_re = n_table[2 * ((size_t)l * ns + i)];
             c->spheres[i].n_im = n_table[2 * ((size_t)l * ns + i) + 1];
         }
+        if (tune) c->lut_staging = l == 0 ? 1 : (l == 1 ? 2 : (ms_stage <= ms_tex ? 1 : 2));
         st = bs_simulate(c, prec);
+        if (tune && l == 0) ms_stage = c->stats.ms_us;
+        if (tune && l == 1) ms_tex = c->stats.ms_us;
         if (st == BS_OK && images) st = bs_get_image(c, kind, images + (size_t)l * npix, npix);
         if (st == BS_OK && envi_path)
             st = bs_write_envi(c, kind, envi_path, l > 0, band_as_nu ? 1e4 / lambdas[l] : lambdas[l]);
     }
     c->prm = saved_p;
     c->spheres = saved_s;
+    c->lut_staging = saved_staging;
     c->have = false;
     return st;
 }

@@ -36,7 +36,10 @@ template <class T>
 void launch_uf(const Scene& sc, const double* tab, cpx<T>* Uf, cudaStream_t st);
 void launch_uf_table(const Scene& sc, double* tab, double* scratch, cudaStream_t st);
 void launch_mie(const Sphere* sph, int ns, double k, zd* scratch, int lstride, zd* A, zd* B, cudaStream_t st);
-void launch_coef_rows(const Sphere& S, double k, const zd* A, const zd* B, zd* tab, double* scratch, cudaStream_t st);
+// spheres [s0, s0 + n) in one launch; starts (device): first global row of each
+// sphere (n + 1 values, the last = total_rows) then first coefficient (n values)
+void launch_coef_rows_batch(const Sphere* sph, int s0, int n, const long long* starts, long long total_rows,
+                            double k, const zd* A, const zd* B, zd* tab, double* scratch, cudaStream_t st);
 void launch_legendre_table(int thetaR, int Lmax, double* P, cudaStream_t st);
 template <class T>
 void launch_lut_build(const zd* tab, int rows, int L, const double* P, int Pstride, int thetaR, Patch<T>* out,

@@ -191,17 +191,31 @@ __global__ void mie_kernel(const Sphere* __restrict__ sph, int ns, double k, zd*
     }
 }
 
-// Per-row order coefficients of one sphere:
+// Per-row order coefficients of the spheres [s0, s0 + n) in one launch:
 //   rows [0, dR):  C_l(r) = B_l (j_l + i y_l)(k r),  r in [r0, dmax]  (sphere.cpp:154-203)
 //   rows [dR, dR+aR): D_l(r) = A_l j_l(k n r),       r in [0, a]      (sphere.cpp:99-152)
-__global__ void coef_rows_kernel(Sphere S, double k, const zd* __restrict__ A, const zd* __restrict__ B,
-                                 zd* __restrict__ tab, double* __restrict__ scratch) {
-    int row = blockIdx.x * blockDim.x + threadIdx.x;
-    int rows = S.dR + S.aR;
-    if (row >= rows) return;
-    int L = S.Nl + 1;
-    zd* out = tab + (size_t)row * L;
-    double* sj = scratch + (size_t)row * 2 * L;
+// Thread g takes global row g; starts[i] / starts[n + 1 + i] are sphere i's
+// first global row and its first coefficient in tab (rows of Nl + 1
+// coefficients; starts[n], the total row count, bounds the grid).  The scratch
+// holds 2 (Nl + 1) doubles per row.
+__global__ void coef_rows_batch_kernel(const Sphere* __restrict__ sph, int s0, int n,
+                                       const long long* __restrict__ starts, double k, const zd* __restrict__ A,
+                                       const zd* __restrict__ B, zd* __restrict__ tab,
+                                       double* __restrict__ scratch) {
+    const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= starts[n]) return;
+    int lo = 0, hi = n - 1;  // last sphere whose first row is <= g
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (starts[mid] <= g) lo = mid;
+        else hi = mid - 1;
+    }
+    const Sphere& S = sph[s0 + lo];
+    const int row = (int)(g - starts[lo]);
+    const int L = S.Nl + 1;
+    const long long c0 = starts[n + 1 + lo] + (long long)row * L;
+    zd* out = tab + c0;
+    double* sj = scratch + 2 * c0;
     if (row < S.dR) {
         double dr = (S.dmax - S.r0) / (S.dR - 1);
         double r = row * dr + S.r0;
@@ -865,9 +879,10 @@ void launch_mie(const Sphere* sph, int ns, double k, zd* scratch, int lstride, z
     mie_kernel<<<blocks_for(ns, 64), 64, 0, st>>>(sph, ns, k, scratch, lstride, A, B);
 }
 
-void launch_coef_rows(const Sphere& S, double k, const zd* A, const zd* B, zd* tab, double* scratch,
-                      cudaStream_t st) {
-    coef_rows_kernel<<<blocks_for(S.dR + S.aR, 64), 64, 0, st>>>(S, k, A, B, tab, scratch);
+void launch_coef_rows_batch(const Sphere* sph, int s0, int n, const long long* starts, long long total_rows,
+                            double k, const zd* A, const zd* B, zd* tab, double* scratch, cudaStream_t st) {
+    coef_rows_batch_kernel<<<(unsigned)((total_rows + 127) / 128), 128, 0, st>>>(sph, s0, n, starts, k, A, B, tab,
+                                                                               scratch);
 }
 
 void launch_legendre_table(int thetaR, int Lmax, double* P, cudaStream_t st) {

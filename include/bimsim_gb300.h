@@ -240,7 +240,9 @@ bs_status bs_plane_point(const bs_params* params, double u, double v, double* xy
  * may be NULL) and, when envi_path is given, to band l of that ENVI file
  * (band value lambda, or 1e4/lambda when band_as_nu).  The context's own
  * wavelength and indices are restored afterwards; results of the last
- * band are dropped. */
+ * band are dropped.  With bs_set_lut_staging left at 0 and at least 4 mixed
+ * bands, bands 0 and 1 time the staged and texture-only LUT kernels and the
+ * faster runs the rest (identical bits either way). */
 bs_status bs_sweep(bs_ctx* ctx, const double* lambdas, int32_t nl, const double* n_table, bs_precision prec,
                    bs_image_kind kind, float* images, const char* envi_path, int32_t band_as_nu);
 

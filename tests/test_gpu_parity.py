@@ -73,11 +73,17 @@ def scene(name):
                             us_lut_r=100, us_lut_theta=300)
         s = [(-6.0, 5.0, 0.0, 2.0, 1.4, 0.04), (9.0, -8.0, 1.0, 1.4, 1.5, 0.01)]
         return p, s, w(256, 0, 0.5, seed=10)
+    if name == "lut_many_rows":
+        # 20 spheres x 30 000 table rows: their coefficient rows are computed in two batches (2^19 rows each)
+        p = abi.make_params(lam=3.0, condenser=(0, 0.5), objective=(0, 0.5), xy=(16, 0), resolution=16, padding=1,
+                            us_lut_r=30000, us_lut_theta=16)
+        s = scenes.random_spheres(20, 16.0, 0.3, 0.9, seed=12)
+        return p, s, w(24, 0, 0.5, seed=11)
     raise KeyError(name)
 
 
 ALL = ["lut", "lut_ufLUT", "direct_cfg1", "direct_multi", "plane_wave", "oblique_xz", "vector", "no_spheres",
-       "supersample", "lut_staged"]
+       "supersample", "lut_staged", "lut_many_rows"]
 _oracle_cache = {}
 
 
@@ -157,6 +163,18 @@ def test_kernel_choice_model_tracks_the_staged_fraction():
     assert abs(st.lut_staged_predicted - measured) < 0.2, (st.lut_staged_predicted, measured)
     auto = run_gpu("lut_staged", BS_PREC_MIXED)["stats"]
     assert (auto.lut_chunks_staged > 0) == (auto.lut_staged_predicted >= 0.25)
+
+
+def test_mixed_rejects_tables_beyond_the_texture_limit():
+    p = abi.make_params(lam=3.0, condenser=(0, 0.5), objective=(0, 0.5), xy=(16, 0), resolution=16, padding=1,
+                        us_lut_r=70000, us_lut_theta=16)
+    with Context(p) as ctx:
+        ctx.set_spheres([(0, 0, 0, 2.0, 1.4, 0.05)])
+        ctx.set_waves(scenes.mc_waves(8, 0, 0.5, seed=1))
+        with pytest.raises(Exception) as e:
+            ctx.simulate(BS_PREC_MIXED)
+        assert "texture limit" in str(e.value)
+        ctx.simulate(BS_PREC_FP64)  # the FP64 path keeps its tables in linear memory
 
 
 def test_images_are_derived_consistently():
