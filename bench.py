@@ -361,6 +361,10 @@ def run_workload(args):
                --sweep-bands wavelengths evenly spaced in 2.5-12.5 um through bs_sweep
       config1  the plain method: 256^2 over 20 um, padding 2, one sphere a = 5 um, 400 waves,
                direct order sums, FP64
+      config5  the large scene: 4096^2 over 400 um (near field 12288^2), 1000 spheres a ~ U(2, 20) in
+               a slab |z| < 60 um, lambda 2 um, 2000 waves, LUT mode, mixed precision (one slice is
+               about 11 minutes: run it with --warmup 0 --steps 1); --c5-resolution / --c5-samples
+               shrink it for a quick check, and the JSON line then says so
     Steps: --warmup untimed and --steps timed runs of the whole workload, L2 flushed between."""
     import numpy as np
     import torch
@@ -375,6 +379,14 @@ def run_workload(args):
         prec = BS_PREC_MIXED
         work = f"config3: 512^2 detector over 100 um (near field 1536^2), 50 spheres, 1000 waves, " \
                f"{len(lambdas)} of the 512 wavelengths in 2.5-12.5 um, LUT 4096x1024"
+    elif args.workload == "config5":
+        p, s, w = scenes.config5(resolution=args.c5_resolution, samples=args.c5_samples)
+        lambdas = table = None
+        prec = BS_PREC_MIXED
+        full = args.c5_resolution == 4096 and args.c5_samples == 2000
+        work = ("config5" if full else "REDUCED config5") + \
+            f": {args.c5_resolution}^2 over 400 um, 1000 spheres a~U(2,20) in |z|<60 um, lambda 2 um, " \
+            f"{args.c5_samples} waves, LUT 4096x1024, mixed"
     else:
         p, s, w = scenes.config1()
         lambdas = table = None
@@ -409,7 +421,10 @@ def run_workload(args):
     st = ctx.stats()
     per = statistics.median(times)
     nb = len(lambdas) if lambdas is not None else 1
-    line = {"metric": "sweep bands/s" if lambdas is not None else "field-slice pixels/s (plain FP64 direct)",
+    metric = ("sweep bands/s" if lambdas is not None else
+              "field-slice pixels/s (plain FP64 direct)" if args.workload == "config1" else
+              "field-slice pixels/s (config 5, mixed)")
+    line = {"metric": metric,
             "value": nb / per if lambdas is not None else R * R / per,
             "unit": "bands/s" if lambdas is not None else "pixels/s",
             "field_slice_pixels_per_s": nb * R * R / per, "n_gpus": 1, "steps": args.steps,
@@ -437,7 +452,9 @@ def main():
     ap.add_argument("--serve-requests", type=int, default=32)
     ap.add_argument("--serve-rate", type=float, default=1.0)
     ap.add_argument("--serve-workers", type=int, default=4)
-    ap.add_argument("--workload", default="slice", choices=["slice", "sweep", "config1"])
+    ap.add_argument("--workload", default="slice", choices=["slice", "sweep", "config1", "config5"])
+    ap.add_argument("--c5-resolution", type=int, default=4096)
+    ap.add_argument("--c5-samples", type=int, default=2000)
     ap.add_argument("--sweep-bands", type=int, default=64)
     args = ap.parse_args()
     if args.impl == "reference":
