@@ -316,6 +316,13 @@ def run_gb300(args):
         case = "intensity and absorbance, same scene family at 256^2, 8 spheres, 200 waves"
     # ---- served latency (after the timed regions) ----
     served = None if args.no_serve or args.small or ws > 1 else run_served(args)
+    if served and fp64:
+        # the reference-style baseline, one plain FP64 slice after another, extrapolated from the FP64
+        # slice measured above by its (pixel, sphere, wave) lookups: far too long to run in full here
+        fp64_rate = lookups / (fp64["ms_per_slice"] * 1e-3)
+        served["fp64_sequential_estimate"] = {
+            "wall_s": served["lookups"] / fp64_rate, "requests_per_s": served["requests"] * fp64_rate / served["lookups"],
+            "basis": f"plain FP64 GPU path at {fp64_rate:.3g} lookups/s (config-2 slice above), no queueing"}
     # ---- CPU baseline (oracle on a bounded band of rows) ----
     cpu = None
     if not args.no_cpu and not args.small:
