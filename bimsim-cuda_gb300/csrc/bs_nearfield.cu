@@ -726,7 +726,10 @@ __global__ void __launch_bounds__(256) lut_build_tex_kernel(const zd* __restrict
 //   outside (d > a):  c_l = B_l (j_l + i y_l)(k d)   with the reference clamps
 //   inside  (d <= a): c_l = A_l j_l(k n d)           (c_0 = A_0 only when
 //                                                      Re(k n d) < 1e-6)
-// The per-wave work is then sum_l c_l P_l(k_w . r^).
+// The per-wave work is then sum_l c_l P_l(k_w . r^), with the Legendre
+// recurrence P_l = ((2l-1) x P_{l-1} - (l-1) P_{l-2}) / l written as
+// a_l x P_{l-1} - b_l P_{l-2} from a per-block table of a_l = (2l-1)/l and
+// b_l = (l-1)/l, which takes the division out of the inner loop.
 // ---------------------------------------------------------------------------
 template <class T>
 __global__ void __launch_bounds__(64) us_direct_kernel(Scene sc, const Sphere* __restrict__ sph, int lstride,
@@ -736,7 +739,14 @@ __global__ void __launch_bounds__(64) us_direct_kernel(Scene sc, const Sphere* _
                                                        cpx<T>* __restrict__ U) {
     extern __shared__ unsigned char smem_raw[];
     cpx<T>* cl = reinterpret_cast<cpx<T>*>(smem_raw);  // [lstride][blockDim.x]
+    T* la = reinterpret_cast<T*>(cl + (size_t)lstride * blockDim.x);  // [lstride] (2l-1)/l
+    T* lb = la + lstride;                                               // [lstride] (l-1)/l
     const int tid = threadIdx.x;
+    for (int l = tid; l < lstride; l += blockDim.x) {
+        la[l] = l ? (T)((2.0 * l - 1.0) / l) : (T)0;
+        lb[l] = l ? (T)((l - 1.0) / l) : (T)0;
+    }
+    __syncthreads();
     int idx = blockIdx.x * blockDim.x + tid;
     bool valid = idx < sc.R * sc.R;
     if (!valid) idx = sc.R * sc.R - 1;
@@ -816,7 +826,7 @@ __global__ void __launch_bounds__(64) us_direct_kernel(Scene sc, const Sphere* _
                 ur += c1.re * Pb;
                 ui += c1.im * Pb;
                 for (int l = 2; l < Leff; l++) {
-                    T Pn = ((2 * l - 1) * x * Pb - (l - 1) * Pa) / l;
+                    T Pn = la[l] * x * Pb - lb[l] * Pa;
                     Pa = Pb;
                     Pb = Pn;
                     cpx<T> cc = cl[l * blockDim.x + tid];
@@ -940,7 +950,7 @@ template <class T>
 void launch_us_direct(const Scene& sc, const Sphere* sph, int lstride, const zd* A, const zd* B,
                       const double* waves, const cpx<T>* ph, const cpx<T>* Uf, cpx<T>* U, cudaStream_t st) {
     const int bt = 64;
-    size_t smem = (size_t)lstride * bt * sizeof(cpx<T>);
+    size_t smem = (size_t)lstride * bt * sizeof(cpx<T>) + 2 * (size_t)lstride * sizeof(T);
     if (smem > 48 * 1024)
         cudaFuncSetAttribute(us_direct_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     long long n = (long long)sc.R * sc.R;

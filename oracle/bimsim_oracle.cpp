@@ -11,6 +11,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <chrono>
 #include <cmath>
 #include <complex>
 #include <cstdio>
@@ -1346,6 +1347,43 @@ int bso_nearfield_rows(const bs_params* p, const bs_sphere* s, int ns, const dou
     Scene sc;
     scene_init(sc, *p, s, ns, waves, nk);
     nearfield_rows(sc, row0, row1, nthreads, reinterpret_cast<cd*>(U), nullptr);
+    return 0;
+}
+
+// Timed band for CPU baselines: times[0] = scene set-up (Mie coefficients and
+// the Bessel/Hankel rows, serial per sphere as the reference builds them on the
+// host), times[1] = every LUT entry of every sphere (OpenMP over entries),
+// times[2] = the near field of rows [row0, row1) with the tables complete.  A
+// whole slice then costs times[0] + times[1] + times[2] * R / (row1 - row0).
+int bso_nearfield_rows_timed(const bs_params* p, const bs_sphere* s, int ns, const double* waves, int nk,
+                             int nthreads, int row0, int row1, double* U, double* times) {
+    auto now = [] { return std::chrono::steady_clock::now(); };
+    auto sec = [](std::chrono::steady_clock::time_point a, std::chrono::steady_clock::time_point b) {
+        return std::chrono::duration<double>(b - a).count();
+    };
+    auto t0 = now();
+    Scene sc;
+    scene_init(sc, *p, s, ns, waves, nk);
+    auto t1 = now();
+    for (SphereLut* L : sc.lut) {
+        const long long nu = (long long)L->sg.dR * L->sg.thetaR, ni = (long long)L->sg.aR * L->sg.thetaR;
+#ifdef _OPENMP
+        int nt = nthreads > 0 ? nthreads : omp_get_max_threads();
+#pragma omp parallel for schedule(dynamic, 256) num_threads(nt)
+#endif
+        for (long long e = 0; e < nu + ni; e++) {
+            if (e < nu)
+                L->Usp((int)(e / L->sg.thetaR), (int)(e % L->sg.thetaR));
+            else
+                L->Uip((int)((e - nu) / L->sg.thetaR), (int)((e - nu) % L->sg.thetaR));
+        }
+    }
+    auto t2 = now();
+    nearfield_rows(sc, row0, row1, nthreads, reinterpret_cast<cd*>(U), nullptr);
+    auto t3 = now();
+    times[0] = sec(t0, t1);
+    times[1] = sec(t1, t2);
+    times[2] = sec(t2, t3);
     return 0;
 }
 

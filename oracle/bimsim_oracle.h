@@ -85,6 +85,10 @@ int bso_nearfield_rows(const bs_params* p, const bs_sphere* s, int ns,
 
 /* Detector chain on given near fields (microscope.cu:608-662, 722-814). */
 int bso_detector(const bs_params* p, const double* U, const double* Uf, double* D, double* Di);
+/* The band of bso_nearfield_rows with its CPU time split into scene set-up,
+ * the complete LUTs and the band itself (times[3], seconds). */
+int bso_nearfield_rows_timed(const bs_params* p, const bs_sphere* s, int ns, const double* waves, int nk,
+                             int nthreads, int row0, int row1, double* U, double* times);
 /* Far field Ud (crop_res^2 complex, interleaved): band-passed U on the crop, scaled by 1/R^2. */
 int bso_far_field(const bs_params* p, const double* U, double* out);
 

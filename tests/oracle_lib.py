@@ -50,6 +50,7 @@ def load():
     lib.bso_uf_table.argtypes = [vp, vp, vp, vp]
     lib.bso_simulate.argtypes = [vp, vp, C.c_int, vp, C.c_int, C.c_int, vp, vp, vp, vp]
     lib.bso_nearfield_rows.argtypes = [vp, vp, C.c_int, vp, C.c_int, C.c_int, C.c_int, C.c_int, vp]
+    lib.bso_nearfield_rows_timed.argtypes = [vp, vp, C.c_int, vp, C.c_int, C.c_int, C.c_int, C.c_int, vp, vp]
     lib.bso_detector.argtypes = [vp, vp, vp, vp, vp]
     lib.bso_far_field.argtypes = [vp, vp, vp]
     lib.bso_fft.argtypes = [C.c_int, C.c_int, vp]
