@@ -354,7 +354,17 @@ def run_gb300(args):
                      "peak_source": "measured FP32 FMA loop on this GPU (bs_measure_fma_peak)",
                      "work": f"{FLOP_PER_LOOKUP} flop x {lookups} (pixel, sphere, wave) lookups per launch",
                      "launch_ms": us_s * 1e3, "lookups_per_s": lookups / us_s,
-                     "hbm_peak_gbs": peaks.get("hbm_gbs"), "fp64_peak_tflops": fp64_tf},
+                     "hbm_peak_gbs": peaks.get("hbm_gbs"), "fp64_peak_tflops": fp64_tf,
+                     "why_not_hbm_or_tensor": "no step is a dense contraction (no tensor-core use) and the kernel "
+                                              "reads 0.19 TB/s of DRAM: its bound is the FP32/L1 issue rate, so the "
+                                              "roofline is the measured FP32 FMA peak; the DRAM view is roofline_hbm"},
+        "roofline_hbm": (None if not (profile_traffic() and peaks.get("hbm_gbs")) else
+                         {"bound": "hbm", "kernel": "us_lut_tex_kernel", "unit": "GB/s",
+                          "achieved": profile_traffic() / us_s / 1e9, "peak": peaks["hbm_gbs"],
+                          "frac": profile_traffic() / us_s / 1e9 / peaks["hbm_gbs"],
+                          "traffic": profile_traffic(), "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)",
+                          "note": "DRAM bytes of one full launch (ncu, profiles/us_lut_tex_config2.md) over this "
+                                  "run's launch time"}),
         "mixed_vs_fp64_rel_l2": {"value": rel, "absorbance": rel_a, "tolerance": 1e-5, "case": case},
         "fp64_plain": fp64,
         "clocks": clocks,

@@ -97,3 +97,28 @@ def test_estimate_covers_what_a_context_allocates(i):
         ctx.image(kind)
         held = ctx.info().device_bytes
     assert held <= est <= held * 1.05 + 4096, (held, est)
+
+
+def test_a_failing_request_leaves_the_others_intact():
+    """A request the library rejects at run time (mixed-precision tables taller than the GPU's
+    gather-texture limit) fails alone: its fetch raises with the message, the rest complete."""
+    from bimsim_gb300 import BimsimError
+    good = [request(i) for i in range(3)]
+    ref = [alone(*r) for r in good]
+    bad_p = abi.make_params(lam=3.0, condenser=(0, 0.5), objective=(0, 0.5), xy=(16, 0), resolution=16, padding=1,
+                            us_lut_r=70000, us_lut_theta=16)
+    with Server(workers=2) as srv:
+        tickets = [srv.submit(p, s, waves=w, precision=prec, image=kind) for p, s, w, prec, kind in good[:2]]
+        bad = srv.submit(bad_p, [(0, 0, 0, 2.0, 1.4, 0.05)], waves=scenes.mc_waves(8, 0, 0.5, seed=1))
+        p, s, w, prec, kind = good[2]
+        tickets.append(srv.submit(p, s, waves=w, precision=prec, image=kind))
+        for t in tickets + [bad]:
+            srv.wait(t, 120.0)
+        with pytest.raises(BimsimError) as e:
+            srv.fetch(bad)
+        assert "texture limit" in str(e.value)
+        for t, r in zip(tickets, ref):
+            img, info = srv.fetch(t)
+            assert np.array_equal(img, r, equal_nan=True)
+        st = srv.stats()
+        assert st.completed == 3 and st.failed == 1
