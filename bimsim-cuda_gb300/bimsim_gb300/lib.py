@@ -54,6 +54,7 @@ def library():
         "bs_set_params": ([vp, vp], C.c_int),
         "bs_sweep": ([vp, vp, i32, vp, C.c_int, C.c_int, vp, C.c_char_p, i32], C.c_int),
         "bs_simulate_sources": ([vp, vp, i32, C.c_int], C.c_int),
+        "bs_simulate_ring_interp": ([vp, i32, i32, C.c_int], C.c_int),
         "bs_plane_point": ([vp, C.c_double, C.c_double, vp], C.c_int),
         "bs_get_far_field": ([vp, C.c_int, vp, sz], C.c_int),
         "bs_material_eval": ([C.c_char_p, vp, i32, vp], C.c_int),
@@ -202,6 +203,10 @@ class Context:
         """sources: (n, 4) rows of focus x, y, z and amplitude; detector images sum over them."""
         a = np.ascontiguousarray(sources, dtype=np.float64).reshape(-1, 4)
         self._check(self.lib.bs_simulate_sources(self.h, _p(a), len(a), precision))
+
+    def simulate_ring_interp(self, points, rings, precision=abi.BS_PREC_MIXED):
+        """The reference's --interpolate 3: ring sources by rotating each ring's first near field."""
+        self._check(self.lib.bs_simulate_ring_interp(self.h, points, rings, precision))
 
     def set_params(self, params):
         self._check(self.lib.bs_set_params(self.h, C.byref(params)))

@@ -453,9 +453,13 @@ int main(int argc, char** argv) {
                 sources.insert(sources.end(), {f[0], f[1], f[2], (double)((float)v / 255)});
             }
         if (verbose) std::cout << "Number of point sources: " << sources.size() / 4 << std::endl;
-    } else if (args.i("interpolate") != -1) {
-        return fail("BIMSim Error: point-source interpolation (--interpolate 0-3) is not part of this build");
     }
+    const int interp = sources.empty() ? args.i("interpolate") : -1;
+    if (interp != -1 && interp != 3)
+        return fail("BIMSim Error: --interpolate " + std::to_string(interp) +
+                    " is not part of this build (mode 3, ring sources by near-field rotation, is)");
+    // --points-rings: sources per ring, then rings (nf.extSource, arguments.h:471-474)
+    const int ring_points = args.i("points-rings", 0), ring_count = args.i("points-rings", 1);
 
     // spheres with their refractive index at lambda (material n + i k, rts/optics/material.h:434-446)
     std::vector<bs_sphere> spheres;
@@ -484,14 +488,14 @@ int main(int argc, char** argv) {
                     "\"padding\": %d, \"supersample\": %d, \"field_order\": %d, \"samples\": %d, \"scalar\": %d, "
                     "\"plane_wave\": %d, \"lut_uf\": %d, \"lut_us\": %d, \"us_lut\": [%d, %d], \"uf_lut\": %d, "
                     "\"precision\": \"%s\", \"wavenumber\": %d, \"append\": %d, \"point_sources\": %zu, "
-                    "\"spheres\": [",
+                    "\"interpolate\": %d, \"points_rings\": [%d, %d], \"spheres\": [",
                     p.lambda, p.amplitude, p.k_dir[0], p.k_dir[1], p.k_dir[2], p.focus[0], p.focus[1], p.focus[2],
                     p.condenser[0], p.condenser[1], p.objective[0], p.objective[1], p.plane_min[0], p.plane_min[1],
                     p.plane_min[2], p.plane_max[0], p.plane_max[1], p.plane_max[2], p.plane_normal[0],
                     p.plane_normal[1], p.plane_normal[2], p.resolution, p.padding, p.supersample, p.field_order, nk,
                     p.scalar, p.plane_wave, p.lut_uf, p.lut_us, p.us_lut_r, p.us_lut_theta, p.uf_lut_r,
                     precision == BS_PREC_FP64 ? "fp64" : "mixed", wavenumber ? 1 : 0, append ? 1 : 0,
-                    sources.size() / 4);
+                    sources.size() / 4, interp, ring_points, ring_count);
         for (size_t i = 0; i < spheres.size(); i++)
             std::printf("%s[%.9g, %.9g, %.9g, %.9g, %.9g, %.9g]", i ? ", " : "", spheres[i].x, spheres[i].y,
                         spheres[i].z, spheres[i].a, spheres[i].n_re, spheres[i].n_im);
@@ -518,7 +522,10 @@ int main(int argc, char** argv) {
             if (check(bs_sample_waves_compat(ctx, nk))) return 1;
         }
     }
-    if (sources.empty()) {
+    if (interp == 3) {
+        // SimulateExtendedSourceWithInterpolation + saveDetector (fileout.cu:218-224)
+        if (check(bs_simulate_ring_interp(ctx, ring_points, ring_count, precision))) return 1;
+    } else if (sources.empty()) {
         if (check(bs_simulate(ctx, precision))) return 1;
         // fileoutStruct::saveNearField / saveFarField (fileout.cu:3-45): field images of
         // the last source in the single-source path

@@ -168,6 +168,7 @@ struct bs_ctx {
     DevBuf d_cones, d_cnt;  // per-chunk wave cones; staged / total counters of the mixed LUT kernel
     DevBuf d_far;           // far fields Ud, Ufd on request (bs_get_far_field)
     DevBuf d_starts;        // row / coefficient offsets of a coefficient batch
+    DevBuf d_fsave;         // U, Uf of a ring's first source (bs_simulate_ring_interp)
     int det_Nv = 0;         // passband rows of the last detector run (0: no far field)
     DevBuf d_fields;  // [2][R*R] U then Uf
     DevBuf d_su, d_sv, d_mask, d_wx, d_wy, d_wix, d_wiy, d_f1, d_f2, d_g1, d_I, d_D, d_img;
@@ -190,7 +191,7 @@ static std::vector<DevBuf*> ctx_bufs(bs_ctx* c) {
             &c->d_tabscr, &c->d_legP, &c->d_lut, &c->d_uft, &c->d_uftscr, &c->d_fields, &c->d_su,
             &c->d_sv, &c->d_mask, &c->d_wx, &c->d_wy, &c->d_wix, &c->d_wiy, &c->d_f1, &c->d_f2,
             &c->d_g1, &c->d_I, &c->d_D, &c->d_img, &c->d_cones, &c->d_cnt, &c->d_far,
-            &c->d_starts};
+            &c->d_starts, &c->d_fsave};
 }
 
 static void release_all(bs_ctx* c) {
@@ -1196,6 +1197,90 @@ bs_status bs_material_eval(const char* path, const double* lambdas, int32_t n, d
         out[2 * i] = r;
         out[2 * i + 1] = k;
     }
+    return BS_OK;
+}
+
+}  // extern "C"
+
+// The detector images of the near field in d_fields rotated by each angle,
+// added to the detector (nearfieldStruct::Interpolate + SimulateImaging,
+// microscope.cu:834-846); d_fields itself is kept in d_fsave and overwritten.
+template <class T>
+static bs_status image_rotations(bs_ctx* c, const std::vector<float>& angles) {
+    const size_t n = 2 * (size_t)c->R * c->R;
+    CK(c->d_fsave.ensure(n * sizeof(cpx<T>)));
+    CK(cudaMemcpyAsync(c->d_fsave.p, c->d_fields.p, n * sizeof(cpx<T>), cudaMemcpyDeviceToDevice, c->st));
+    for (float a : angles) {
+        launch_rotate_fields<T>(c->R, (float)std::cos((double)a), (float)std::sin((double)a), c->d_fsave.as<cpx<T>>(),
+                                c->d_fields.as<cpx<T>>(), c->st);
+        LAUNCHED(c);
+        bs_status st = run_detector<T>(c, true);
+        if (st != BS_OK) return st;
+    }
+    CK(cudaStreamSynchronize(c->st));
+    CK(cudaGetLastError());
+    return BS_OK;
+}
+
+extern "C" {
+
+bs_status bs_simulate_ring_interp(bs_ctx* c, int32_t points, int32_t rings, bs_precision prec) {
+    if (!c || points < 1 || rings < 1) return fail(BS_ERR_ARG, "bs_simulate_ring_interp: points and rings must be >= 1");
+    if (prec != BS_PREC_FP64 && prec != BS_PREC_MIXED)
+        return fail(BS_ERR_ARG, "bs_simulate_ring_interp: unknown precision");
+    const bs_params saved = c->prm;
+    const bool saved_reuse = c->reuse;
+    c->reuse = true;  // the sphere tables do not depend on the focus or the amplitude
+    bs_stats sum{};
+    auto add = [&sum](const bs_stats& s) {
+        sum.ms_total += s.ms_total;
+        sum.ms_uf += s.ms_uf;
+        sum.ms_mie += s.ms_mie;
+        sum.ms_lut += s.ms_lut;
+        sum.ms_us += s.ms_us;
+        sum.ms_detector += s.ms_detector;
+        sum.kernel_launches += s.kernel_launches;
+        sum.us_interactions += s.us_interactions;
+        sum.lut_chunks_staged += s.lut_chunks_staged;
+        sum.lut_chunks_total += s.lut_chunks_total;
+        sum.lut_tables_built += s.lut_tables_built;
+    };
+    // the source at the context's own focus (SimulateExtendedSourceWithInterpolation, microscope.cu:1185-1253)
+    bs_status st = simulate_impl(c, prec, false);
+    if (st == BS_OK) add(c->stats);
+    // rings of radius 1, 2, ... um; point i at angle 2 pi (i + 1) / points, accumulated in float from
+    // 2 * PI / points (generatePointSources, microscope.cu:1298-1325), amplitude 1, z = 0; cosines
+    // and sines are taken in double and rounded to float (the reference used float cos and sin).  Only a ring's
+    // first point is simulated; point i's near field is that one rotated by point i's own angle.
+    const float step = 2 * (float)PI_REF / (float)points;
+    for (int ring = 1; ring < rings && st == BS_OK; ring++) {
+        const float radius = (float)ring;
+        std::vector<float> theta(points);
+        float th = step;
+        for (int i = 0; i < points; i++) {
+            theta[i] = th;
+            th += step;
+        }
+        c->prm.focus[0] = (float)std::cos((double)theta[0]) * radius;
+        c->prm.focus[1] = (float)std::sin((double)theta[0]) * radius;
+        c->prm.focus[2] = 0;
+        c->prm.amplitude = 1;
+        st = simulate_impl(c, prec, true);
+        if (st != BS_OK) break;
+        add(c->stats);
+        const std::vector<float> angles(theta.begin() + 1, theta.end());
+        if (!angles.empty())
+            st = prec == BS_PREC_FP64 ? image_rotations<double>(c, angles) : image_rotations<float>(c, angles);
+    }
+    c->prm = saved;
+    c->reuse = saved_reuse;
+    if (!saved_reuse) c->lut_valid = false;
+    if (st != BS_OK) {
+        c->have = false;
+        return st;
+    }
+    c->stats = sum;
+    c->have = true;
     return BS_OK;
 }
 

@@ -68,6 +68,10 @@ void launch_us_direct(const Scene& sc, const Sphere* sph, int lstride, const zd*
                       const cpx<T>* ph, const cpx<T>* Uf, cpx<T>* U, cudaStream_t st);
 template <class T>
 void launch_sum_only(const Scene& sc, const Sphere* sph, const cpx<T>* Uf, cpx<T>* U, cudaStream_t st);
+// U and Uf (src: U then Uf, R x R each) rotated about the slice centre into dst;
+// c, s: cosine and sine of the angle
+template <class T>
+void launch_rotate_fields(int R, float c, float s, const cpx<T>* src, cpx<T>* dst, cudaStream_t st);
 
 // ---- detector ----
 // twiddles: out[i * ld_i + j * ld_j] = exp(sign 2 pi i ((off_i + i) * freq[j] mod R) / R)

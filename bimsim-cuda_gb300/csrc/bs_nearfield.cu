@@ -963,7 +963,47 @@ void launch_sum_only(const Scene& sc, const Sphere* sph, const cpx<T>* Uf, cpx<T
     sum_only_kernel<T><<<blocks_for(n, 128), 128, 0, st>>>(sc, sph, Uf, U);
 }
 
+// ---------------------------------------------------------------------------
+// Near-field rotation (gpuInterpolateU / gpuInterpolateUf, nfInterpolate.cu:13-58):
+// dst(iu, iv) = src sampled at the pixel rotated by an angle about the slice
+// centre, bilinear, zero outside the slice (border addressing).  The centre is
+// (int)(R/2) for U and R/2 for Uf, as in the reference; coordinates are formed
+// in single precision like the reference's (cosine and sine of the angle come
+// from the host rounded to float; every operation is rounded on its own, no
+// fused multiply-add), the weights are exact.
+// ---------------------------------------------------------------------------
+template <class T>
+__global__ void rotate_fields_kernel(int R, float c, float s, const cpx<T>* __restrict__ src,
+                                     cpx<T>* __restrict__ dst) {
+    const int iu = blockIdx.x * blockDim.x + threadIdx.x, iv = blockIdx.y;
+    const int b = blockIdx.z;  // 0: U, 1: Uf
+    if (iu >= R) return;
+    const float uc = b == 0 ? (float)(int)(R / 2.0) : (float)(R / 2.0);
+    const float du = __fsub_rn((float)iu, uc), dv = __fsub_rn((float)iv, uc);
+    const float nx = __fsub_rn(__fadd_rn(uc, __fmul_rn(du, c)), __fmul_rn(dv, s));
+    const float ny = __fadd_rn(__fadd_rn(uc, __fmul_rn(du, s)), __fmul_rn(dv, c));
+    const cpx<T>* f = src + (size_t)b * R * R;
+    const float fx = floorf(nx), fy = floorf(ny);
+    const int i0 = (int)fx, j0 = (int)fy;
+    const T a = (T)(nx - fx), e = (T)(ny - fy);
+    auto at = [&](int i, int j) -> cpx<T> {
+        return (i >= 0 && i < R && j >= 0 && j < R) ? f[(size_t)j * R + i] : mk((T)0, (T)0);
+    };
+    const cpx<T> v00 = at(i0, j0), v01 = at(i0 + 1, j0), v10 = at(i0, j0 + 1), v11 = at(i0 + 1, j0 + 1);
+    const T w00 = (1 - a) * (1 - e), w01 = a * (1 - e), w10 = (1 - a) * e, w11 = a * e;
+    dst[(size_t)b * R * R + (size_t)iv * R + iu] =
+        mk(w00 * v00.re + w01 * v01.re + w10 * v10.re + w11 * v11.re,
+           w00 * v00.im + w01 * v01.im + w10 * v10.im + w11 * v11.im);
+}
+
+template <class T>
+void launch_rotate_fields(int R, float c, float s, const cpx<T>* src, cpx<T>* dst, cudaStream_t st) {
+    dim3 grid(blocks_for(R, 128), R, 2);
+    rotate_fields_kernel<T><<<grid, 128, 0, st>>>(R, c, s, src, dst);
+}
+
 #define BS_INST(T)                                                                                              \
+    template void launch_rotate_fields<T>(int, float, float, const cpx<T>*, cpx<T>*, cudaStream_t);             \
     template void launch_uf<T>(const Scene&, const double*, cpx<T>*, cudaStream_t);                             \
     template void launch_lut_build<T>(const zd*, int, int, const double*, int, int, Patch<T>*, cudaStream_t);   \
     template void launch_phase<T>(const Scene&, const Sphere*, const double*, cpx<T>*, float4*, cudaStream_t);  \

@@ -227,6 +227,16 @@ bs_status bs_simulate_sources(bs_ctx* ctx, const double* sources, int32_t n, bs_
  * Blank lines are skipped (the reference's parser never returns on one). */
 bs_status bs_material_eval(const char* path, const double* lambdas, int32_t n, double* n_out);
 
+/* Ring point sources by near-field rotation: the reference's --interpolate 3
+ * (SimulateExtendedSourceWithInterpolation, microscope.cu:1185-1253, with
+ * nfInterpolate.cu:13-115).  The detector sums the slice of the context's own
+ * source and, for rings r = 1 .. rings-1 of radius r um, `points` sources at
+ * angles 2 pi (i + 1) / points (z = 0, amplitude 1): each ring's first source
+ * is simulated, and source i's near field is that one rotated about the slice
+ * centre by source i's own angle (bilinear, zero outside the slice), as the
+ * reference does.  The context's focus and amplitude are kept. */
+bs_status bs_simulate_ring_interp(bs_ctx* ctx, int32_t points, int32_t rings, bs_precision prec);
+
 /* Point pos(u, v) = A + u X + v Y of the detector plane quad (microscopeStruct::pos;
  * the quad of arguments.h:340-407 built by rts/math/quad.h:55-84), e.g. for
  * placing point sources at image pixels (u = x / width, v = y / height). */

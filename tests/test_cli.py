@@ -177,6 +177,8 @@ def test_extended_source_images_give_one_source_per_nonzero_pixel(tmp_path):
     assert r.returncode == 1 and "cannot open" in r.stdout
     r = run("--interpolate", 1, "--dry-run", check=False)
     assert r.returncode == 1
+    d = dry("--interpolate", 3, "--points-rings", 6, 3)
+    assert d["interpolate"] == 3 and d["points_rings"] == [6, 3]
 
 
 def brewer_rgb(values, vmin, vmax):
