@@ -55,6 +55,8 @@ def library():
         "bs_sweep": ([vp, vp, i32, vp, C.c_int, C.c_int, vp, C.c_char_p, i32], C.c_int),
         "bs_simulate_sources": ([vp, vp, i32, C.c_int], C.c_int),
         "bs_simulate_ring_interp": ([vp, i32, i32, C.c_int], C.c_int),
+    "bs_simulate_ring_detector": ([vp, i32, i32, C.c_int], C.c_int),
+    "bs_simulate_ring_line": ([vp, i32, i32, C.c_int], C.c_int),
         "bs_plane_point": ([vp, C.c_double, C.c_double, vp], C.c_int),
         "bs_get_far_field": ([vp, C.c_int, vp, sz], C.c_int),
         "bs_material_eval": ([C.c_char_p, vp, i32, vp], C.c_int),
@@ -207,6 +209,14 @@ class Context:
     def simulate_ring_interp(self, points, rings, precision=abi.BS_PREC_MIXED):
         """The reference's --interpolate 3: ring sources by rotating each ring's first near field."""
         self._check(self.lib.bs_simulate_ring_interp(self.h, points, rings, precision))
+
+    def simulate_ring_detector(self, points, rings, precision=abi.BS_PREC_MIXED):
+        """The reference's --interpolate 1: ring sources by rotating each ring's first detector image."""
+        self._check(self.lib.bs_simulate_ring_detector(self.h, points, rings, precision))
+
+    def simulate_ring_line(self, points, rings, precision=abi.BS_PREC_MIXED):
+        """The reference's --interpolate 2: detector images from a radial line of ring samples."""
+        self._check(self.lib.bs_simulate_ring_line(self.h, points, rings, precision))
 
     def set_params(self, params):
         self._check(self.lib.bs_set_params(self.h, C.byref(params)))

@@ -455,11 +455,21 @@ int main(int argc, char** argv) {
         if (verbose) std::cout << "Number of point sources: " << sources.size() / 4 << std::endl;
     }
     const int interp = sources.empty() ? args.i("interpolate") : -1;
-    if (interp != -1 && interp != 3)
-        return fail("BIMSim Error: --interpolate " + std::to_string(interp) +
-                    " is not part of this build (mode 3, ring sources by near-field rotation, is)");
     // --points-rings: sources per ring, then rings (nf.extSource, arguments.h:471-474)
-    const int ring_points = args.i("points-rings", 0), ring_count = args.i("points-rings", 1);
+    int ring_points = args.i("points-rings", 0), ring_count = args.i("points-rings", 1);
+    if (interp < -1 || interp > 3)
+        return fail("BIMSim Error: --interpolate " + std::to_string(interp) + " is not a mode (-1, 0, 1, 2, 3)");
+    // Mode 0 (SimulateExtendedGausssianSourceNoInterp, microscope.cu:1327-1409) steps its ring loop
+    // `for (int j = spacing; j < numRings; j += spacing)` by spacing = 0.5, which never advances an int:
+    // with one ring or more the reference never finishes; with none it simulates the central source.
+    if (interp == 0 && ring_count >= 1)
+        return fail("BIMSim Error: --interpolate 0 with " + std::to_string(ring_count) +
+                    " rings does not terminate in the reference (its ring loop never advances)");
+    // Modes 1 and 3 with fewer than two rings simulate the central source only, whatever the points.
+    if ((interp == 1 || interp == 3) && ring_count < 2) {
+        ring_count = 1;
+        ring_points = ring_points < 1 ? 1 : ring_points;
+    }
 
     // spheres with their refractive index at lambda (material n + i k, rts/optics/material.h:434-446)
     std::vector<bs_sphere> spheres;
@@ -522,9 +532,13 @@ int main(int argc, char** argv) {
             if (check(bs_sample_waves_compat(ctx, nk))) return 1;
         }
     }
-    if (interp == 3) {
-        // SimulateExtendedSourceWithInterpolation + saveDetector (fileout.cu:218-224)
-        if (check(bs_simulate_ring_interp(ctx, ring_points, ring_count, precision))) return 1;
+    if (interp >= 1) {
+        // fileout.cu:218-243: mode 3 SimulateExtendedSourceWithInterpolation, 1
+        // SimulateExtendedSourceInterpAtDetector, 2 SimulateExtendedSourceInterpLineAtDetector; then saveDetector
+        bs_status st = interp == 3   ? bs_simulate_ring_interp(ctx, ring_points, ring_count, precision)
+                       : interp == 1 ? bs_simulate_ring_detector(ctx, ring_points, ring_count, precision)
+                                     : bs_simulate_ring_line(ctx, ring_points, ring_count, precision);
+        if (check(st)) return 1;
     } else if (sources.empty()) {
         if (check(bs_simulate(ctx, precision))) return 1;
         // fileoutStruct::saveNearField / saveFarField (fileout.cu:3-45): field images of
@@ -557,7 +571,8 @@ int main(int argc, char** argv) {
             if (!bsio::write_scalar_image(file, n, n, v, mag, cmap, err)) return fail("BIMSim Error: " + err);
             return 0;
         };
-        if (field_image(nearFile, false) || field_image(farFile, true)) return 1;
+        // mode 0 with no rings saves the detector only (fileout.cu:230-236)
+        if (interp == -1 && (field_image(nearFile, false) || field_image(farFile, true))) return 1;
     } else {
         // SimulateExtendedSource (microscope.cu:873-913): the detector sums the point sources
         if (check(bs_simulate_sources(ctx, sources.data(), (int)(sources.size() / 4), precision))) return 1;

@@ -169,6 +169,8 @@ struct bs_ctx {
     DevBuf d_far;           // far fields Ud, Ufd on request (bs_get_far_field)
     DevBuf d_starts;        // row / coefficient offsets of a coefficient batch
     DevBuf d_fsave;         // U, Uf of a ring's first source (bs_simulate_ring_interp)
+    DevBuf d_dacc;          // detector sum of bs_simulate_ring_detector
+    DevBuf d_line, d_ringcs;  // radial lines and ring (cos, sin) of bs_simulate_ring_line
     int det_Nv = 0;         // passband rows of the last detector run (0: no far field)
     DevBuf d_fields;  // [2][R*R] U then Uf
     DevBuf d_su, d_sv, d_mask, d_wx, d_wy, d_wix, d_wiy, d_f1, d_f2, d_g1, d_I, d_D, d_img;
@@ -191,7 +193,7 @@ static std::vector<DevBuf*> ctx_bufs(bs_ctx* c) {
             &c->d_tabscr, &c->d_legP, &c->d_lut, &c->d_uft, &c->d_uftscr, &c->d_fields, &c->d_su,
             &c->d_sv, &c->d_mask, &c->d_wx, &c->d_wy, &c->d_wix, &c->d_wiy, &c->d_f1, &c->d_f2,
             &c->d_g1, &c->d_I, &c->d_D, &c->d_img, &c->d_cones, &c->d_cnt, &c->d_far,
-            &c->d_starts, &c->d_fsave};
+            &c->d_starts, &c->d_fsave, &c->d_dacc, &c->d_line, &c->d_ringcs};
 }
 
 static void release_all(bs_ctx* c) {
@@ -1202,11 +1204,54 @@ bs_status bs_material_eval(const char* path, const double* lambdas, int32_t n, d
 
 }  // extern "C"
 
+// Ring point sources (--interpolate 1, 2, 3; microscope.cu:1004-1253).  Ring
+// r = 1, 2, ... has radius r um; its sources sit at the angles of
+// generatePointSources (microscope.cu:1298-1325): t_0 = 2 pi / points in float,
+// each next one the float sum of the previous and that step; cosines and sines
+// are double values rounded to float (the reference used float ones).
+static std::vector<float> ring_angles(int points) {
+    const float step = 2 * (float)PI_REF / (float)points;
+    std::vector<float> t(points);
+    float th = step;
+    for (int i = 0; i < points; i++) {
+        t[i] = th;
+        th += step;
+    }
+    return t;
+}
+
+static void stats_add(bs_stats& sum, const bs_stats& s) {
+    sum.ms_total += s.ms_total;
+    sum.ms_uf += s.ms_uf;
+    sum.ms_mie += s.ms_mie;
+    sum.ms_lut += s.ms_lut;
+    sum.ms_us += s.ms_us;
+    sum.ms_detector += s.ms_detector;
+    sum.kernel_launches += s.kernel_launches;
+    sum.us_interactions += s.us_interactions;
+    sum.lut_chunks_staged += s.lut_chunks_staged;
+    sum.lut_chunks_total += s.lut_chunks_total;
+    sum.lut_tables_built += s.lut_tables_built;
+    sum.lut_staged_predicted = s.lut_staged_predicted;
+}
+
+// One source of a ring driver at (x, y, z) with amplitude a; its stats are
+// added to sum.  The sphere tables are built by the first source and reused.
+static bs_status ring_source(bs_ctx* c, bs_precision prec, const double* xyz, double a, bool accumulate,
+                             bs_stats& sum) {
+    if (xyz)
+        for (int k = 0; k < 3; k++) c->prm.focus[k] = xyz[k];
+    c->prm.amplitude = a;
+    bs_status st = simulate_impl(c, prec, accumulate);
+    if (st == BS_OK) stats_add(sum, c->stats);
+    return st;
+}
+
 // The detector images of the near field in d_fields rotated by each angle,
 // added to the detector (nearfieldStruct::Interpolate + SimulateImaging,
 // microscope.cu:834-846); d_fields itself is kept in d_fsave and overwritten.
 template <class T>
-static bs_status image_rotations(bs_ctx* c, const std::vector<float>& angles) {
+static bs_status field_rotations(bs_ctx* c, const std::vector<float>& angles) {
     const size_t n = 2 * (size_t)c->R * c->R;
     CK(c->d_fsave.ensure(n * sizeof(cpx<T>)));
     CK(cudaMemcpyAsync(c->d_fsave.p, c->d_fields.p, n * sizeof(cpx<T>), cudaMemcpyDeviceToDevice, c->st));
@@ -1222,56 +1267,45 @@ static bs_status image_rotations(bs_ctx* c, const std::vector<float>& angles) {
     return BS_OK;
 }
 
-extern "C" {
+// Mode 1 (InterpAtDetector, microscope.cu:312-321): the sum so far is in
+// d_dacc, the ring's first source alone in d_D; both are added to d_dacc, then
+// that image rotated by each angle.
+template <class T>
+static bs_status image_rotations(bs_ctx* c, const std::vector<float>& angles) {
+    const T* one = c->d_D.as<T>();
+    T* acc = c->d_dacc.as<T>();
+    launch_rotate_add_images<T>(c->res, 1.f, 0.f, one, acc, c->st);  // angle 0: the image itself
+    LAUNCHED(c);
+    for (float a : angles) {
+        launch_rotate_add_images<T>(c->res, (float)std::cos((double)a), (float)std::sin((double)a), one, acc, c->st);
+        LAUNCHED(c);
+    }
+    CK(cudaStreamSynchronize(c->st));
+    CK(cudaGetLastError());
+    return BS_OK;
+}
 
-bs_status bs_simulate_ring_interp(bs_ctx* c, int32_t points, int32_t rings, bs_precision prec) {
-    if (!c || points < 1 || rings < 1) return fail(BS_ERR_ARG, "bs_simulate_ring_interp: points and rings must be >= 1");
-    if (prec != BS_PREC_FP64 && prec != BS_PREC_MIXED)
-        return fail(BS_ERR_ARG, "bs_simulate_ring_interp: unknown precision");
+// Mode 2 (InterpLineForAllPointSources, microscope.cu:336-354): the current
+// source's D and Di feed their radial lines.
+template <class T>
+static bs_status line_samples(bs_ctx* c, int points, int L) {
+    launch_ring_line<T>(c->res, points, L, c->d_ringcs.as<float2>(), c->d_D.as<T>(), c->d_line.as<T>(), c->st);
+    LAUNCHED(c);
+    CK(cudaGetLastError());
+    return BS_OK;
+}
+
+// Shared frame of the ring drivers: tables reused across the sources, the
+// context's focus, amplitude and reuse setting restored afterwards.
+template <class F>
+static bs_status ring_driver(bs_ctx* c, bs_precision prec, int32_t points, int32_t rings, const char* name, F&& body) {
+    if (!c || points < 1 || rings < 1) return fail(BS_ERR_ARG, "%s: points and rings must be >= 1", name);
+    if (prec != BS_PREC_FP64 && prec != BS_PREC_MIXED) return fail(BS_ERR_ARG, "%s: unknown precision", name);
     const bs_params saved = c->prm;
     const bool saved_reuse = c->reuse;
     c->reuse = true;  // the sphere tables do not depend on the focus or the amplitude
     bs_stats sum{};
-    auto add = [&sum](const bs_stats& s) {
-        sum.ms_total += s.ms_total;
-        sum.ms_uf += s.ms_uf;
-        sum.ms_mie += s.ms_mie;
-        sum.ms_lut += s.ms_lut;
-        sum.ms_us += s.ms_us;
-        sum.ms_detector += s.ms_detector;
-        sum.kernel_launches += s.kernel_launches;
-        sum.us_interactions += s.us_interactions;
-        sum.lut_chunks_staged += s.lut_chunks_staged;
-        sum.lut_chunks_total += s.lut_chunks_total;
-        sum.lut_tables_built += s.lut_tables_built;
-    };
-    // the source at the context's own focus (SimulateExtendedSourceWithInterpolation, microscope.cu:1185-1253)
-    bs_status st = simulate_impl(c, prec, false);
-    if (st == BS_OK) add(c->stats);
-    // rings of radius 1, 2, ... um; point i at angle 2 pi (i + 1) / points, accumulated in float from
-    // 2 * PI / points (generatePointSources, microscope.cu:1298-1325), amplitude 1, z = 0; cosines
-    // and sines are taken in double and rounded to float (the reference used float cos and sin).  Only a ring's
-    // first point is simulated; point i's near field is that one rotated by point i's own angle.
-    const float step = 2 * (float)PI_REF / (float)points;
-    for (int ring = 1; ring < rings && st == BS_OK; ring++) {
-        const float radius = (float)ring;
-        std::vector<float> theta(points);
-        float th = step;
-        for (int i = 0; i < points; i++) {
-            theta[i] = th;
-            th += step;
-        }
-        c->prm.focus[0] = (float)std::cos((double)theta[0]) * radius;
-        c->prm.focus[1] = (float)std::sin((double)theta[0]) * radius;
-        c->prm.focus[2] = 0;
-        c->prm.amplitude = 1;
-        st = simulate_impl(c, prec, true);
-        if (st != BS_OK) break;
-        add(c->stats);
-        const std::vector<float> angles(theta.begin() + 1, theta.end());
-        if (!angles.empty())
-            st = prec == BS_PREC_FP64 ? image_rotations<double>(c, angles) : image_rotations<float>(c, angles);
-    }
+    bs_status st = body(sum);
     c->prm = saved;
     c->reuse = saved_reuse;
     if (!saved_reuse) c->lut_valid = false;
@@ -1282,6 +1316,93 @@ bs_status bs_simulate_ring_interp(bs_ctx* c, int32_t points, int32_t rings, bs_p
     c->stats = sum;
     c->have = true;
     return BS_OK;
+}
+
+static void ring_focus(float t0, int ring, double* xyz) {
+    xyz[0] = (float)std::cos((double)t0) * (float)ring;
+    xyz[1] = (float)std::sin((double)t0) * (float)ring;
+    xyz[2] = 0;
+}
+
+extern "C" {
+
+bs_status bs_simulate_ring_interp(bs_ctx* c, int32_t points, int32_t rings, bs_precision prec) {
+    return ring_driver(c, prec, points, rings, "bs_simulate_ring_interp", [&](bs_stats& sum) {
+        // the source at the context's own focus (SimulateExtendedSourceWithInterpolation, microscope.cu:1189-1253)
+        bs_status st = ring_source(c, prec, nullptr, c->prm.amplitude, false, sum);
+        const std::vector<float> th = ring_angles(points);
+        const std::vector<float> rest(th.begin() + 1, th.end());
+        for (int ring = 1; ring < rings && st == BS_OK; ring++) {
+            double f[3];
+            ring_focus(th[0], ring, f);
+            // only a ring's first source is simulated; source i's near field is that one rotated by its angle
+            st = ring_source(c, prec, f, 1.0, true, sum);
+            if (st == BS_OK && !rest.empty())
+                st = prec == BS_PREC_FP64 ? field_rotations<double>(c, rest) : field_rotations<float>(c, rest);
+        }
+        return st;
+    });
+}
+
+bs_status bs_simulate_ring_detector(bs_ctx* c, int32_t points, int32_t rings, bs_precision prec) {
+    return ring_driver(c, prec, points, rings, "bs_simulate_ring_detector", [&](bs_stats& sum) {
+        // SimulateExtendedSourceInterpAtDetector (microscope.cu:1004-1093)
+        bs_status st = ring_source(c, prec, nullptr, c->prm.amplitude, false, sum);
+        if (st != BS_OK) return st;
+        const size_t bytes = 2 * (size_t)c->res * c->res * elem_r(prec);
+        CK(c->d_dacc.ensure(bytes));
+        CK(cudaMemcpyAsync(c->d_dacc.p, c->d_D.p, bytes, cudaMemcpyDeviceToDevice, c->st));
+        const std::vector<float> th = ring_angles(points);
+        const std::vector<float> rest(th.begin() + 1, th.end());
+        for (int ring = 1; ring < rings && st == BS_OK; ring++) {
+            double f[3];
+            ring_focus(th[0], ring, f);
+            st = ring_source(c, prec, f, 1.0, false, sum);  // d_D: this source alone (saveDetectorForOnePs)
+            if (st == BS_OK)
+                st = prec == BS_PREC_FP64 ? image_rotations<double>(c, rest) : image_rotations<float>(c, rest);
+        }
+        if (st != BS_OK) return st;
+        CK(cudaMemcpyAsync(c->d_D.p, c->d_dacc.p, bytes, cudaMemcpyDeviceToDevice, c->st));
+        CK(cudaStreamSynchronize(c->st));
+        return BS_OK;
+    });
+}
+
+bs_status bs_simulate_ring_line(bs_ctx* c, int32_t points, int32_t rings, bs_precision prec) {
+    if (points > BS_RING_LINE_MAX_POINTS)
+        return fail(BS_ERR_ARG, "bs_simulate_ring_line: at most %d points per ring (one thread block per ring)",
+                    BS_RING_LINE_MAX_POINTS);
+    return ring_driver(c, prec, points, rings, "bs_simulate_ring_line", [&](bs_stats& sum) {
+        // SimulateExtendedSourceInterpLineAtDetector (microscope.cu:1097-1183): the context's focus, then
+        // (j, 0, 0) for j = 1 .. rings-1, all with amplitude 1; every source's image feeds the radial lines
+        // of `rings` entries, which then replace the detector images.
+        const size_t er = elem_r(prec), L = (size_t)rings;
+        CK(c->d_line.ensure(2 * L * er));
+        CK(cudaMemsetAsync(c->d_line.p, 0, 2 * L * er, c->st));
+        std::vector<float2> cs(points);
+        for (int k = 0; k < points; k++) {
+            const float t = (float)((2.0 * PI_REF / points) * (k + 1));
+            cs[k] = make_float2((float)std::cos((double)t), (float)std::sin((double)t));
+        }
+        CK(c->d_ringcs.ensure(cs.size() * sizeof(float2)));
+        CK(cudaMemcpyAsync(c->d_ringcs.p, cs.data(), cs.size() * sizeof(float2), cudaMemcpyHostToDevice, c->st));
+        bs_status st = BS_OK;
+        for (int j = 0; j < rings && st == BS_OK; j++) {
+            const double f[3] = {(double)j, 0, 0};
+            st = ring_source(c, prec, j == 0 ? nullptr : f, 1.0, false, sum);
+            if (st == BS_OK) st = prec == BS_PREC_FP64 ? line_samples<double>(c, points, rings)
+                                                       : line_samples<float>(c, points, rings);
+        }
+        if (st != BS_OK) return st;
+        if (prec == BS_PREC_FP64)
+            launch_line_image<double>(c->res, rings, c->d_line.as<double>(), c->d_D.as<double>(), c->st);
+        else
+            launch_line_image<float>(c->res, rings, c->d_line.as<float>(), c->d_D.as<float>(), c->st);
+        LAUNCHED(c);
+        CK(cudaStreamSynchronize(c->st));
+        CK(cudaGetLastError());
+        return BS_OK;
+    });
 }
 
 bs_status bs_plane_point(const bs_params* params, double u, double v, double* xyz) {

@@ -175,12 +175,110 @@ void launch_image(int n, int kind, const T* D, const T* Di, T* out, cudaStream_t
     image_kernel<T><<<(n + 255) / 256, 256, 0, st>>>(n, kind, D, Di, out);
 }
 
+// ---------------------------------------------------------------------------
+// Ring point sources on the detector (--interpolate 1 and 2).  The reference
+// samples the images through linearly filtered float textures with border
+// addressing; here coordinates are formed in single precision as its kernels
+// form them (each operation rounded on its own, no fused multiply-add) and the
+// bilinear weights are exact, zero outside the image.
+// ---------------------------------------------------------------------------
+template <class T>
+__device__ __forceinline__ T image_bilinear(const T* __restrict__ f, int res, float x, float y) {
+    const float fx = floorf(x), fy = floorf(y);
+    const int i0 = (int)fx, j0 = (int)fy;
+    const T a = (T)(x - fx), e = (T)(y - fy);
+    auto at = [&](int i, int j) -> T {
+        return (i >= 0 && i < res && j >= 0 && j < res) ? f[(size_t)j * res + i] : (T)0;
+    };
+    return (1 - a) * (1 - e) * at(i0, j0) + a * (1 - e) * at(i0 + 1, j0) + (1 - a) * e * at(i0, j0 + 1) +
+           a * e * at(i0 + 1, j0 + 1);
+}
+
+// InterpolateAndIntegrateUd / Ufd (microscope.cu:89-135): dst[b] += src[b]
+// rotated by (c, s) about ((int)(res/2), (int)(res/2)); b = 0: D, 1: Di.
+template <class T>
+__global__ void rotate_add_images_kernel(int res, float c, float s, const T* __restrict__ src, T* __restrict__ dst) {
+    const int iu = blockIdx.x * blockDim.x + threadIdx.x, iv = blockIdx.y, b = blockIdx.z;
+    if (iu >= res) return;
+    const float uc = (float)(int)(res / 2.0);
+    const float du = __fsub_rn((float)iu, uc), dv = __fsub_rn((float)iv, uc);
+    const float x = __fsub_rn(__fadd_rn(uc, __fmul_rn(du, c)), __fmul_rn(dv, s));
+    const float y = __fadd_rn(__fadd_rn(uc, __fmul_rn(du, s)), __fmul_rn(dv, c));
+    const size_t plane = (size_t)res * res;
+    dst[b * plane + (size_t)iv * res + iu] += image_bilinear(src + b * plane, res, x, y);
+}
+
+// simRing_Ud / simRing_Ufd (microscope.cu:138-250): block (r, b) adds to
+// line[b][r] the image samples at (uc + r cos t_k, uc - r sin t_k), k < points,
+// summed in the reference's shared-memory tree (steps points/2, ..., 1: with a
+// count that is not a power of two some samples never reach the sum).
+// cs[k] = (cos t_k, sin t_k) rounded to float.
+template <class T>
+__global__ void ring_line_kernel(int res, int points, int L, const float2* __restrict__ cs, const T* __restrict__ img,
+                                 T* __restrict__ line) {
+    extern __shared__ __align__(16) unsigned char ring_smem[];
+    T* sh = reinterpret_cast<T*>(ring_smem);
+    const int r = blockIdx.x, b = blockIdx.y;
+    const float uc = (float)(int)(res / 2.0);
+    const T* f = img + (size_t)b * res * res;
+    for (int k = threadIdx.x; k < points; k += blockDim.x) {
+        const float2 t = cs[k];
+        const float x = __fadd_rn(uc, __fmul_rn((float)r, t.x)), y = __fsub_rn(uc, __fmul_rn((float)r, t.y));
+        sh[k] = image_bilinear(f, res, x, y);
+    }
+    __syncthreads();
+    for (unsigned step = (unsigned)points / 2; step >= 1; step >>= 1) {
+        for (unsigned k = threadIdx.x; k < step; k += blockDim.x) sh[k] += sh[k + step];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) line[(size_t)b * L + r] += sh[0];
+}
+
+// InterpolateAndIntegrateUdFromLine / UfdFromLine (microscope.cu:37-85): the
+// detector pixel at distance r = sqrt((iu-uc)^2 + (iv-uc)^2) from the centre
+// is line[b] linearly interpolated at r, zero beyond its L entries.
+template <class T>
+__global__ void line_image_kernel(int res, int L, const T* __restrict__ line, T* __restrict__ D) {
+    const int iu = blockIdx.x * blockDim.x + threadIdx.x, iv = blockIdx.y, b = blockIdx.z;
+    if (iu >= res) return;
+    const float uc = (float)(int)(res / 2.0);
+    const float du = __fsub_rn((float)iu, uc), dv = __fsub_rn((float)iv, uc);
+    const float r = __fsqrt_rn(__fadd_rn(__fmul_rn(du, du), __fmul_rn(dv, dv)));
+    const float fr = floorf(r);
+    const int i0 = (int)fr;
+    const T a = (T)(r - fr);
+    const T* l = line + (size_t)b * L;
+    const T v0 = i0 < L ? l[i0] : (T)0, v1 = i0 + 1 < L ? l[i0 + 1] : (T)0;
+    D[(size_t)b * res * res + (size_t)iv * res + iu] = (1 - a) * v0 + a * v1;
+}
+
+template <class T>
+void launch_rotate_add_images(int res, float c, float s, const T* src, T* dst, cudaStream_t st) {
+    dim3 grid((res + 127) / 128, res, 2);
+    rotate_add_images_kernel<T><<<grid, 128, 0, st>>>(res, c, s, src, dst);
+}
+
+template <class T>
+void launch_ring_line(int res, int points, int L, const float2* cs, const T* img, T* line, cudaStream_t st) {
+    const int threads = points >= 1024 ? 1024 : ((points + 31) / 32) * 32;
+    ring_line_kernel<T><<<dim3(L, 2), threads, (size_t)points * sizeof(T), st>>>(res, points, L, cs, img, line);
+}
+
+template <class T>
+void launch_line_image(int res, int L, const T* line, T* D, cudaStream_t st) {
+    dim3 grid((res + 127) / 128, res, 2);
+    line_image_kernel<T><<<grid, 128, 0, st>>>(res, L, line, D);
+}
+
 #define BS_DET_INST(T)                                                                                          \
     template void launch_twiddle<T>(int, int, const int*, int, int, int, int, int, cpx<T>*, cudaStream_t);      \
     template void launch_cgemm<T>(int, int, int, int, const cpx<T>*, int, long long, const cpx<T>*, int,       \
                                   long long, cpx<T>*, int, long long, int, const float*, T, T*, cudaStream_t); \
     template void launch_bin<T>(int, int, int, int, const T*, T*, cudaStream_t);                                    \
-    template void launch_image<T>(int, int, const T*, const T*, T*, cudaStream_t);
+    template void launch_image<T>(int, int, const T*, const T*, T*, cudaStream_t);                             \
+    template void launch_rotate_add_images<T>(int, float, float, const T*, T*, cudaStream_t);                 \
+    template void launch_ring_line<T>(int, int, int, const float2*, const T*, T*, cudaStream_t);              \
+    template void launch_line_image<T>(int, int, const T*, T*, cudaStream_t);
 BS_DET_INST(float)
 BS_DET_INST(double)
 

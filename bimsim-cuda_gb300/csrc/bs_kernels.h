@@ -93,6 +93,17 @@ void launch_cgemm(int M, int N, int K, int batch, const cpx<T>* A, int lda, long
 template <class T>
 void launch_bin(int res, int ss, int batch, int accumulate, const T* I, T* D, cudaStream_t st);
 
+// Ring point sources on the detector (microscope.cu:37-250): dst[b] += src[b]
+// rotated by (c, s) about ((int)(res/2), (int)(res/2)), b = 0, 1; line[b][r] +=
+// the tree sum of src[b] at radius r, angles with (cos, sin) cs[k], k < points
+// (points <= 1023); D[b] = line[b] interpolated at each pixel's radius.
+template <class T>
+void launch_rotate_add_images(int res, float c, float s, const T* src, T* dst, cudaStream_t st);
+template <class T>
+void launch_ring_line(int res, int points, int L, const float2* cs, const T* img, T* line, cudaStream_t st);
+template <class T>
+void launch_line_image(int res, int L, const T* line, T* D, cudaStream_t st);
+
 // image kinds 2, 3: -log10(D/Di), D/Di (microscope.cu:722-775); 0, 1: copies
 template <class T>
 void launch_image(int n, int kind, const T* D, const T* Di, T* out, cudaStream_t st);

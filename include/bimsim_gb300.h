@@ -237,6 +237,29 @@ bs_status bs_material_eval(const char* path, const double* lambdas, int32_t n, d
  * reference does.  The context's focus and amplitude are kept. */
 bs_status bs_simulate_ring_interp(bs_ctx* ctx, int32_t points, int32_t rings, bs_precision prec);
 
+/* Ring point sources by detector-image rotation: the reference's --interpolate 1
+ * (SimulateExtendedSourceInterpAtDetector, microscope.cu:1004-1093, with
+ * InterpolateAndIntegrateUd/Ufd, microscope.cu:89-135).  The same sources as
+ * bs_simulate_ring_interp; each ring's first source is simulated and source i's
+ * detector images are that source's images rotated about the detector centre
+ * ((int)(res/2), both axes) by source i's angle (bilinear, zero outside). */
+bs_status bs_simulate_ring_detector(bs_ctx* ctx, int32_t points, int32_t rings, bs_precision prec);
+
+/* Radial-line ring sources: the reference's --interpolate 2
+ * (SimulateExtendedSourceInterpLineAtDetector, microscope.cu:1097-1183, with
+ * simRing_Ud/Ufd :138-250 and InterpolateAndIntegrateUdFromLine :37-85).
+ * Sources at the context's focus and at (j, 0, 0) um, j = 1 .. rings-1, all with
+ * amplitude 1.  For each source and each radius r < rings (pixels), the
+ * source's detector image is sampled at `points` angles 2 pi (k + 1) / points
+ * around the detector centre and the samples are added in the reference's
+ * shared-memory tree (for a count that is not a power of two some samples are
+ * left out, as there); the per-radius sums over all sources form a line of
+ * `rings` entries, and each detector pixel is that line interpolated at its
+ * distance from the centre (zero beyond the line).  points <= 1023 (the
+ * reference runs one thread block of at most 1024 threads per ring). */
+#define BS_RING_LINE_MAX_POINTS 1023
+bs_status bs_simulate_ring_line(bs_ctx* ctx, int32_t points, int32_t rings, bs_precision prec);
+
 /* Point pos(u, v) = A + u X + v Y of the detector plane quad (microscopeStruct::pos;
  * the quad of arguments.h:340-407 built by rts/math/quad.h:55-84), e.g. for
  * placing point sources at image pixels (u = x / width, v = y / height). */

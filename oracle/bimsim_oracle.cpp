@@ -1039,6 +1039,111 @@ void detector(const bs_params& p, const Geom& g, const cd* U, double* D) {
 }
 
 // ---------------------------------------------------------------------------
+// Ring point sources (--interpolate 1, 2, 3).  The reference samples rotated
+// images through linearly filtered textures with border addressing; here the
+// sample coordinates are formed in single precision as the reference's kernels
+// form them (each operation rounded on its own), cosines and sines are double
+// values rounded to float, and the bilinear weights are exact (zero outside).
+// ---------------------------------------------------------------------------
+template <class V>
+V bilinear_at(const V* f, int W, int H, float x, float y) {
+    const float fx = std::floor(x), fy = std::floor(y);
+    const int i0 = (int)fx, j0 = (int)fy;
+    const double a = (double)(x - fx), e = (double)(y - fy);
+    auto at = [&](int i, int j) -> V { return (i >= 0 && i < W && j >= 0 && j < H) ? f[(size_t)j * W + i] : V(0); };
+    return (1 - a) * (1 - e) * at(i0, j0) + a * (1 - e) * at(i0 + 1, j0) + (1 - a) * e * at(i0, j0 + 1) +
+           a * e * at(i0 + 1, j0 + 1);
+}
+
+// Position of pixel (iu, iv) rotated by (c, s) about (uc, uc):
+// uc + (iu - uc) c - (iv - uc) s, uc + (iu - uc) s + (iv - uc) c
+// (nfInterpolate.cu:28-29, microscope.cu:101-102).
+void rotated_xy(int iu, int iv, float uc, float c, float s, float& x, float& y) {
+    const float du = (float)iu - uc, dv = (float)iv - uc;
+    x = (uc + du * c) - dv * s;
+    y = (uc + du * s) + dv * c;
+}
+
+// gpuInterpolateU / gpuInterpolateUf (nfInterpolate.cu:13-66): centre (int)(R/2)
+// for U, R/2 for Uf.
+void rotate_field(int R, float c, float s, bool int_centre, const cd* src, cd* dst) {
+    const float uc = int_centre ? (float)(int)(R / 2.0) : (float)(R / 2.0);
+    for (int iv = 0; iv < R; iv++)
+        for (int iu = 0; iu < R; iu++) {
+            float x, y;
+            rotated_xy(iu, iv, uc, c, s, x, y);
+            dst[(size_t)iv * R + iu] = bilinear_at(src, R, R, x, y);
+        }
+}
+
+// InterpolateAndIntegrateUd / Ufd (microscope.cu:89-135): dst += src rotated
+// about ((int)(res/2), (int)(res/2)).
+void rotate_add_image(int res, float c, float s, const double* src, double* dst) {
+    const float uc = (float)(int)(res / 2.0);
+    for (int iv = 0; iv < res; iv++)
+        for (int iu = 0; iu < res; iu++) {
+            float x, y;
+            rotated_xy(iu, iv, uc, c, s, x, y);
+            dst[(size_t)iv * res + iu] += bilinear_at(src, res, res, x, y);
+        }
+}
+
+// simRing_Ud / simRing_Ufd (microscope.cu:138-250): for each radius r < L,
+// line[r] += the sum of the image at (uc + r cos t_k, uc - r sin t_k),
+// t_k = (2 pi / points)(k + 1) formed in double and rounded to float, added in
+// the reference's shared-memory tree (steps points/2, points/4, ..., 1; with a
+// count that is not a power of two some samples never reach the sum).
+void ring_line(int res, int points, int L, const double* img, double* line) {
+    const float uc = (float)(int)(res / 2.0);
+    std::vector<float> cs(2 * (size_t)points);
+    for (int k = 0; k < points; k++) {
+        const float t = (float)((2.0 * PI_REF / points) * (k + 1));
+        cs[2 * k] = (float)std::cos((double)t);
+        cs[2 * k + 1] = (float)std::sin((double)t);
+    }
+    std::vector<double> sh(points);
+    for (int r = 0; r < L; r++) {
+        for (int k = 0; k < points; k++) {
+            const float x = uc + (float)r * cs[2 * k], y = uc - (float)r * cs[2 * k + 1];
+            sh[k] = bilinear_at(img, res, res, x, y);
+        }
+        for (unsigned step = (unsigned)points / 2; step >= 1; step >>= 1)
+            for (unsigned k = 0; k < step; k++) sh[k] += sh[k + step];
+        line[r] += sh[0];
+    }
+}
+
+// InterpolateAndIntegrateUdFromLine / UfdFromLine (microscope.cu:37-85): D at
+// distance r = sqrt((iu-uc)^2 + (iv-uc)^2) (single precision) from the centre
+// is the line linearly interpolated at r, zero beyond its L entries.
+void line_image(int res, int L, const double* line, double* D) {
+    const float uc = (float)(int)(res / 2.0);
+    for (int iv = 0; iv < res; iv++)
+        for (int iu = 0; iu < res; iu++) {
+            const float du = (float)iu - uc, dv = (float)iv - uc;
+            const float r = std::sqrt(du * du + dv * dv);
+            const float fr = std::floor(r);
+            const int i0 = (int)fr;
+            const double a = (double)(r - fr);
+            const double v0 = i0 < L ? line[i0] : 0.0, v1 = i0 + 1 < L ? line[i0 + 1] : 0.0;
+            D[(size_t)iv * res + iu] = (1 - a) * v0 + a * v1;
+        }
+}
+
+// Ring angles of generatePointSources (microscope.cu:1298-1325): t_0 = 2 pi / points
+// in float, each next one the float sum of the previous and that step.
+std::vector<float> ring_angles(int points) {
+    const float step = 2 * (float)PI_REF / (float)points;
+    std::vector<float> t(points);
+    float th = step;
+    for (int i = 0; i < points; i++) {
+        t[i] = th;
+        th += step;
+    }
+    return t;
+}
+
+// ---------------------------------------------------------------------------
 // ENVI
 // ---------------------------------------------------------------------------
 std::string fmt_g(double v) {
@@ -1419,6 +1524,77 @@ int bso_simulate(const bs_params* p, const bs_sphere* s, int ns, const double* w
     if (Uf) std::memcpy(Uf, uf.data(), uf.size() * sizeof(cd));
     if (D) detector(*p, sc.g, u.data(), D);
     if (Di) detector(*p, sc.g, uf.data(), Di);
+    return 0;
+}
+
+// The reference's ring drivers: mode 3 SimulateExtendedSourceWithInterpolation
+// (microscope.cu:1189-1253), mode 1 SimulateExtendedSourceInterpAtDetector
+// (:1004-1093), mode 2 SimulateExtendedSourceInterpLineAtDetector (:1097-1183).
+int bso_simulate_rings(const bs_params* p, const bs_sphere* s, int ns, const double* waves, int nk, int nthreads,
+                       int mode, int points, int rings, double* D, double* Di) {
+    if (points < 1 || rings < 1 || (mode != 1 && mode != 2 && mode != 3)) return 1;
+    const Geom g = derive(*p);
+    const int R = g.R, res = g.res;
+    const size_t nf = (size_t)R * R, ni = (size_t)res * res;
+    std::vector<cd> u(nf), uf(nf), ur(nf), ufr(nf);
+    std::vector<double> d(ni), di(ni), t(ni);
+    std::fill(D, D + ni, 0.0);
+    std::fill(Di, Di + ni, 0.0);
+    auto source = [&](bs_params q) {
+        bso_simulate(&q, s, ns, waves, nk, nthreads, reinterpret_cast<double*>(u.data()),
+                     reinterpret_cast<double*>(uf.data()), d.data(), di.data());
+    };
+    if (mode == 2) {
+        // every source's image feeds the radial line; the detector is the line
+        std::vector<double> line(rings, 0.0), linei(rings, 0.0);
+        bs_params q = *p;
+        q.amplitude = 1;
+        for (int j = 0; j < rings; j++) {
+            if (j > 0) {
+                q.focus[0] = j;
+                q.focus[1] = 0;
+                q.focus[2] = 0;
+            }
+            source(q);
+            ring_line(res, points, rings, d.data(), line.data());
+            ring_line(res, points, rings, di.data(), linei.data());
+        }
+        line_image(res, rings, line.data(), D);
+        line_image(res, rings, linei.data(), Di);
+        return 0;
+    }
+    source(*p);
+    for (size_t i = 0; i < ni; i++) {
+        D[i] += d[i];
+        Di[i] += di[i];
+    }
+    for (int ring = 1; ring < rings; ring++) {
+        const std::vector<float> th = ring_angles(points);
+        bs_params q = *p;
+        q.focus[0] = (float)std::cos((double)th[0]) * (float)ring;
+        q.focus[1] = (float)std::sin((double)th[0]) * (float)ring;
+        q.focus[2] = 0;
+        q.amplitude = 1;
+        source(q);
+        for (size_t i = 0; i < ni; i++) {
+            D[i] += d[i];
+            Di[i] += di[i];
+        }
+        for (int k = 1; k < points; k++) {
+            const float c = (float)std::cos((double)th[k]), sn = (float)std::sin((double)th[k]);
+            if (mode == 3) {
+                rotate_field(R, c, sn, true, u.data(), ur.data());
+                rotate_field(R, c, sn, false, uf.data(), ufr.data());
+                detector(*p, g, ur.data(), t.data());
+                for (size_t i = 0; i < ni; i++) D[i] += t[i];
+                detector(*p, g, ufr.data(), t.data());
+                for (size_t i = 0; i < ni; i++) Di[i] += t[i];
+            } else {
+                rotate_add_image(res, c, sn, d.data(), D);
+                rotate_add_image(res, c, sn, di.data(), Di);
+            }
+        }
+    }
     return 0;
 }
 

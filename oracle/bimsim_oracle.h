@@ -92,6 +92,12 @@ int bso_nearfield_rows_timed(const bs_params* p, const bs_sphere* s, int ns, con
 /* Far field Ud (crop_res^2 complex, interleaved): band-passed U on the crop, scaled by 1/R^2. */
 int bso_far_field(const bs_params* p, const double* U, double* out);
 
+/* Ring point sources, mode 1 (detector images rotated, microscope.cu:1004-1093),
+ * 2 (radial line of ring samples, :1097-1183) or 3 (near fields rotated,
+ * :1189-1253 with nfInterpolate.cu); D, Di: det_res^2 detector images. */
+int bso_simulate_rings(const bs_params* p, const bs_sphere* s, int ns, const double* waves, int nk, int nthreads,
+                       int mode, int points, int rings, double* D, double* Di);
+
 /* Forward (sign=-1) or inverse (sign=+1, unnormalised) 1-D DFT of n complex. */
 int bso_fft(int n, int sign, double* data);
 

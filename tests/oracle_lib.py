@@ -52,6 +52,7 @@ def load():
     lib.bso_nearfield_rows.argtypes = [vp, vp, C.c_int, vp, C.c_int, C.c_int, C.c_int, C.c_int, vp]
     lib.bso_nearfield_rows_timed.argtypes = [vp, vp, C.c_int, vp, C.c_int, C.c_int, C.c_int, C.c_int, vp, vp]
     lib.bso_detector.argtypes = [vp, vp, vp, vp, vp]
+    lib.bso_simulate_rings.argtypes = [vp, vp, C.c_int, vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, vp, vp]
     lib.bso_far_field.argtypes = [vp, vp, vp]
     lib.bso_fft.argtypes = [C.c_int, C.c_int, vp]
     lib.bso_envi_add_band.argtypes = [C.c_char_p, vp, C.c_int, C.c_int, C.c_double, C.c_int]
@@ -75,6 +76,20 @@ def sphere_geom(params, sphere):
     g = SphereGeom()
     load().bso_sphere_derive(C.byref(params), C.byref(sphere), C.byref(g))
     return g
+
+
+def simulate_rings(params, spheres, ns, waves, mode, points, rings, nthreads=0):
+    """Ring point sources (--interpolate mode 1, 2 or 3) -> (D, Di)."""
+    lib = load()
+    res = geom(params).det_res
+    D = np.zeros(res * res)
+    Di = np.zeros(res * res)
+    w = np.ascontiguousarray(waves, dtype=np.float64).reshape(-1)
+    nk = len(w) // 3
+    rc = lib.bso_simulate_rings(C.byref(params), C.byref(spheres), ns, P(w) if nk else None, nk, nthreads, mode,
+                                points, rings, P(D), P(Di))
+    assert rc == 0, rc
+    return D.reshape(res, res), Di.reshape(res, res)
 
 
 def simulate(params, spheres, ns, waves, nthreads=0):

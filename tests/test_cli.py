@@ -175,10 +175,17 @@ def test_extended_source_images_give_one_source_per_nonzero_pixel(tmp_path):
     assert dry("--extended-source", bmp8, "--xy", 10, 0)["point_sources"] == 3
     r = run("--extended-source", tmp_path / "missing.pgm", "--dry-run", check=False)
     assert r.returncode == 1 and "cannot open" in r.stdout
-    r = run("--interpolate", 1, "--dry-run", check=False)
-    assert r.returncode == 1
-    d = dry("--interpolate", 3, "--points-rings", 6, 3)
-    assert d["interpolate"] == 3 and d["points_rings"] == [6, 3]
+    for mode in (1, 2, 3):
+        d = dry("--interpolate", mode, "--points-rings", 6, 3)
+        assert d["interpolate"] == mode and d["points_rings"] == [6, 3]
+    # modes 1 and 3 with fewer than two rings: the central source only
+    assert dry("--interpolate", 3, "--points-rings", 0, 0)["points_rings"] == [1, 1]
+    # mode 0's ring loop never advances in the reference: refused with rings, the central source without
+    r = run("--interpolate", 0, "--dry-run", check=False)
+    assert r.returncode == 1 and "does not terminate" in r.stdout
+    assert dry("--interpolate", 0, "--points-rings", 2, 0)["interpolate"] == 0
+    r = run("--interpolate", 4, "--dry-run", check=False)
+    assert r.returncode == 1 and "not a mode" in r.stdout
 
 
 def brewer_rgb(values, vmin, vmax):

@@ -105,72 +105,45 @@ def test_far_field_matches_oracle(prec):
     assert np.linalg.norm(far_i) > 0
 
 
-PI_F = np.float32(3.14159)
 
-
-def rotate_fields(F, R, c, s, centre_int):
-    """nfInterpolate.cu:13-58 restated: F sampled at the pixel rotated about the centre, bilinear with
-    exact weights, zero outside; coordinates in float32, each operation rounded."""
-    uc = np.float32(int(R / 2.0)) if centre_int else np.float32(R / 2.0)
-    iu = np.arange(R, dtype=np.float32)[None, :]
-    iv = np.arange(R, dtype=np.float32)[:, None]
-    du, dv = iu - uc, iv - uc
-    nx = (uc + du * c) - dv * s
-    ny = (uc + du * s) + dv * c
-    fx, fy = np.floor(nx), np.floor(ny)
-    a = (nx - fx).astype(np.float64)
-    e = (ny - fy).astype(np.float64)
-    i0, j0 = fx.astype(np.int64), fy.astype(np.int64)
-
-    def at(i, j):
-        ok = (i >= 0) & (i < R) & (j >= 0) & (j < R)
-        return np.where(ok, F[np.clip(j, 0, R - 1), np.clip(i, 0, R - 1)], 0)
-    return ((1 - a) * (1 - e) * at(i0, j0) + a * (1 - e) * at(i0 + 1, j0) + (1 - a) * e * at(i0, j0 + 1)
-            + a * e * at(i0 + 1, j0 + 1))
+RING_CASES = [(3, 4, 3), (1, 4, 3), (2, 6, 3), (2, 8, 4), (3, 1, 2), (1, 5, 1)]
 
 
 @pytest.mark.parametrize("prec", [BS_PREC_FP64, BS_PREC_MIXED])
-def test_ring_interpolation_matches_oracle_restatement(prec):
-    """The reference's --interpolate 3: central source, then per ring the first source simulated and the
-    others imaged from its near field rotated by their own angles (the oracle's slices, rotated in numpy,
-    through the oracle's detector)."""
-    import ctypes as C
-    import math
-    points, rings = 4, 3
+@pytest.mark.parametrize("mode,points,rings", RING_CASES)
+def test_ring_sources_match_oracle(prec, mode, points, rings):
+    """The reference's --interpolate 1, 2, 3 (ring sources by rotated detector images, a radial line of
+    ring samples, rotated near fields) against the oracle's restatement of the same drivers.  Mode 2 with
+    6 points exercises the reference's tree sum, which leaves samples out for counts that are not powers
+    of two."""
     p = abi.make_params(lam=3.0, condenser=(0, 0.5), objective=(0, 0.5), xy=(14, 0), resolution=16, padding=1,
-                        us_lut_r=128, us_lut_theta=160)
+                        us_lut_r=128, us_lut_theta=160, focus=(0.5, -0.25, 0.0), amplitude=0.75)
     s = [(0.0, 0.0, 0.0, 2.0, 1.4, 0.04)]
     w = scenes.mc_waves(32, 0, 0.5, seed=15)
+    run = {1: "simulate_ring_detector", 2: "simulate_ring_line", 3: "simulate_ring_interp"}[mode]
     with Context(p) as ctx:
         ctx.set_spheres(s)
         ctx.set_waves(w)
-        ctx.simulate_ring_interp(points, rings, prec)
+        getattr(ctx, run)(points, rings, prec)
         D = ctx.image(BS_IMG_INTENSITY, f64=True)
         Di = ctx.image(BS_IMG_INCIDENT, f64=True)
-    ol = oracle_lib.load()
-    arr, ns = abi.sphere_array(s)
-    R = oracle_lib.geom(p).R
-    _, _, Do, Dio = oracle_lib.simulate(p, arr, ns, w)
-    Do, Dio = Do.copy(), Dio.copy()
-    step = np.float32(np.float32(2) * PI_F) / np.float32(points)
-    for ring in range(1, rings):
-        th = [step]
-        for _ in range(points - 1):
-            th.append(np.float32(th[-1] + step))
-        f0 = (float(np.float32(math.cos(float(th[0]))) * np.float32(ring)),
-              float(np.float32(math.sin(float(th[0]))) * np.float32(ring)), 0.0)
-        q = abi.make_params(lam=3.0, condenser=(0, 0.5), objective=(0, 0.5), xy=(14, 0), resolution=16, padding=1,
-                            us_lut_r=128, us_lut_theta=160, focus=f0, amplitude=1.0)
-        U, Uf, d, di = oracle_lib.simulate(q, arr, ns, w)
-        Do += d
-        Dio += di
-        for a in th[1:]:
-            c, sn = np.float32(math.cos(float(a))), np.float32(math.sin(float(a)))
-            Ur = np.ascontiguousarray(rotate_fields(U.reshape(R, R), R, c, sn, True), dtype=np.complex128)
-            Ufr = np.ascontiguousarray(rotate_fields(Uf.reshape(R, R), R, c, sn, False), dtype=np.complex128)
-            d1, di1 = np.zeros_like(Do), np.zeros_like(Dio)
-            ol.bso_detector(C.byref(p), Ur.ctypes.data_as(C.c_void_p), Ufr.ctypes.data_as(C.c_void_p),
-                            d1.ctypes.data_as(C.c_void_p), di1.ctypes.data_as(C.c_void_p))
-            Do += d1
-            Dio += di1
+        st = ctx.stats()
+        # the context's own focus and amplitude are kept for later runs
+        ctx.simulate(prec)
+        D1 = ctx.image(BS_IMG_INTENSITY, f64=True)
+    Do, Dio = oracle_lib.simulate_rings(p, *abi.sphere_array(s), w, mode, points, rings)
     assert rel(D, Do) <= TOL[prec] and rel(Di, Dio) <= TOL[prec], (rel(D, Do), rel(Di, Dio))
+    assert st.lut_tables_built == len(s)  # built for the first source only
+    _, _, d1, _ = oracle_lib.simulate(p, *abi.sphere_array(s), w)
+    assert rel(D1, d1) <= TOL[prec]
+
+
+def test_ring_line_point_limit():
+    p, s, w = scene()
+    with Context(p) as ctx:
+        ctx.set_spheres(s)
+        ctx.set_waves(w)
+        with pytest.raises(RuntimeError, match="at most 1023"):
+            ctx.simulate_ring_line(1024, 2, BS_PREC_MIXED)
+        with pytest.raises(RuntimeError, match=">= 1"):
+            ctx.simulate_ring_detector(0, 2, BS_PREC_MIXED)
