@@ -723,7 +723,7 @@ static double predict_staged_fraction(const bs_ctx* c, const std::vector<float4>
                     const int t_lo = std::max(0, (int)std::floor((thc - k.w - gam) * tsc) - 1);
                     const int t_hi = std::min(S.thetaR, (int)std::floor((thc + k.w + gam) * tsc) + 2);
                     const int W = t_hi - t_lo + 1;
-                    if (W >= 2 && (long long)nrows * W <= LUT_STAGE_ENTRIES) staged++;
+                    if (W >= 2 && (long long)nrows * lut_stage_stride(W) <= LUT_STAGE_ENTRIES) staged++;
                 }
             }
         }

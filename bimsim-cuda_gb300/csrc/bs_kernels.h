@@ -19,6 +19,9 @@ constexpr int WAVE_CHUNK = 64;
 constexpr int LUT_TILE = 16;
 constexpr int LUT_STAGE_ENTRIES = 5400;
 constexpr float LUT_STAGE_MARGIN = 2e-3f;
+// Shared-memory row stride of a staged window W entries wide: odd, so that
+// lanes reading the same column of different rows fall in different banks.
+__host__ __device__ constexpr int lut_stage_stride(int W) { return W | 1; }
 
 template <class T>
 struct cpx;

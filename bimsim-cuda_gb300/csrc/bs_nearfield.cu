@@ -589,7 +589,7 @@ __global__ void __launch_bounds__(UST_BLOCK, STAGE ? 4 : 6) us_lut_tex_kernel(Sc
             const int nw = min(UST_CHUNK, sc.nk - w0);
             __syncthreads();  // the previous chunk's readers are done; s_ts is written
             const int nrows = s_ts.nrows;
-            int t_lo = 0, W = 1;
+            int t_lo = 0, W = 1, Ws = 1;
             bool staged = false;
             if (STAGE && nrows > 0) {
                 const float4 cone = cones[ch];
@@ -599,7 +599,8 @@ __global__ void __launch_bounds__(UST_BLOCK, STAGE ? 4 : 6) us_lut_tex_kernel(Sc
                 t_lo = max(0, (int)floorf((thc - cone.w - gam) * tsc) - 1);
                 const int t_hi = min(s_ts.thetaR, (int)floorf((thc + cone.w + gam) * tsc) + 2);
                 W = t_hi - t_lo + 1;
-                staged = W >= 2 && nrows * W <= UST_STAGE;
+                Ws = lut_stage_stride(W);
+                staged = W >= 2 && nrows * Ws <= UST_STAGE;
             }
             if (threadIdx.x < nw) {
                 const cpx<float> pv = ph[(size_t)s * sc.nk + w0 + threadIdx.x];
@@ -612,7 +613,7 @@ __global__ void __launch_bounds__(UST_BLOCK, STAGE ? 4 : 6) us_lut_tex_kernel(Sc
                 const int ls = s_ts.lin_stride;
                 for (int rr = warp; rr < nrows; rr += UST_BLOCK / 32) {
                     const float2* src = table + (size_t)rr * ls;
-                    float2* dst = s_stage + rr * W;
+                    float2* dst = s_stage + rr * Ws;
                     for (int tt = lane; tt < W; tt += 32) copy_async8(dst + tt, src + tt);
                 }
                 copy_async_wait_all();
@@ -622,8 +623,8 @@ __global__ void __launch_bounds__(UST_BLOCK, STAGE ? 4 : 6) us_lut_tex_kernel(Sc
             float ar = 0.f, ai = 0.f;
             if (STAGE && staged) {
                 staged_chunks++;
-                const float2* row0 = s_stage + lr0 * W;
-                const int drow = (lr1 - lr0) * W;
+                const float2* row0 = s_stage + lr0 * Ws;
+                const int drow = (lr1 - lr0) * Ws;
                 const unsigned lt_max = (unsigned)(W - 2);
 #pragma unroll 1
                 for (int w = 0; w < nw; w++) {
