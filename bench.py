@@ -244,6 +244,7 @@ def run_gb300(args):
         us_ms.append(st.ms_us)
         launches += st.kernel_launches
     clocks = sampler.stop()
+    staged = st.lut_chunks_staged / st.lut_chunks_total if st.lut_chunks_total else 0.0
     total = sum(times)
     if dist:
         t = torch.tensor([total], device=dev)
@@ -354,6 +355,7 @@ def run_gb300(args):
                      "peak_source": "measured FP32 FMA loop on this GPU (bs_measure_fma_peak)",
                      "work": f"{FLOP_PER_LOOKUP} flop x {lookups} (pixel, sphere, wave) lookups per launch",
                      "launch_ms": us_s * 1e3, "lookups_per_s": lookups / us_s,
+                     "staged_fraction": staged,
                      "hbm_peak_gbs": peaks.get("hbm_gbs"), "fp64_peak_tflops": fp64_tf,
                      "why_not_hbm_or_tensor": "no step is a dense contraction (no tensor-core use) and the kernel "
                                               "reads 0.19 TB/s of DRAM: its bound is the FP32/L1 issue rate, so the "

@@ -78,6 +78,7 @@ struct Request {
     size_t est = 0;            // device bytes at its own table budget
     uint64_t lut_budget = 0;   // table budget the request runs with (0 = all tables at once)
     uint64_t sig = 0;
+    uint64_t shape = 0;        // sig, direction count and table budget: equal shapes allocate equal buffers
     int skipped = 0;
     int state = 0;             // 0 queued, 1 running, 2 done
     bs_status status = BS_OK;
@@ -92,7 +93,9 @@ struct Worker {
     std::thread th;
     bs_ctx* ctx = nullptr;
     uint64_t sig = 0;       // scene whose tables the context holds (0: none)
+    uint64_t shape = 0;     // shape of the last request the buffers were sized for (0: none)
     size_t bytes = 0;       // device bytes the context holds
+    size_t run_bytes = 0;   // bound on the device bytes while the current job runs
     Request* job = nullptr;
 };
 
@@ -116,12 +119,21 @@ struct bs_server {
     // Device bytes of every context, a busy one counted at least at its job's estimate.
     size_t in_use() const {
         size_t t = 0;
-        for (const auto& w : workers) t += w->job ? std::max(w->bytes, w->job->est) : w->bytes;
+        for (const auto& w : workers) t += w->job ? w->run_bytes : w->bytes;
         return t;
     }
 
+    // Bound on the device bytes of w's context while it runs r.  Buffers only
+    // grow, each to the larger of its held and needed size, so a request of
+    // another shape can leave the context with up to held + estimate bytes; one
+    // of the same shape needs no more than the larger of the two.
+    static size_t need(const Worker& w, const Request& r) {
+        if (w.bytes == 0) return r.est;
+        return r.shape == w.shape ? std::max(w.bytes, r.est) : w.bytes + r.est;
+    }
+
     bool fits(const Worker& w, const Request& r) const {
-        const size_t u = in_use() - w.bytes + std::max(w.bytes, r.est);
+        const size_t u = in_use() - w.bytes + need(w, r);
         return u <= budget;
     }
 
@@ -163,7 +175,7 @@ size_t bs_server::run(Worker& w, Request& r) {
         std::this_thread::sleep_for(std::chrono::milliseconds(1));
         r.out.assign((size_t)r.prm.resolution * r.prm.resolution, (float)r.id);
         r.status = BS_OK;
-        return std::max(w.bytes, r.est);
+        return w.run_bytes;  // what a context could hold afterwards: the admission bound
     }
     bs_ctx* c = w.ctx;
     cudaSetDevice(device);
@@ -207,6 +219,7 @@ void bs_server::loop(Worker& w) {
                 if (!cfg.dry_run) bs_release_buffers(w.ctx);
                 w.bytes = 0;
                 w.sig = 0;
+                w.shape = 0;
                 r = pick(w);
                 cv_work.notify_all();
                 return r != nullptr;
@@ -214,6 +227,7 @@ void bs_server::loop(Worker& w) {
             return false;
         });
         if (!r) return;  // stop
+        w.run_bytes = need(w, *r);
         w.job = r;
         r->state = 1;
         r->t_start = Clock::now();
@@ -229,6 +243,7 @@ void bs_server::loop(Worker& w) {
         r->info.status = r->status;
         r->info.worker = w.index;
         w.sig = r->status == BS_OK ? r->sig : 0;
+        w.shape = r->status == BS_OK ? r->shape : 0;
         w.job = nullptr;
         r->state = 2;
         running--;
@@ -370,6 +385,11 @@ bs_status bs_submit(bs_server* s, const bs_request* q, uint64_t* ticket) {
     }
     r->est = (size_t)est;
     r->sig = scene_signature(r->prm, r->spheres, r->prec);
+    {
+        uint64_t h = r->sig;
+        for (uint64_t v : {(uint64_t)(uint32_t)r->nk, (uint64_t)r->lut_budget}) h = (h ^ v) * 1099511628211ull;
+        r->shape = h;
+    }
     std::lock_guard<std::mutex> lk(s->mu);
     if (s->stop) return set_error(BS_ERR_STATE, "bs_submit: server is stopping");
     r->id = s->next_id++;

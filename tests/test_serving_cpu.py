@@ -72,6 +72,25 @@ def test_dry_run_budget_limits_concurrency():
         assert st.bytes_peak <= est + est // 2
 
 
+def test_requests_of_another_shape_count_held_plus_new_bytes():
+    # a context's buffers only grow, so after a request of another shape it may hold the union of
+    # both allocations: with a budget below the sum, the worker gives its buffers back first
+    a = scene(res=64, ns=3, nk=64)
+    b = scene(res=48, ns=4, nk=128, seed=5)
+    ea, eb = estimate_bytes(*a[:2], len(a[2])), estimate_bytes(*b[:2], len(b[2]))
+    budget = max(ea, eb) + min(ea, eb) // 2
+    with Server(workers=1, hbm_budget=budget, dry_run=True) as srv:
+        tickets = [srv.submit(*(a if i % 2 == 0 else b)[:2], waves=(a if i % 2 == 0 else b)[2]) for i in range(6)]
+        for t in tickets:
+            srv.wait(t, 10.0)
+        assert srv.stats().completed == 6 and srv.stats().bytes_peak <= budget
+    with Server(workers=1, hbm_budget=ea + eb, dry_run=True) as srv:
+        tickets = [srv.submit(*(a if i % 2 == 0 else b)[:2], waves=(a if i % 2 == 0 else b)[2]) for i in range(4)]
+        for t in tickets:
+            srv.wait(t, 10.0)
+        assert srv.stats().bytes_peak > max(ea, eb)  # room for both: the buffers stay and grow
+
+
 def test_request_larger_than_budget_is_rejected_or_chunked():
     p, s, w = scene(ns=4)
     full = estimate_bytes(p, s, len(w))
