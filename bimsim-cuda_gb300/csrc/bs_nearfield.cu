@@ -459,7 +459,7 @@ constexpr float UST_MARGIN = LUT_STAGE_MARGIN;
 struct TileSphere {
     float cx, cy, cz;  // unit direction from the sphere to the tile centre
     float gam;         // angular radius of the tile seen from the sphere, plus margin
-    float tsc, tscpi, tmax;
+    float tsc, tscpi;
     int rlo, nrows;    // staged table rows [rlo, rlo + nrows); nrows = 0: texture path only
     int thetaR, lin_stride;
     long long off;     // first entry of the table in the linear pool
@@ -523,7 +523,6 @@ __global__ void __launch_bounds__(UST_BLOCK, STAGE ? 4 : 6) us_lut_tex_kernel(Sc
             if (threadIdx.x == 0) {
                 s_ts.tsc = (float)((S.thetaR - 1) / PI_REF);
                 s_ts.tscpi = (float)((S.thetaR - 1) / PI_REF * TRUE_PI);
-                s_ts.tmax = (float)(S.thetaR - 1);
                 s_ts.nrows = 0;
             }
         } else {
@@ -571,7 +570,6 @@ __global__ void __launch_bounds__(UST_BLOCK, STAGE ? 4 : 6) us_lut_tex_kernel(Sc
                 s_ts.gam = __int_as_float(gbits) + UST_MARGIN;
                 s_ts.tsc = (float)((S.thetaR - 1) / PI_REF);
                 s_ts.tscpi = (float)((S.thetaR - 1) / PI_REF * TRUE_PI);
-                s_ts.tmax = (float)(S.thetaR - 1);
                 // staged rows: [rlo, rhi + 1] clamped to the table
                 s_ts.rlo = rlo;
                 s_ts.nrows = ok ? min(rhi + 1, ts.rows - 1) - rlo + 1 : 0;
@@ -619,7 +617,9 @@ __global__ void __launch_bounds__(UST_BLOCK, STAGE ? 4 : 6) us_lut_tex_kernel(Sc
                 copy_async_wait_all();
             }
             __syncthreads();
-            const float tsc = s_ts.tsc, tscpi = s_ts.tscpi, tmax = s_ts.tmax;
+            // t < thetaR - 1 + 1e-3 (PI_REF < pi): the last column is repeated in the staged rows and
+            // clamped in the texture planes, so t past thetaR - 1 reads the last column, as a clamp would
+            const float tsc = s_ts.tsc, tscpi = s_ts.tscpi;
             float ar = 0.f, ai = 0.f;
             if (STAGE && staged) {
                 staged_chunks++;
@@ -630,7 +630,7 @@ __global__ void __launch_bounds__(UST_BLOCK, STAGE ? 4 : 6) us_lut_tex_kernel(Sc
                 for (int w = 0; w < nw; w++) {
                     const float4 kk = s_k[w];
                     const float c = fmaf(kk.x, rx, fmaf(kk.y, ry, kk.z * rz));  // cb = 0: every d > 0 here
-                    const float t = fminf(theta_index(c, tsc, tscpi), tmax);
+                    const float t = theta_index(c, tsc, tscpi);
                     const float tf = floorf(t);
                     const float be = t - tf;
                     // in the window by construction; the unsigned clamp only keeps a bad bound in bounds
@@ -650,7 +650,7 @@ __global__ void __launch_bounds__(UST_BLOCK, STAGE ? 4 : 6) us_lut_tex_kernel(Sc
                 for (int w = 0; w < nw; w++) {
                     const float4 kk = s_k[w];
                     const float c = fmaf(kk.x, rx, fmaf(kk.y, ry, fmaf(kk.z, rz, cb)));
-                    const float t = fminf(theta_index(c, tsc, tscpi), tmax);
+                    const float t = theta_index(c, tsc, tscpi);
                     const float tf = floorf(t);
                     const float be = t - tf;
                     const float4 gr = tex2Dgather<float4>(tre, tf + 1.0f, y, 0);
