@@ -369,6 +369,8 @@ static bs_status derive(bs_ctx* c) {
         S.dR = p.us_lut_r > 0 ? p.us_lut_r : 2 * c->R;
         S.thetaR = p.us_lut_theta > 0 ? p.us_lut_theta : 1000;
         S.r0 = std::max(in.a, S.dmin);
+        S.xs_usp = (S.dR - 1) / (S.dmax - S.r0);
+        S.xs_uip = (S.aR - 1) / (S.a - S.dmin);
         S.coef_off = coef;
         coef += S.Nl + 1;
         c->Lmax = std::max(c->Lmax, S.Nl + 1);

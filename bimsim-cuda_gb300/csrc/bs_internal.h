@@ -56,6 +56,7 @@ struct Sphere {
     int64_t uip_off;         // first patch of Uip in the LUT pool
     int coef_off;            // first order of this sphere in the coefficient arrays
     int lin_stride;          // mixed path: row stride of the linear float2 tables (thetaR + 1, even)
+    double xs_usp, xs_uip;   // (dR - 1) / (dmax - r0) and (aR - 1) / (a - dmin): radial index scales
 };
 
 // Host helpers (bs_host.cpp).

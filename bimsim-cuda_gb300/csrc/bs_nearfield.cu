@@ -339,6 +339,24 @@ __device__ __forceinline__ TableSel select_table(const Sphere& S, double d) {
     return t;
 }
 
+// select_table with the per-sphere scales (rows - 1) / (range) of the host in
+// place of the division: the index may differ in its last bit, which moves a
+// sample across a row boundary only where the bilinear value is continuous.
+__device__ __forceinline__ TableSel select_table_scaled(const Sphere& S, double d) {
+    TableSel t;
+    if (d < S.a) {
+        t.off = S.uip_off;
+        t.rows = S.aR;
+        t.x = (d - S.dmin) * S.xs_uip;
+    } else {
+        t.off = S.usp_off;
+        t.rows = S.dR;
+        t.x = (d - S.r0) * S.xs_usp;
+    }
+    t.x = fmin(fmax(t.x, 0.0), (double)(t.rows - 1));
+    return t;
+}
+
 // plain double precision, one pixel per thread
 __global__ void __launch_bounds__(128) us_lut_f64_kernel(Scene sc, const Sphere* __restrict__ sph, int s0, int s1,
                                                           int accumulate, int finalize,
@@ -448,6 +466,11 @@ __device__ __forceinline__ void copy_async8(float2* dst, const float2* src) {
     asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src) : "memory");
 }
 
+__device__ __forceinline__ void copy_async16(float4* dst, const float4* src) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(src) : "memory");
+}
+
 __device__ __forceinline__ void copy_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 constexpr int UST_CHUNK = WAVE_CHUNK;
 constexpr int UST_STAGE = LUT_STAGE_ENTRIES;
@@ -464,6 +487,21 @@ struct TileSphere {
     int thetaR, lin_stride;
     long long off;     // first entry of the table in the linear pool
 };
+
+// Window of a wave chunk with bounding cone `cone` for the block's (tile, sphere):
+// first column and width, width 0 when the block does not stage this sphere or
+// the window does not fit.  Columns go up to thetaR: the linear rows carry a
+// copy of the last column there.
+__device__ __forceinline__ int2 chunk_plan(const float4 cone, const TileSphere& ts) {
+    if (ts.nrows == 0) return make_int2(0, 0);
+    const float tsc = ts.tsc, gam = ts.gam;
+    const float thc = acosf(fminf(fmaxf(cone.x * ts.cx + cone.y * ts.cy + cone.z * ts.cz, -1.f), 1.f));
+    const int t_lo = max(0, (int)floorf((thc - cone.w - gam) * tsc) - 1);
+    const int t_hi = min(ts.thetaR, (int)floorf((thc + cone.w + gam) * tsc) + 2);
+    int W = t_hi - t_lo + 1;
+    if (W < 2 || ts.nrows * lut_stage_stride(W) > UST_STAGE) W = 0;
+    return make_int2(t_lo, W);
+}
 
 // STAGE = false: texture path only, no dynamic shared memory (the L1 keeps
 // its full size for the texture cache) and 6 blocks per SM.
@@ -483,6 +521,8 @@ __global__ void __launch_bounds__(UST_BLOCK, STAGE ? 4 : 6) us_lut_tex_kernel(Sc
     __shared__ float2 s_p[UST_CHUNK];
     __shared__ int s_red[4][UST_BLOCK / 32];
     __shared__ TileSphere s_ts;
+    __shared__ int2 s_plan;  // staged window of the next chunk: first column, width (0: texture path)
+    __shared__ double s_pa[3][16], s_pb[3][16];  // pixel position = s_pa[.][column] + s_pb[.][row]
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     // each warp covers an 8 x 4 pixel block of the 16 x 16 tile
     const int tiles_u = (sc.R + 15) / 16;
@@ -490,6 +530,18 @@ __global__ void __launch_bounds__(UST_BLOCK, STAGE ? 4 : 6) us_lut_tex_kernel(Sc
     const int iu = tu + (lane & 7) + 8 * (warp & 1);
     const int iv = tv + (lane >> 3) + 4 * (warp >> 1);
     const bool valid = iu < sc.R && iv < sc.R;
+    // pixel_pos computes (A + X u) + Y v: the terms of the tile's 16 columns and 16 rows, once
+    if (threadIdx.x < 32) {
+        const int k = threadIdx.x & 15;
+        const double t = __ddiv_rn((double)min((threadIdx.x < 16 ? tu : tv) + k, sc.R - 1), (double)sc.R);
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            if (threadIdx.x < 16) s_pa[c][k] = __dadd_rn(sc.A[c], __dmul_rn(sc.X[c], t));
+            else s_pb[c][k] = __dmul_rn(sc.Y[c], t);
+        }
+    }
+    __syncthreads();
+    const int lu = min(iu, sc.R - 1) - tu, lv = min(iv, sc.R - 1) - tv;
     float tot_r = 0.f, tot_i = 0.f, cmp_r = 0.f, cmp_i = 0.f;  // Kahan sum over chunk partials
     if (accumulate && valid) {
         tot_r = U[iv * sc.R + iu].re;
@@ -500,9 +552,10 @@ __global__ void __launch_bounds__(UST_BLOCK, STAGE ? 4 : 6) us_lut_tex_kernel(Sc
     for (int s = s0; s < s1; s++) {
         const Sphere& S = sph[s];
         double p[3], r[3];
-        pixel_pos(sc, min(iu, sc.R - 1), min(iv, sc.R - 1), p);
+#pragma unroll
+        for (int c = 0; c < 3; c++) p[c] = __dadd_rn(s_pa[c][lu], s_pb[c][lv]);
         const double d = dist_exact(p, S.p, r);
-        const TableSel ts = select_table(S, d);
+        const TableSel ts = select_table_scaled(S, d);
         const int ir = (int)floor(ts.x);
         const float al = (float)(ts.x - ir);
         const float y = (float)ir + 1.0f;  // gather footprint rows ir, ir + 1
@@ -510,10 +563,10 @@ __global__ void __launch_bounds__(UST_BLOCK, STAGE ? 4 : 6) us_lut_tex_kernel(Sc
         const cudaTextureObject_t tre = tex[k], tim = tex[k + 1];
         float rx = 0.f, ry = 0.f, rz = 0.f, cb = 1.f;  // d == 0: cos(theta) := 1
         if (d != 0) {
-            const double inv = 1.0 / d;
-            rx = (float)(r[0] * inv);
-            ry = (float)(r[1] * inv);
-            rz = (float)(r[2] * inv);
+            const float inv = 1.f / (float)d;
+            rx = (float)r[0] * inv;
+            ry = (float)r[1] * inv;
+            rz = (float)r[2] * inv;
             cb = 0.f;
         }
         // ---- tile bounds: table rows and angular radius gamma ----
@@ -576,6 +629,7 @@ __global__ void __launch_bounds__(UST_BLOCK, STAGE ? 4 : 6) us_lut_tex_kernel(Sc
                 s_ts.thetaR = S.thetaR;
                 s_ts.lin_stride = S.lin_stride;
                 s_ts.off = ts.off;
+                s_plan = chunk_plan(cones[0], s_ts);
             }
         }
         // local rows of this pixel in the staged block (clamped, so always in bounds)
@@ -587,23 +641,14 @@ __global__ void __launch_bounds__(UST_BLOCK, STAGE ? 4 : 6) us_lut_tex_kernel(Sc
             const int nw = min(UST_CHUNK, sc.nk - w0);
             __syncthreads();  // the previous chunk's readers are done; s_ts is written
             const int nrows = s_ts.nrows;
-            int t_lo = 0, W = 1, Ws = 1;
-            bool staged = false;
-            if (STAGE && nrows > 0) {
-                const float4 cone = cones[ch];
-                const float tsc = s_ts.tsc, gam = s_ts.gam;
-                const float thc = acosf(fminf(fmaxf(cone.x * s_ts.cx + cone.y * s_ts.cy + cone.z * s_ts.cz, -1.f), 1.f));
-                // columns up to thetaR: the linear rows carry a copy of the last column there
-                t_lo = max(0, (int)floorf((thc - cone.w - gam) * tsc) - 1);
-                const int t_hi = min(s_ts.thetaR, (int)floorf((thc + cone.w + gam) * tsc) + 2);
-                W = t_hi - t_lo + 1;
-                Ws = lut_stage_stride(W);
-                staged = W >= 2 && nrows * Ws <= UST_STAGE;
-            }
+            // window of this chunk: planned by thread 0 (before the first chunk, or while the
+            // previous chunk was summed)
+            const int2 pl = STAGE ? s_plan : make_int2(0, 0);
+            const int t_lo = pl.x, W = pl.y, Ws = lut_stage_stride(W);
+            const bool staged = STAGE && W > 0;
             if (threadIdx.x < nw) {
-                const cpx<float> pv = ph[(size_t)s * sc.nk + w0 + threadIdx.x];
-                s_k[threadIdx.x] = kw4[w0 + threadIdx.x];
-                s_p[threadIdx.x] = make_float2(pv.re, pv.im);
+                copy_async16(&s_k[threadIdx.x], kw4 + w0 + threadIdx.x);
+                copy_async8(&s_p[threadIdx.x], reinterpret_cast<const float2*>(ph + (size_t)s * sc.nk + w0) + threadIdx.x);
             }
             if (STAGE && staged) {
                 // asynchronous copies, one table row per warp at a time, all in flight together
@@ -614,9 +659,10 @@ __global__ void __launch_bounds__(UST_BLOCK, STAGE ? 4 : 6) us_lut_tex_kernel(Sc
                     float2* dst = s_stage + rr * Ws;
                     for (int tt = lane; tt < W; tt += 32) copy_async8(dst + tt, src + tt);
                 }
-                copy_async_wait_all();
             }
+            copy_async_wait_all();
             __syncthreads();
+            if (STAGE && threadIdx.x == 0 && ch + 1 < nchunks) s_plan = chunk_plan(cones[ch + 1], s_ts);
             // t < thetaR - 1 + 1e-3 (PI_REF < pi): the last column is repeated in the staged rows and
             // clamped in the texture planes, so t past thetaR - 1 reads the last column, as a clamp would
             const float tsc = s_ts.tsc, tscpi = s_ts.tscpi;
@@ -681,10 +727,15 @@ __global__ void __launch_bounds__(UST_BLOCK, STAGE ? 4 : 6) us_lut_tex_kernel(Sc
     const int idx = iv * sc.R + iu;
     if (finalize) {
         double p[3];
-        pixel_pos(sc, iu, iv, p);
+#pragma unroll
+        for (int c = 0; c < 3; c++) p[c] = __dadd_rn(s_pa[c][lu], s_pb[c][lv]);
         bool outside = true;
-        for (int s = 0; s < sc.ns; s++) {
+        for (int s = 0; s < sc.ns && outside; s++) {
             const Sphere& S = sph[s];
+            // clearly outside in single precision (0.1 % margin on d^2), else the exact test
+            const float dx = (float)(p[0] - S.p[0]), dy = (float)(p[1] - S.p[1]), dz = (float)(p[2] - S.p[2]);
+            const float af = (float)S.a;
+            if (dx * dx + dy * dy + dz * dz > 1.001f * af * af) continue;
             double r[3];
             if (dist_exact(p, S.p, r) < S.a) outside = false;
         }
