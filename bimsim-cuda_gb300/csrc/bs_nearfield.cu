@@ -471,6 +471,36 @@ __device__ __forceinline__ void copy_async16(float4* dst, const float4* src) {
     asm volatile("cp.async.ca.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(src) : "memory");
 }
 
+__device__ __forceinline__ void copy_async4(float* dst, const float* src) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src) : "memory");
+}
+
+// Two single-precision lanes in one 64-bit register pair (low lane first), worked
+// on by Blackwell's packed f32x2 instructions; each lane rounds exactly like the
+// scalar instruction (round to nearest, no flush).
+typedef unsigned long long f32x2;
+__device__ __forceinline__ f32x2 f2_splat(float a) {
+    f32x2 r;
+    asm("mov.b64 %0, {%1, %1};" : "=l"(r) : "f"(a));
+    return r;
+}
+__device__ __forceinline__ f32x2 f2_sub(f32x2 a, f32x2 b) {
+    f32x2 r;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f32x2 f2_fma(f32x2 a, f32x2 b, f32x2 c) {
+    f32x2 r;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+    return r;
+}
+__device__ __forceinline__ float2 f2_unpack(f32x2 v) {
+    float2 r;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(r.x), "=f"(r.y) : "l"(v));
+    return r;
+}
+
 __device__ __forceinline__ void copy_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 constexpr int UST_CHUNK = WAVE_CHUNK;
 constexpr int UST_STAGE = LUT_STAGE_ENTRIES;
@@ -518,7 +548,7 @@ __global__ void __launch_bounds__(UST_BLOCK, STAGE ? 4 : 6) us_lut_tex_kernel(Sc
                                                                     unsigned long long* __restrict__ counters) {
     extern __shared__ float2 s_stage[];
     __shared__ float4 s_k[UST_CHUNK];
-    __shared__ float2 s_p[UST_CHUNK];
+    __shared__ float4 s_p[UST_CHUNK];  // phase (x, x, y, y): lane pairs for the packed products
     __shared__ int s_red[4][UST_BLOCK / 32];
     __shared__ TileSphere s_ts;
     __shared__ int2 s_plan;  // staged window of the next chunk: first column, width (0: texture path)
@@ -648,7 +678,12 @@ __global__ void __launch_bounds__(UST_BLOCK, STAGE ? 4 : 6) us_lut_tex_kernel(Sc
             const bool staged = STAGE && W > 0;
             if (threadIdx.x < nw) {
                 copy_async16(&s_k[threadIdx.x], kw4 + w0 + threadIdx.x);
-                copy_async8(&s_p[threadIdx.x], reinterpret_cast<const float2*>(ph + (size_t)s * sc.nk + w0) + threadIdx.x);
+                const float* pv = reinterpret_cast<const float*>(ph + (size_t)s * sc.nk + w0 + threadIdx.x);
+                float* dp = reinterpret_cast<float*>(&s_p[threadIdx.x]);
+                copy_async4(dp, pv);
+                copy_async4(dp + 1, pv);
+                copy_async4(dp + 2, pv + 1);
+                copy_async4(dp + 3, pv + 1);
             }
             if (STAGE && staged) {
                 // asynchronous copies, one table row per warp at a time, all in flight together
@@ -666,13 +701,17 @@ __global__ void __launch_bounds__(UST_BLOCK, STAGE ? 4 : 6) us_lut_tex_kernel(Sc
             // t < thetaR - 1 + 1e-3 (PI_REF < pi): the last column is repeated in the staged rows and
             // clamped in the texture planes, so t past thetaR - 1 reads the last column, as a clamp would
             const float tsc = s_ts.tsc, tscpi = s_ts.tscpi;
-            float ar = 0.f, ai = 0.f;
+            // the chunk's sum of pw v as sum(pw.x v) and sum(pw.y v), each a (re, im) pair:
+            // Re = x.re - y.im, Im = x.im + y.re
+            float2 sx, sy;
             if (STAGE && staged) {
                 staged_chunks++;
                 const float2* row0 = s_stage + lr0 * Ws;
                 const int drow = (lr1 - lr0) * Ws;
                 const unsigned lt_max = (unsigned)(W - 2);
-#pragma unroll 1
+                const f32x2 alp = f2_splat(al);
+                f32x2 ax = 0ull, ay = 0ull;
+#pragma unroll 8
                 for (int w = 0; w < nw; w++) {
                     const float4 kk = s_k[w];
                     const float c = fmaf(kk.x, rx, fmaf(kk.y, ry, kk.z * rz));  // cb = 0: every d > 0 here
@@ -681,17 +720,20 @@ __global__ void __launch_bounds__(UST_BLOCK, STAGE ? 4 : 6) us_lut_tex_kernel(Sc
                     const float be = t - tf;
                     // in the window by construction; the unsigned clamp only keeps a bad bound in bounds
                     const unsigned lt = min((unsigned)((int)tf - t_lo), lt_max);
-                    const float2* q = row0 + lt;
-                    const float2 e00 = q[0], e01 = q[1], e10 = q[drow], e11 = q[drow + 1];
-                    const float ar0 = fmaf(be, e01.x - e00.x, e00.x), ar1 = fmaf(be, e11.x - e10.x, e10.x);
-                    const float ai0 = fmaf(be, e01.y - e00.y, e00.y), ai1 = fmaf(be, e11.y - e10.y, e10.y);
-                    const float vr = fmaf(al, ar1 - ar0, ar0);
-                    const float vi = fmaf(al, ai1 - ai0, ai0);
-                    const float2 pw = s_p[w];
-                    ar = fmaf(pw.x, vr, fmaf(-pw.y, vi, ar));
-                    ai = fmaf(pw.x, vi, fmaf(pw.y, vr, ai));
+                    const f32x2* q = reinterpret_cast<const f32x2*>(row0 + lt);
+                    const f32x2 e00 = q[0], e01 = q[1], e10 = q[drow], e11 = q[drow + 1];
+                    const f32x2 bep = f2_splat(be);
+                    const f32x2 a0 = f2_fma(bep, f2_sub(e01, e00), e00);
+                    const f32x2 a1 = f2_fma(bep, f2_sub(e11, e10), e10);
+                    const f32x2 v = f2_fma(alp, f2_sub(a1, a0), a0);
+                    const ulonglong2 pw = reinterpret_cast<const ulonglong2*>(s_p)[w];  // (x, x), (y, y)
+                    ax = f2_fma(pw.x, v, ax);
+                    ay = f2_fma(pw.y, v, ay);
                 }
+                sx = f2_unpack(ax);
+                sy = f2_unpack(ay);
             } else {
+                sx = sy = make_float2(0.f, 0.f);
 #pragma unroll 1
                 for (int w = 0; w < nw; w++) {
                     const float4 kk = s_k[w];
@@ -705,11 +747,14 @@ __global__ void __launch_bounds__(UST_BLOCK, STAGE ? 4 : 6) us_lut_tex_kernel(Sc
                     const float ai0 = fmaf(be, gi.z - gi.w, gi.w), ai1 = fmaf(be, gi.y - gi.x, gi.x);
                     const float vr = fmaf(al, ar1 - ar0, ar0);
                     const float vi = fmaf(al, ai1 - ai0, ai0);
-                    const float2 pw = s_p[w];
-                    ar = fmaf(pw.x, vr, fmaf(-pw.y, vi, ar));
-                    ai = fmaf(pw.x, vi, fmaf(pw.y, vr, ai));
+                    const float4 pw = s_p[w];
+                    sx.x = fmaf(pw.x, vr, sx.x);
+                    sx.y = fmaf(pw.x, vi, sx.y);
+                    sy.x = fmaf(pw.z, vr, sy.x);
+                    sy.y = fmaf(pw.z, vi, sy.y);
                 }
             }
+            const float ar = sx.x - sy.y, ai = sx.y + sy.x;
             // Kahan: add the chunk partial to the running total
             const float yr = ar - cmp_r, yi = ai - cmp_i;
             const float tr = tot_r + yr, ti = tot_i + yi;
