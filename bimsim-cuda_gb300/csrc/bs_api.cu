@@ -565,27 +565,35 @@ static bs_status plan_luts(bs_ctx* c, bool mixed, std::vector<int>& chunk_start,
     return plan_tables(c->hs, mixed, budget, chunk_start, pool, maxrows, maxL);
 }
 
-// Order plane waves along a Hilbert curve of their projection on the plane
-// perpendicular to the mean direction.  The sum over waves does not depend
-// on the order (up to rounding), but neighbouring waves then give
-// neighbouring LUT angles for every pixel, which keeps each block's LUT
-// working set small enough for the L1 cache.
-static uint32_t hilbert_d(uint32_t n, uint32_t x, uint32_t y) {
-    uint32_t d = 0;
-    for (uint32_t s = n / 2; s > 0; s /= 2) {
-        uint32_t rx = (x & s) > 0, ry = (y & s) > 0;
-        d += s * s * ((3 * rx) ^ ry);
-        if (ry == 0) {
-            if (rx == 1) {
-                x = s - 1 - x;
-                y = s - 1 - y;
-            }
-            uint32_t t = x;
-            x = y;
-            y = t;
-        }
+// Order plane waves in compact groups of WAVE_CHUNK: their projections on the
+// plane perpendicular to the mean direction are split recursively at a
+// multiple of WAVE_CHUNK along the wider axis (a median split when the count
+// allows), so every group but one holds WAVE_CHUNK waves and the one short
+// group goes last.  The sum over waves does not depend on the order (up to
+// rounding); compact groups have narrow bounding cones, so each tile's table
+// window per group stays small enough for shared memory (on the config-2 scene
+// 98-99.7 % of windows fit, against 60-86 % for chunks cut from a Hilbert
+// curve order, whose chunks can straddle the curve's jumps).
+static void group_split(std::vector<size_t>& idx, size_t lo, size_t hi, const std::vector<double>& px,
+                        const std::vector<double>& py, std::vector<std::pair<size_t, size_t>>& groups) {
+    const size_t n = hi - lo;
+    if (n <= (size_t)WAVE_CHUNK) {
+        groups.push_back({lo, hi});
+        return;
     }
-    return d;
+    double x0 = px[idx[lo]], x1 = x0, y0 = py[idx[lo]], y1 = y0;
+    for (size_t i = lo; i < hi; i++) {
+        x0 = std::min(x0, px[idx[i]]);
+        x1 = std::max(x1, px[idx[i]]);
+        y0 = std::min(y0, py[idx[i]]);
+        y1 = std::max(y1, py[idx[i]]);
+    }
+    const std::vector<double>& key = (x1 - x0 >= y1 - y0) ? px : py;
+    std::stable_sort(idx.begin() + lo, idx.begin() + hi, [&key](size_t a, size_t b) { return key[a] < key[b]; });
+    const size_t half = (size_t)std::llround((double)n / (2.0 * WAVE_CHUNK));
+    const size_t k = (size_t)WAVE_CHUNK * std::max<size_t>(1, half);
+    group_split(idx, lo, lo + k, px, py, groups);
+    group_split(idx, lo + k, hi, px, py, groups);
 }
 
 static void sort_waves(std::vector<double>& w) {
@@ -603,20 +611,23 @@ static void sort_waves(std::vector<double>& w) {
     double l1 = std::sqrt(e1[0] * e1[0] + e1[1] * e1[1] + e1[2] * e1[2]);
     for (int c = 0; c < 3; c++) e1[c] /= l1;
     double e2[3] = {m[1] * e1[2] - m[2] * e1[1], m[2] * e1[0] - m[0] * e1[2], m[0] * e1[1] - m[1] * e1[0]};
-    std::vector<std::pair<uint32_t, size_t>> key(nk);
-    const uint32_t G = 1024;
+    std::vector<double> px(nk), py(nk);
+    std::vector<size_t> idx(nk);
     for (size_t i = 0; i < nk; i++) {
         const double* k = &w[3 * i];
-        double x = k[0] * e1[0] + k[1] * e1[1] + k[2] * e1[2];
-        double y = k[0] * e2[0] + k[1] * e2[1] + k[2] * e2[2];
-        uint32_t gx = (uint32_t)std::min<double>(G - 1, std::max(0.0, (x + 1.0) * 0.5 * G));
-        uint32_t gy = (uint32_t)std::min<double>(G - 1, std::max(0.0, (y + 1.0) * 0.5 * G));
-        key[i] = {hilbert_d(G, gx, gy), i};
+        px[i] = k[0] * e1[0] + k[1] * e1[1] + k[2] * e1[2];
+        py[i] = k[0] * e2[0] + k[1] * e2[1] + k[2] * e2[2];
+        idx[i] = i;
     }
-    std::stable_sort(key.begin(), key.end());
-    std::vector<double> out(w.size());
-    for (size_t i = 0; i < nk; i++)
-        for (int c = 0; c < 3; c++) out[3 * i + c] = w[3 * key[i].second + c];
+    std::vector<std::pair<size_t, size_t>> groups;
+    group_split(idx, 0, nk, px, py, groups);
+    std::stable_partition(groups.begin(), groups.end(),
+                          [](const std::pair<size_t, size_t>& g) { return g.second - g.first == (size_t)WAVE_CHUNK; });
+    std::vector<double> out;
+    out.reserve(w.size());
+    for (const auto& g : groups)
+        for (size_t i = g.first; i < g.second; i++)
+            for (int c = 0; c < 3; c++) out.push_back(w[3 * idx[i] + c]);
     w.swap(out);
 }
 

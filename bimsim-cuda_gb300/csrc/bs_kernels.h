@@ -11,7 +11,7 @@ namespace bs {
 
 // Plane waves are processed in chunks of this many (after a Hilbert-curve
 // sort); the host supplies one bounding cone per chunk.
-constexpr int WAVE_CHUNK = 40;
+constexpr int WAVE_CHUNK = 64;
 
 // Mixed LUT kernel staging: float2 table values a 16 x 16 pixel tile stages
 // per wave chunk (43 KB of shared memory, 4 blocks per SM), and the angle

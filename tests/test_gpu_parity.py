@@ -141,8 +141,8 @@ def test_mixed_lut_kernel_uses_both_table_paths():
     st = g["stats"]
     p, s, w = scene("lut_staged")
     tiles = (oracle_lib.geom(p).R + 15) // 16
-    # tiles of 16 x 16 near-field pixels x spheres x wave chunks of 40
-    assert st.lut_chunks_total == tiles * tiles * len(s) * ((len(w) + 39) // 40)
+    # tiles of 16 x 16 near-field pixels x spheres x wave chunks of 64
+    assert st.lut_chunks_total == tiles * tiles * len(s) * ((len(w) + 63) // 64)
     assert 0 < st.lut_chunks_staged < st.lut_chunks_total, (st.lut_chunks_staged, st.lut_chunks_total)
     g64 = run_gpu("lut_staged", BS_PREC_FP64)
     assert g64["stats"].lut_chunks_total == 0
