@@ -57,7 +57,8 @@ class Stats(C.Structure):
                 ("ms_lut", C.c_double), ("ms_us", C.c_double), ("ms_detector", C.c_double),
                 ("kernel_launches", C.c_int64), ("us_interactions", C.c_int64),
                 ("lut_chunks_staged", C.c_int64), ("lut_chunks_total", C.c_int64),
-                ("lut_tables_built", C.c_int64), ("lut_staged_predicted", C.c_double)]
+                ("lut_tables_built", C.c_int64), ("lut_staged_predicted", C.c_double),
+                ("lut_wave_chunk", C.c_int64)]
 
 
 class ServerConfig(C.Structure):

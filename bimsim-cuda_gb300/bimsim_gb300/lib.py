@@ -62,6 +62,7 @@ def library():
         "bs_material_eval": ([C.c_char_p, vp, i32, vp], C.c_int),
         "bs_set_lut_reuse": ([vp, i32], C.c_int),
         "bs_set_lut_staging": ([vp, i32], C.c_int),
+    "bs_set_lut_wave_chunk": ([vp, i32], C.c_int),
         "bs_release_buffers": ([vp], C.c_int),
         "bs_estimate_bytes": ([vp, vp, i32, i32, C.c_int, C.c_uint64, C.POINTER(C.c_uint64)], C.c_int),
         "bs_server_create": ([vp, C.POINTER(vp)], C.c_int),
@@ -225,6 +226,10 @@ class Context:
     def set_lut_staging(self, mode):
         """0 model-chosen, 1 staged kernel, 2 texture-only kernel (same results)."""
         self._check(self.lib.bs_set_lut_staging(self.h, mode))
+
+    def set_lut_wave_chunk(self, chunk):
+        """Waves per chunk of the mixed LUT kernel: 0 chooses per run, else 16, 32 or 64."""
+        self._check(self.lib.bs_set_lut_wave_chunk(self.h, chunk))
 
     def set_lut_reuse(self, enable):
         self._check(self.lib.bs_set_lut_reuse(self.h, 1 if enable else 0))

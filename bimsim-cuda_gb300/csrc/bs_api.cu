@@ -183,6 +183,7 @@ struct bs_ctx {
     // table reuse between runs (bs_set_lut_reuse)
     bool reuse = false;
     int lut_staging = 0;  // bs_set_lut_staging: 0 model-chosen, 1 staged kernel, 2 texture-only kernel
+    int lut_chunk = 0;    // bs_set_lut_wave_chunk: 0 model-chosen, else waves per chunk
     bool lut_valid = false;
     std::vector<double> lut_key;
 };
@@ -565,19 +566,19 @@ static bs_status plan_luts(bs_ctx* c, bool mixed, std::vector<int>& chunk_start,
     return plan_tables(c->hs, mixed, budget, chunk_start, pool, maxrows, maxL);
 }
 
-// Order plane waves in compact groups of WAVE_CHUNK: their projections on the
+// Order plane waves in compact groups of `chunk`: their projections on the
 // plane perpendicular to the mean direction are split recursively at a
-// multiple of WAVE_CHUNK along the wider axis (a median split when the count
-// allows), so every group but one holds WAVE_CHUNK waves and the one short
+// multiple of `chunk` along the wider axis (a median split when the count
+// allows), so every group but one holds `chunk` waves and the one short
 // group goes last.  The sum over waves does not depend on the order (up to
 // rounding); compact groups have narrow bounding cones, so each tile's table
 // window per group stays small enough for shared memory (on the config-2 scene
 // 98-99.7 % of windows fit, against 60-86 % for chunks cut from a Hilbert
 // curve order, whose chunks can straddle the curve's jumps).
 static void group_split(std::vector<size_t>& idx, size_t lo, size_t hi, const std::vector<double>& px,
-                        const std::vector<double>& py, std::vector<std::pair<size_t, size_t>>& groups) {
+                        const std::vector<double>& py, size_t chunk, std::vector<std::pair<size_t, size_t>>& groups) {
     const size_t n = hi - lo;
-    if (n <= (size_t)WAVE_CHUNK) {
+    if (n <= chunk) {
         groups.push_back({lo, hi});
         return;
     }
@@ -590,13 +591,13 @@ static void group_split(std::vector<size_t>& idx, size_t lo, size_t hi, const st
     }
     const std::vector<double>& key = (x1 - x0 >= y1 - y0) ? px : py;
     std::stable_sort(idx.begin() + lo, idx.begin() + hi, [&key](size_t a, size_t b) { return key[a] < key[b]; });
-    const size_t half = (size_t)std::llround((double)n / (2.0 * WAVE_CHUNK));
-    const size_t k = (size_t)WAVE_CHUNK * std::max<size_t>(1, half);
-    group_split(idx, lo, lo + k, px, py, groups);
-    group_split(idx, lo + k, hi, px, py, groups);
+    const size_t half = (size_t)std::llround((double)n / (2.0 * (double)chunk));
+    const size_t k = chunk * std::max<size_t>(1, half);
+    group_split(idx, lo, lo + k, px, py, chunk, groups);
+    group_split(idx, lo + k, hi, px, py, chunk, groups);
 }
 
-static void sort_waves(std::vector<double>& w) {
+static void sort_waves(std::vector<double>& w, int chunk) {
     size_t nk = w.size() / 3;
     if (nk < 3) return;
     double m[3] = {0, 0, 0};
@@ -620,9 +621,9 @@ static void sort_waves(std::vector<double>& w) {
         idx[i] = i;
     }
     std::vector<std::pair<size_t, size_t>> groups;
-    group_split(idx, 0, nk, px, py, groups);
+    group_split(idx, 0, nk, px, py, (size_t)chunk, groups);
     std::stable_partition(groups.begin(), groups.end(),
-                          [](const std::pair<size_t, size_t>& g) { return g.second - g.first == (size_t)WAVE_CHUNK; });
+                          [chunk](const std::pair<size_t, size_t>& g) { return g.second - g.first == (size_t)chunk; });
     std::vector<double> out;
     out.reserve(w.size());
     for (const auto& g : groups)
@@ -631,16 +632,16 @@ static void sort_waves(std::vector<double>& w) {
     w.swap(out);
 }
 
-// Bounding cone (unit axis, half-angle in radians) of every WAVE_CHUNK
+// Bounding cone (unit axis, half-angle in radians) of every `chunk`
 // consecutive waves, with a small margin for single-precision rounding.  A
 // chunk holding a direction that is not a unit vector gets half-angle pi,
 // which turns the angular window off for it.
-static std::vector<float4> wave_cones(const std::vector<double>& w) {
+static std::vector<float4> wave_cones(const std::vector<double>& w, int chunk) {
     size_t nk = w.size() / 3;
-    size_t nch = (nk + WAVE_CHUNK - 1) / WAVE_CHUNK;
+    size_t nch = (nk + chunk - 1) / chunk;
     std::vector<float4> out(nch);
     for (size_t ch = 0; ch < nch; ch++) {
-        size_t a = ch * WAVE_CHUNK, b = std::min(nk, a + WAVE_CHUNK);
+        size_t a = ch * chunk, b = std::min(nk, a + chunk);
         double m[3] = {0, 0, 0};
         bool unit = true;
         for (size_t i = a; i < b; i++) {
@@ -674,8 +675,10 @@ static std::vector<float4> wave_cones(const std::vector<double>& w) {
 // the rows, the corners' angles from the tile-centre direction give gamma.
 // When few windows fit, the texture-only kernel is faster (no shared memory
 // taken from the texture cache).
-constexpr double STAGED_KERNEL_MIN_FRACTION = 0.25;  // measured: 61% staged -> staged kernel 1.27x faster,
-                                                     // 0.6% staged -> texture-only kernel 1.09x faster
+// Measured on the config-2 scene at 1536^2 near-field pixels (texture-only
+// kernel 383 ms): staged kernel with 23 % of windows staged 395 ms, 41 %
+// 360 ms, 85 % 329 ms; at 3072^2, 98 % staged 772 ms against 1510 ms.
+constexpr double STAGED_KERNEL_MIN_FRACTION = 0.3;
 static double predict_staged_fraction(const bs_ctx* c, const std::vector<float4>& cones, int s0, int s1) {
     const Scene& sc = c->sc;
     const int R = sc.R, tiles = (R + LUT_TILE - 1) / LUT_TILE;
@@ -743,6 +746,52 @@ static double predict_staged_fraction(const bs_ctx* c, const std::vector<float4>
     return total ? (double)staged / (double)total : 0.0;
 }
 
+// Waves per chunk for the mixed LUT kernel, with the matching wave order and
+// cones: the largest of 64, 32 and 16 whose predicted staged fraction reaches
+// 0.8, else the one with the largest fraction.  Smaller chunks have narrower
+// cones, so more windows fit, but each chunk pays a window copy, two barriers
+// and a Kahan step.  64 whenever the texture-only kernel will run;
+// bs_set_lut_wave_chunk fixes the chunk instead.
+struct ChunkPlan {
+    int chunk = WAVE_CHUNK_MAX;
+    std::vector<double> w;
+    std::vector<float4> cones;
+    double predicted = 0;
+};
+
+static ChunkPlan choose_chunk(const bs_ctx* c, const std::vector<double>& waves, int ns) {
+    ChunkPlan first, best;
+    best.predicted = -1;
+    if (c->lut_chunk) {
+        best.chunk = c->lut_chunk;
+        best.w = waves;
+        sort_waves(best.w, best.chunk);
+        best.cones = wave_cones(best.w, best.chunk);
+        best.predicted = predict_staged_fraction(c, best.cones, 0, ns);
+        return best;
+    }
+    for (int cand : {WAVE_CHUNK_MAX, WAVE_CHUNK_MAX / 2, WAVE_CHUNK_MAX / 4}) {
+        ChunkPlan cp;
+        cp.chunk = cand;
+        cp.w = waves;
+        sort_waves(cp.w, cand);
+        cp.cones = wave_cones(cp.w, cand);
+        cp.predicted = predict_staged_fraction(c, cp.cones, 0, ns);
+        if (cand == WAVE_CHUNK_MAX) {
+            first = cp;
+            if (c->lut_staging == 2) return first;
+        }
+        const bool enough = cp.predicted >= 0.8;
+        if (cp.predicted > best.predicted || enough) best = std::move(cp);
+        if (enough) break;
+    }
+    if (c->lut_staging == 0 && best.predicted < STAGED_KERNEL_MIN_FRACTION) {
+        first.predicted = best.predicted;  // the texture-only kernel runs; report the best staging model
+        return first;
+    }
+    return best;
+}
+
 // ---------------------------------------------------------------------------
 // The near field
 // ---------------------------------------------------------------------------
@@ -758,8 +807,21 @@ static bs_status run_nearfield(bs_ctx* c) {
     // upload spheres and waves
     CK(c->d_sph.ensure(std::max(1, ns) * sizeof(Sphere)));
     std::vector<double> w(c->waves);
-    if (p.plane_wave) w.assign(p.k_dir, p.k_dir + 3);
-    else sort_waves(w);
+    std::vector<float4> cones;
+    int chunk = WAVE_CHUNK_MAX;
+    double predicted = 0;
+    if (p.plane_wave) {
+        w.assign(p.k_dir, p.k_dir + 3);
+    } else if (!fp64 && p.scalar && p.lut_us && ns > 0) {
+        ChunkPlan cp = choose_chunk(c, w, ns);
+        chunk = cp.chunk;
+        w.swap(cp.w);
+        cones.swap(cp.cones);
+        predicted = cp.predicted;
+    } else {
+        sort_waves(w, chunk);
+    }
+    c->stats.lut_wave_chunk = chunk;
     CK(c->d_waves.ensure(w.size() * sizeof(double)));
     CK(cudaMemcpyAsync(c->d_waves.p, w.data(), w.size() * sizeof(double), cudaMemcpyHostToDevice, c->st));
 
@@ -873,8 +935,11 @@ static bs_status run_nearfield(bs_ctx* c) {
                                 std::max(S.dR, S.aR), S.thetaR, maxh - 1, maxw);
             if ((int)c->slots.size() < max_chunk) c->slots.resize(max_chunk);
             CK(c->d_texobj.ensure((size_t)4 * max_chunk * sizeof(unsigned long long)));
-            std::vector<float4> cones = wave_cones(w);
-            c->stats.lut_staged_predicted = predict_staged_fraction(c, cones, 0, ns);
+            if (cones.empty()) {
+                cones = wave_cones(w, chunk);
+                predicted = predict_staged_fraction(c, cones, 0, ns);
+            }
+            c->stats.lut_staged_predicted = predicted;
             use_stage = c->lut_staging == 1 ||
                         (c->lut_staging == 0 && c->stats.lut_staged_predicted >= STAGED_KERNEL_MIN_FRACTION);
             CK(c->d_cones.ensure(cones.size() * sizeof(float4)));
@@ -941,7 +1006,7 @@ static bs_status run_nearfield(bs_ctx* c) {
                                   c->d_cones.as<float4>(), c->d_ph.as<cpx<float>>(),
                                   c->d_texobj.as<unsigned long long>(), c->d_lut.as<float2>(), (const cpx<float>*)Uf,
                                   (cpx<float>*)U, ns > 0 ? c->d_cnt.as<unsigned long long>() : nullptr, use_stage,
-                                  c->st);
+                                  chunk, c->st);
             }
             LAUNCHED(c);
             // the handle list and the table slots are reused by the next chunk
@@ -1008,7 +1073,7 @@ static size_t estimate_bytes(bs_ctx* c, bool fp64, size_t lut_budget) {
                 }
                 b += 2 * thetaR * (hd + ha) * sizeof(float);
             }
-            b += B(4 * max_chunk * sizeof(unsigned long long)) + B((nk + WAVE_CHUNK - 1) / WAVE_CHUNK * sizeof(float4)) +
+            b += B(4 * max_chunk * sizeof(unsigned long long)) + B((nk + 15) / 16 * sizeof(float4)) +
                  B(2 * sizeof(unsigned long long));
         }
     }
@@ -1027,6 +1092,13 @@ static size_t estimate_bytes(bs_ctx* c, bool fp64, size_t lut_budget) {
 }
 
 extern "C" {
+
+bs_status bs_set_lut_wave_chunk(bs_ctx* c, int32_t chunk) {
+    if (!c || (chunk != 0 && chunk != 16 && chunk != 32 && chunk != 64))
+        return fail(BS_ERR_ARG, "bs_set_lut_wave_chunk: chunk must be 0, 16, 32 or 64");
+    c->lut_chunk = chunk;
+    return BS_OK;
+}
 
 bs_status bs_set_lut_staging(bs_ctx* c, int32_t mode) {
     if (!c || mode < 0 || mode > 2) return fail(BS_ERR_ARG, "bs_set_lut_staging: mode must be 0, 1 or 2");
@@ -1150,6 +1222,7 @@ bs_status bs_simulate_sources(bs_ctx* c, const double* sources, int32_t n, bs_pr
         sum.lut_chunks_total += s.lut_chunks_total;
         sum.lut_tables_built += s.lut_tables_built;
         sum.lut_staged_predicted = s.lut_staged_predicted;
+        sum.lut_wave_chunk = s.lut_wave_chunk;
     }
     c->reuse = saved_reuse;
     if (!saved_reuse) c->lut_valid = false;
@@ -1246,6 +1319,7 @@ static void stats_add(bs_stats& sum, const bs_stats& s) {
     sum.lut_chunks_total += s.lut_chunks_total;
     sum.lut_tables_built += s.lut_tables_built;
     sum.lut_staged_predicted = s.lut_staged_predicted;
+    sum.lut_wave_chunk = s.lut_wave_chunk;
 }
 
 // One source of a ring driver at (x, y, z) with amplitude a; its stats are
@@ -1525,6 +1599,19 @@ bs_status bs_sweep(bs_ctx* c, const double* lambdas, int32_t nl, const double* n
                       ns > 0;
     float ms_stage = 0, ms_tex = 0;
     bs_status st = BS_OK;
+    // Both trial kernels run at the chunk a single auto-chosen run of this scene uses (the choice
+    // depends on the tile and table geometry, which is the same for every band), so every band has
+    // the bits of a single run.
+    const int saved_chunk = c->lut_chunk;
+    if (tune && saved_chunk == 0) {
+        c->prm.lambda = lambdas[0];
+        for (size_t i = 0; i < ns; i++) {
+            c->spheres[i].n_re = n_table[2 * i];
+            c->spheres[i].n_im = n_table[2 * i + 1];
+        }
+        st = derive(c);
+        if (st == BS_OK) c->lut_chunk = choose_chunk(c, c->waves, (int)ns).chunk;
+    }
     for (int32_t l = 0; l < nl && st == BS_OK; l++) {
         c->prm.lambda = lambdas[l];
         for (size_t i = 0; i < ns; i++) {
@@ -1542,6 +1629,7 @@ bs_status bs_sweep(bs_ctx* c, const double* lambdas, int32_t nl, const double* n
     c->prm = saved_p;
     c->spheres = saved_s;
     c->lut_staging = saved_staging;
+    c->lut_chunk = saved_chunk;
     c->have = false;
     return st;
 }

@@ -9,9 +9,10 @@
 
 namespace bs {
 
-// Plane waves are processed in chunks of this many (after a Hilbert-curve
-// sort); the host supplies one bounding cone per chunk.
-constexpr int WAVE_CHUNK = 64;
+// Plane waves are processed in chunks of 64, 32 or 16 (chosen per run from the
+// predicted fraction of staged windows) after grouping them by direction; the
+// host supplies one bounding cone per chunk.
+constexpr int WAVE_CHUNK_MAX = 64;
 
 // Mixed LUT kernel staging: float2 table values a 16 x 16 pixel tile stages
 // per wave chunk (43 KB of shared memory, 4 blocks per SM), and the angle
@@ -56,13 +57,13 @@ void launch_us_lut_f64(const Scene& sc, const Sphere* sph, int s0, int s1, int a
 // {Usp re, Usp im, Uip re, Uip im} at [4 j .. 4 j + 3]
 // lin: linear float2 tables (Sphere::usp_off / uip_off in float2 units, rows
 // of Sphere::lin_stride entries);
-// cones: one {axis, half-angle} per WAVE_CHUNK waves; counters[0..1] receive
+// cones: one {axis, half-angle} per `chunk` waves; counters[0..1] receive
 // the staged and total (sphere, chunk) counts of every block (may be null);
 // stage = false runs the texture-only variant
 void launch_us_lut_tex(const Scene& sc, const Sphere* sph, int s0, int s1, int accumulate, int finalize,
                        const float4* kw4, const float4* cones, const cpx<float>* ph, const unsigned long long* tex,
                        const float2* lin, const cpx<float>* Uf, cpx<float>* U, unsigned long long* counters,
-                       bool stage, cudaStream_t st);
+                       bool stage, int chunk, cudaStream_t st);
 void launch_lut_build_tex(const zd* tab, int rows, int L, const double* P, int Pstride, int thetaR,
                           cudaSurfaceObject_t sre, cudaSurfaceObject_t sim, float2* lin, int lin_stride,
                           cudaStream_t st);

@@ -502,7 +502,7 @@ __device__ __forceinline__ float2 f2_unpack(f32x2 v) {
 }
 
 __device__ __forceinline__ void copy_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
-constexpr int UST_CHUNK = WAVE_CHUNK;
+constexpr int UST_CHUNK = WAVE_CHUNK_MAX;  // shared arrays; the run's chunk may be smaller
 constexpr int UST_STAGE = LUT_STAGE_ENTRIES;
 constexpr float UST_MARGIN = LUT_STAGE_MARGIN;
 
@@ -545,7 +545,8 @@ __global__ void __launch_bounds__(UST_BLOCK, STAGE ? 4 : 6) us_lut_tex_kernel(Sc
                                                                     const float2* __restrict__ lin,
                                                                     const cpx<float>* __restrict__ Uf,
                                                                     cpx<float>* __restrict__ U,
-                                                                    unsigned long long* __restrict__ counters) {
+                                                                    unsigned long long* __restrict__ counters,
+                                                                    int chunk) {
     extern __shared__ float2 s_stage[];
     __shared__ float4 s_k[UST_CHUNK];
     __shared__ float4 s_p[UST_CHUNK];  // phase (x, x, y, y): lane pairs for the packed products
@@ -577,7 +578,7 @@ __global__ void __launch_bounds__(UST_BLOCK, STAGE ? 4 : 6) us_lut_tex_kernel(Sc
         tot_r = U[iv * sc.R + iu].re;
         tot_i = U[iv * sc.R + iu].im;
     }
-    const int nchunks = (sc.nk + UST_CHUNK - 1) / UST_CHUNK;
+    const int nchunks = (sc.nk + chunk - 1) / chunk;
     unsigned staged_chunks = 0;
     for (int s = s0; s < s1; s++) {
         const Sphere& S = sph[s];
@@ -667,8 +668,8 @@ __global__ void __launch_bounds__(UST_BLOCK, STAGE ? 4 : 6) us_lut_tex_kernel(Sc
         const int lr0 = min(max(ir - rlo, 0), max(nrows_b, 1) - 1);
         const int lr1 = min(max(min(ir + 1, ts.rows - 1) - rlo, 0), max(nrows_b, 1) - 1);
         for (int ch = 0; ch < nchunks; ch++) {
-            const int w0 = ch * UST_CHUNK;
-            const int nw = min(UST_CHUNK, sc.nk - w0);
+            const int w0 = ch * chunk;
+            const int nw = min(chunk, sc.nk - w0);
             __syncthreads();  // the previous chunk's readers are done; s_ts is written
             const int nrows = s_ts.nrows;
             // window of this chunk: planned by thread 0 (before the first chunk, or while the
@@ -1020,12 +1021,12 @@ void launch_us_lut_f64(const Scene& sc, const Sphere* sph, int s0, int s1, int a
 void launch_us_lut_tex(const Scene& sc, const Sphere* sph, int s0, int s1, int accumulate, int finalize,
                        const float4* kw4, const float4* cones, const cpx<float>* ph, const unsigned long long* tex,
                        const float2* lin, const cpx<float>* Uf, cpx<float>* U, unsigned long long* counters,
-                       bool stage, cudaStream_t st) {
+                       bool stage, int chunk, cudaStream_t st) {
     int tiles = (sc.R + 15) / 16;
     if (!stage) {
         us_lut_tex_kernel<false><<<(unsigned)tiles * tiles, UST_BLOCK, 0, st>>>(sc, sph, s0, s1, accumulate, finalize,
                                                                                  kw4, cones, ph, tex, lin, Uf, U,
-                                                                                 counters);
+                                                                                 counters, chunk);
         return;
     }
     const int smem = UST_STAGE * (int)sizeof(float2);
@@ -1033,7 +1034,7 @@ void launch_us_lut_tex(const Scene& sc, const Sphere* sph, int s0, int s1, int a
     cudaFuncSetAttribute(us_lut_tex_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     us_lut_tex_kernel<true><<<(unsigned)tiles * tiles, UST_BLOCK, smem, st>>>(sc, sph, s0, s1, accumulate, finalize,
                                                                                kw4, cones, ph, tex, lin, Uf, U,
-                                                                               counters);
+                                                                               counters, chunk);
 }
 
 void launch_lut_build_tex(const zd* tab, int rows, int L, const double* P, int Pstride, int thetaR,

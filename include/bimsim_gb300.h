@@ -121,6 +121,7 @@ typedef struct bs_stats {
     int64_t lut_chunks_total;
     int64_t lut_tables_built;  /* sphere tables (Usp + Uip) built; 0 when reused */
     double lut_staged_predicted;  /* the kernel choice's model of lut_chunks_staged / total */
+    int64_t lut_wave_chunk;       /* waves per chunk of the mixed LUT kernel (64, 32 or 16) */
 } bs_stats;
 
 typedef struct bs_ctx bs_ctx;
@@ -278,6 +279,11 @@ bs_status bs_plane_point(const bs_params* params, double u, double v, double* xy
  * faster runs the rest (identical bits either way). */
 bs_status bs_sweep(bs_ctx* ctx, const double* lambdas, int32_t nl, const double* n_table, bs_precision prec,
                    bs_image_kind kind, float* images, const char* envi_path, int32_t band_as_nu);
+
+/* Waves per chunk of the mixed LUT kernel: 0 (default) picks 64, 32 or 16 per
+ * run from the predicted fraction of staged windows; 16, 32 or 64 fixes it.
+ * The staged and texture-only kernels give the same bits at the same chunk. */
+bs_status bs_set_lut_wave_chunk(bs_ctx* ctx, int32_t chunk);
 
 /* Kernel of the mixed-precision LUT stage: 0 (default) chooses from a model
  * of how many table windows fit in shared memory, 1 always stages windows in
