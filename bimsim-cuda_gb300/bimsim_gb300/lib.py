@@ -60,6 +60,7 @@ def library():
         "bs_plane_point": ([vp, C.c_double, C.c_double, vp], C.c_int),
         "bs_get_far_field": ([vp, C.c_int, vp, sz], C.c_int),
         "bs_material_eval": ([C.c_char_p, vp, i32, vp], C.c_int),
+    "bs_material_kk": ([C.c_char_p, C.c_double, i32, i32, vp, vp], C.c_int),
         "bs_set_lut_reuse": ([vp, i32], C.c_int),
         "bs_set_lut_staging": ([vp, i32], C.c_int),
     "bs_set_lut_wave_chunk": ([vp, i32], C.c_int),
@@ -247,6 +248,18 @@ def material_eval(path, lambdas):
     if st != 0:
         raise BimsimError(st, lib.bs_last_error().decode())
     return out.view(np.complex128)
+
+
+def material_kk(path, n0, n_samples=0, pf=2):
+    """Kramers-Kronig real index of a material file: (wavelengths, n + i kappa)."""
+    lib = library()
+    lam = np.zeros(n_samples if n_samples else 16384)  # 16384 = BS_KK_MAX_SAMPLES
+    out = np.zeros(2 * lam.size)
+    st = lib.bs_material_kk(str(path).encode(), float(n0), int(n_samples), int(pf), _p(lam), _p(out))
+    if st != 0:
+        raise BimsimError(st, lib.bs_last_error().decode())
+    n = n_samples if n_samples else int(np.count_nonzero(lam))  # wavelengths are positive
+    return lam[:n].copy(), out[:2 * n].view(np.complex128).copy()
 
 
 def plane_point(params, u, v):

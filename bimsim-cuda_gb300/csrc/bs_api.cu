@@ -1288,6 +1288,59 @@ bs_status bs_material_eval(const char* path, const double* lambdas, int32_t n, d
     return BS_OK;
 }
 
+bs_status bs_material_kk(const char* path, double n0, int32_t n_samples, int32_t pf, double* lambdas, double* n_out) {
+    if (!path || !lambdas || !n_out || n_samples < 0 || pf < 1 || !(n0 > 0))
+        return fail(BS_ERR_ARG, "bs_material_kk: bad arguments");
+    std::ifstream f(path);
+    if (!f) return fail(BS_ERR_IO, "Material Error -- file not found: %s", path);
+    std::string text((std::istreambuf_iterator<char>(f)), std::istreambuf_iterator<char>());
+    std::vector<float> lam, re, im;
+    std::string err;
+    if (!material_load(text, lam, re, im, err)) return fail(BS_ERR_IO, "%s: %s", path, err.c_str());
+    const int N = n_samples ? n_samples : (int)lam.size();
+    if (N < 2 || N > BS_KK_MAX_SAMPLES)
+        return fail(BS_ERR_ARG, "bs_material_kk: %d samples (2 to %d)", N, BS_KK_MAX_SAMPLES);
+    const int M = N * pf;
+    // resample kappa at evenly spaced wavenumbers, from the shortest wavelength up (material.h:294-316)
+    const double nu_min = 10000.0 / (double)lam.back(), nu_max = 10000.0 / (double)lam.front();
+    const double dnu = (nu_max - nu_min) / (N - 1);
+    std::vector<double> chi2(N), kap(N);
+    for (int i = 0; i < N; i++) {
+        const double l = 10000.0 / (nu_max - i * dnu);
+        float nr, ni;
+        material_eval(lam, re, im, (float)l, nr, ni);
+        kap[i] = ni;
+        const float k = (float)(2 * (float)PI_REF / l);      // float k, alpha as in the reference
+        const float alpha = (float)((double)ni * (double)(2 * k));
+        chi2[i] = -(double)alpha * (n0 / (double)k);
+        lambdas[i] = l;
+    }
+    double *d_chi2 = nullptr, *d_g = nullptr, *d_chi1 = nullptr;
+    cudaStream_t st = nullptr;
+    cudaError_t e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMalloc(&d_chi2, N * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&d_g, (size_t)M * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&d_chi1, N * sizeof(double));
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_chi2, chi2.data(), N * sizeof(double), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) {
+        launch_kk(N, M, d_chi2, d_g, d_chi1, st);
+        e = cudaGetLastError();
+    }
+    std::vector<double> chi1(N);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(chi1.data(), d_chi1, N * sizeof(double), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    cudaFree(d_chi2);
+    cudaFree(d_g);
+    cudaFree(d_chi1);
+    if (st) cudaStreamDestroy(st);
+    if (e != cudaSuccess) return fail(BS_ERR_CUDA, "bs_material_kk: %s", cudaGetErrorString(e));
+    for (int i = 0; i < N; i++) {
+        n_out[2 * i] = chi1[i] / (2 * n0) + n0;
+        n_out[2 * i + 1] = kap[i];
+    }
+    return BS_OK;
+}
+
 }  // extern "C"
 
 // Ring point sources (--interpolate 1, 2, 3; microscope.cu:1004-1253).  Ring

@@ -270,6 +270,42 @@ void launch_line_image(int res, int L, const T* line, T* D, cudaStream_t st) {
     line_image_kernel<T><<<grid, 128, 0, st>>>(res, L, line, D);
 }
 
+// ---------------------------------------------------------------------------
+// Kramers-Kronig (material::computeN, rts/optics/material.h:257-432): the
+// reference multiplies the FFT of the zero-padded chi2 (M points) by i for
+// 0 < f < M/2, by -i for f >= M/2 and by 0 at f = 0, transforms back and
+// divides by M.  For real chi2 the real part of that is a circular convolution
+// with g(m) = (1/M) (sum_{0<f<M/2} -sin(2 pi f m / M) + sum_{f>=M/2} sin(2 pi f m / M)),
+// computed here directly in double precision (sinpi of the exactly reduced
+// argument 2 (f m mod M) / M).
+// ---------------------------------------------------------------------------
+__global__ void kk_kernel_g(int M, double* __restrict__ g) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= M) return;
+    const int half = (M + 1) / 2;  // f < M / 2.0  <=>  f < half
+    double acc = 0;
+    for (int f = 1; f < M; f++) {
+        const long long r = ((long long)f * m) % M;
+        const double sn = sinpi(2.0 * (double)r / (double)M);
+        acc += f < half ? -sn : sn;
+    }
+    g[m] = acc / (double)M;
+}
+
+__global__ void kk_kernel_conv(int N, int M, const double* __restrict__ chi2, const double* __restrict__ g,
+                               double* __restrict__ chi1) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    double acc = 0;
+    for (int j = 0; j < N; j++) acc += chi2[j] * g[(i - j + M) % M];
+    chi1[i] = acc;
+}
+
+void launch_kk(int N, int M, const double* chi2, double* g, double* chi1, cudaStream_t st) {
+    kk_kernel_g<<<(M + 127) / 128, 128, 0, st>>>(M, g);
+    kk_kernel_conv<<<(N + 127) / 128, 128, 0, st>>>(N, M, chi2, g, chi1);
+}
+
 #define BS_DET_INST(T)                                                                                          \
     template void launch_twiddle<T>(int, int, const int*, int, int, int, int, int, cpx<T>*, cudaStream_t);      \
     template void launch_cgemm<T>(int, int, int, int, const cpx<T>*, int, long long, const cpx<T>*, int,       \

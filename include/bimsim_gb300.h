@@ -228,6 +228,23 @@ bs_status bs_simulate_sources(bs_ctx* ctx, const double* sources, int32_t n, bs_
  * Blank lines are skipped (the reference's parser never returns on one). */
 bs_status bs_material_eval(const char* path, const double* lambdas, int32_t n, double* n_out);
 
+/* Kramers-Kronig real index of a material file (material::computeN,
+ * rts/optics/material.h:257-432, which the reference never calls and which
+ * needs FFTW).  kappa is resampled at n_samples (0: the file's entry count,
+ * at most BS_KK_MAX_SAMPLES) wavenumbers evenly spaced from 1e4 / lambda_min
+ * down to 1e4 / lambda_max; chi2 = -alpha n0 / k with k = 2 pi / lambda and
+ * alpha = 2 k kappa in single precision (the reference's float k and alpha);
+ * chi2 zero-padded to pf * n_samples points goes through the reference's FFT
+ * Hilbert transform (x i for 0 < f < M/2, x -i for f >= M/2, DC removed,
+ * inverse / M), here as the equivalent circular convolution on the GPU in
+ * double precision; n = Re(chi1) / (2 n0) + n0.  Outputs: the sample
+ * wavelengths (increasing, um) and (n, kappa) pairs.  The reference's routine
+ * hands complex<float> arrays to FFTW's double transforms; this restates the
+ * double-precision transform it describes. */
+#define BS_KK_MAX_SAMPLES 16384
+bs_status bs_material_kk(const char* path, double n0, int32_t n_samples, int32_t pf, double* lambdas,
+                         double* n_out);
+
 /* Ring point sources by near-field rotation: the reference's --interpolate 3
  * (SimulateExtendedSourceWithInterpolation, microscope.cu:1185-1253, with
  * nfInterpolate.cu:13-115).  The detector sums the slice of the context's own

@@ -1598,6 +1598,29 @@ int bso_simulate_rings(const bs_params* p, const bs_sphere* s, int ns, const dou
     return 0;
 }
 
+// material::computeN (rts/optics/material.h:257-432) from the resampled kappa:
+// chi2 = -alpha n0 / k with float k = 2 PI / lambda and float alpha = kappa 2k,
+// zero-padded to M = pf N points, forward FFT, x i for 0 < f < M/2.0, x -i for
+// f >= M/2.0, DC zeroed, inverse FFT / M, n = Re chi1 / (2 n0) + n0.
+int bso_kk_transform(int N, int pf, double n0, const double* lambdas, const double* kappas, double* n_out) {
+    const int M = N * pf;
+    std::vector<cd> a(M, cd(0, 0));
+    for (int i = 0; i < N; i++) {
+        const float k = (float)(2 * (float)PI_REF / lambdas[i]);
+        const float alpha = (float)(kappas[i] * (double)(2 * k));
+        a[i] = cd(-(double)alpha * (n0 / (double)k), 0);
+    }
+    fft_any(a, -1);
+    for (int f = 0; f < M; f++) {
+        if (f == 0) a[f] = 0;
+        else if (f < M / 2.0) a[f] *= cd(0, 1);
+        else a[f] *= cd(0, -1);
+    }
+    fft_any(a, +1);
+    for (int i = 0; i < N; i++) n_out[i] = (a[i].real() / M) / (2 * n0) + n0;
+    return 0;
+}
+
 int bso_fft(int n, int sign, double* data) {
     std::vector<cd> a(n);
     for (int i = 0; i < n; i++) a[i] = cd(data[2 * i], data[2 * i + 1]);

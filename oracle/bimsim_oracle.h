@@ -98,6 +98,10 @@ int bso_far_field(const bs_params* p, const double* U, double* out);
 int bso_simulate_rings(const bs_params* p, const bs_sphere* s, int ns, const double* waves, int nk, int nthreads,
                        int mode, int points, int rings, double* D, double* Di);
 
+/* Kramers-Kronig real index from kappa at the resampled wavelengths
+ * (material::computeN, rts/optics/material.h:257-432): n_out[N]. */
+int bso_kk_transform(int N, int pf, double n0, const double* lambdas, const double* kappas, double* n_out);
+
 /* Forward (sign=-1) or inverse (sign=+1, unnormalised) 1-D DFT of n complex. */
 int bso_fft(int n, int sign, double* data);
 
