@@ -64,6 +64,7 @@ def library():
         "bs_set_lut_reuse": ([vp, i32], C.c_int),
         "bs_set_lut_staging": ([vp, i32], C.c_int),
     "bs_set_lut_wave_chunk": ([vp, i32], C.c_int),
+    "bs_set_backpropagation": ([vp, i32, C.c_double], C.c_int),
         "bs_release_buffers": ([vp], C.c_int),
         "bs_estimate_bytes": ([vp, vp, i32, i32, C.c_int, C.c_uint64, C.POINTER(C.c_uint64)], C.c_int),
         "bs_server_create": ([vp, C.POINTER(vp)], C.c_int),
@@ -227,6 +228,10 @@ class Context:
     def set_lut_staging(self, mode):
         """0 model-chosen, 1 staged kernel, 2 texture-only kernel (same results)."""
         self._check(self.lib.bs_set_lut_staging(self.h, mode))
+
+    def set_backpropagation(self, enable, d=0.0):
+        """Propagate U over d um before the band-pass (the reference's disabled applyBackpropagation)."""
+        self._check(self.lib.bs_set_backpropagation(self.h, int(bool(enable)), float(d)))
 
     def set_lut_wave_chunk(self, chunk):
         """Waves per chunk of the mixed LUT kernel: 0 chooses per run, else 16, 32 or 64."""

@@ -184,6 +184,9 @@ struct bs_ctx {
     bool reuse = false;
     int lut_staging = 0;  // bs_set_lut_staging: 0 model-chosen, 1 staged kernel, 2 texture-only kernel
     int lut_chunk = 0;    // bs_set_lut_wave_chunk: 0 model-chosen, else waves per chunk
+    bool bp_on = false;   // bs_set_backpropagation
+    double bp_d = 0;
+    DevBuf d_bp;          // back-propagation phase on the passband grid
     bool lut_valid = false;
     std::vector<double> lut_key;
 };
@@ -194,7 +197,7 @@ static std::vector<DevBuf*> ctx_bufs(bs_ctx* c) {
             &c->d_tabscr, &c->d_legP, &c->d_lut, &c->d_uft, &c->d_uftscr, &c->d_fields, &c->d_su,
             &c->d_sv, &c->d_mask, &c->d_wx, &c->d_wy, &c->d_wix, &c->d_wiy, &c->d_f1, &c->d_f2,
             &c->d_g1, &c->d_I, &c->d_D, &c->d_img, &c->d_cones, &c->d_cnt, &c->d_far,
-            &c->d_starts, &c->d_fsave, &c->d_dacc, &c->d_line, &c->d_ringcs};
+            &c->d_starts, &c->d_fsave, &c->d_dacc, &c->d_line, &c->d_ringcs, &c->d_bp};
 }
 
 static void release_all(bs_ctx* c) {
@@ -465,6 +468,24 @@ static bs_status run_detector(bs_ctx* c, bool accumulate) {
     launch_cgemm<T>(Nv, Nu, R, 2, wy, R, 0, f1, Nu, (long long)R * Nu, f2, Nu, (long long)Nv * Nu, 1,
                     c->d_mask.as<float>(), (T)1, nullptr, c->st);
     LAUNCHED(c);
+    if (c->bp_on) {
+        // applyBackpropagation (microscope.cu:423-470, 592-605) on U only: -exp(i kz d) with
+        // kz = sqrt(k^2 - kx^2 - ky^2), k = 2 PI / lambda, kx = 2 PI u; zero where kx^2 + ky^2 >= k^2
+        std::vector<cpx<T>> bp((size_t)Nv * Nu);
+        const double k = 2 * PI_REF / p.lambda;
+        for (int j = 0; j < Nv; j++)
+            for (int kk = 0; kk < Nu; kk++) {
+                const double kx = 2 * PI_REF * freq(su[kk], du), ky = 2 * PI_REF * freq(sv[j], dv);
+                const double q = k * k - kx * kx - ky * ky;
+                const double ph = q > 0 ? std::sqrt(q) * c->bp_d : 0;
+                bp[(size_t)j * Nu + kk] = q > 0 ? mk((T)(-std::cos(ph)), (T)(-std::sin(ph))) : mk((T)0, (T)0);
+            }
+        CK(c->d_bp.ensure(bp.size() * sizeof(cpx<T>)));
+        CK(cudaMemcpyAsync(c->d_bp.p, bp.data(), bp.size() * sizeof(cpx<T>), cudaMemcpyHostToDevice, c->st));
+        launch_cmul<T>(Nv * Nu, c->d_bp.as<cpx<T>>(), f2, c->st);  // batch 0: U
+        LAUNCHED(c);
+        CK(cudaStreamSynchronize(c->st));  // bp is a host vector of this scope
+    }
     launch_cgemm<T>(Nv, C, Nu, 2, f2, Nu, (long long)Nv * Nu, wix, C, 0, g1, C, (long long)Nv * C, 0, nullptr, (T)1,
                     nullptr, c->st);
     LAUNCHED(c);
@@ -1092,6 +1113,13 @@ static size_t estimate_bytes(bs_ctx* c, bool fp64, size_t lut_budget) {
 }
 
 extern "C" {
+
+bs_status bs_set_backpropagation(bs_ctx* c, int32_t enable, double d) {
+    if (!c || !std::isfinite(d)) return fail(BS_ERR_ARG, "bs_set_backpropagation: bad arguments");
+    c->bp_on = enable != 0;
+    c->bp_d = d;
+    return BS_OK;
+}
 
 bs_status bs_set_lut_wave_chunk(bs_ctx* c, int32_t chunk) {
     if (!c || (chunk != 0 && chunk != 16 && chunk != 32 && chunk != 64))

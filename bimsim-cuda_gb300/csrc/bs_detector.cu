@@ -306,6 +306,20 @@ void launch_kk(int N, int M, const double* chi2, double* g, double* chi1, cudaSt
     kk_kernel_conv<<<(N + 127) / 128, 128, 0, st>>>(N, M, chi2, g, chi1);
 }
 
+// x[i] *= a[i] for complex arrays (applyBackpropagation's phase on the passband spectrum)
+template <class T>
+__global__ void cmul_kernel(int n, const cpx<T>* __restrict__ a, cpx<T>* __restrict__ x) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const cpx<T> p = a[i], q = x[i];
+    x[i] = mk(p.re * q.re - p.im * q.im, p.re * q.im + p.im * q.re);
+}
+
+template <class T>
+void launch_cmul(int n, const cpx<T>* a, cpx<T>* x, cudaStream_t st) {
+    if (n > 0) cmul_kernel<T><<<(n + 255) / 256, 256, 0, st>>>(n, a, x);
+}
+
 #define BS_DET_INST(T)                                                                                          \
     template void launch_twiddle<T>(int, int, const int*, int, int, int, int, int, cpx<T>*, cudaStream_t);      \
     template void launch_cgemm<T>(int, int, int, int, const cpx<T>*, int, long long, const cpx<T>*, int,       \
@@ -314,7 +328,8 @@ void launch_kk(int N, int M, const double* chi2, double* g, double* chi1, cudaSt
     template void launch_image<T>(int, int, const T*, const T*, T*, cudaStream_t);                             \
     template void launch_rotate_add_images<T>(int, float, float, const T*, T*, cudaStream_t);                 \
     template void launch_ring_line<T>(int, int, int, const float2*, const T*, T*, cudaStream_t);              \
-    template void launch_line_image<T>(int, int, const T*, T*, cudaStream_t);
+    template void launch_line_image<T>(int, int, const T*, T*, cudaStream_t);                                \
+    template void launch_cmul<T>(int, const cpx<T>*, cpx<T>*, cudaStream_t);
 BS_DET_INST(float)
 BS_DET_INST(double)
 

@@ -112,6 +112,10 @@ void launch_line_image(int res, int L, const T* line, T* D, cudaStream_t st);
 // to M) at the first N points, chi1; g is scratch of M doubles.
 void launch_kk(int N, int M, const double* chi2, double* g, double* chi1, cudaStream_t st);
 
+// x[i] *= a[i], i < n (complex)
+template <class T>
+void launch_cmul(int n, const cpx<T>* a, cpx<T>* x, cudaStream_t st);
+
 // image kinds 2, 3: -log10(D/Di), D/Di (microscope.cu:722-775); 0, 1: copies
 template <class T>
 void launch_image(int n, int kind, const T* D, const T* Di, T* out, cudaStream_t st);

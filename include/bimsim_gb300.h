@@ -297,6 +297,15 @@ bs_status bs_plane_point(const bs_params* params, double u, double v, double* xy
 bs_status bs_sweep(bs_ctx* ctx, const double* lambdas, int32_t nl, const double* n_table, bs_precision prec,
                    bs_image_kind kind, float* images, const char* envi_path, int32_t band_as_nu);
 
+/* Back-propagation of the total near field U over distance d (um) before the
+ * objective band-pass: the reference's applyBackpropagation
+ * (microscope.cu:423-470, 592-605), which its Simulate() has commented out
+ * (microscope.cu:853), with d the plane position z_d (arguments.h:409).  The
+ * spectrum is multiplied by -exp(i kz d), kz = sqrt(k^2 - kx^2 - ky^2),
+ * k = 2 pi / lambda, on the band-pass frequency grid (zero where kx^2 + ky^2
+ * >= k^2).  The incident field Uf is not propagated.  Off by default. */
+bs_status bs_set_backpropagation(bs_ctx* ctx, int32_t enable, double d);
+
 /* Waves per chunk of the mixed LUT kernel: 0 (default) picks 64, 32 or 16 per
  * run from the predicted fraction of staged windows; 16, 32 or 64 fixes it.
  * The staged and texture-only kernels give the same bits at the same chunk. */

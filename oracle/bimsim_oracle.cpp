@@ -1000,16 +1000,30 @@ void fft2(std::vector<cd>& f, int R, int sign) {
 
 // applyBandpass / bandpass / getFarField / integrateDetector
 // (microscope.cu:495-526, 608-662; fieldslice.cpp:25-94; fieldslice.cu:71-108,319-338)
-std::vector<cd> bandpassed(const bs_params& p, const Geom& g, const cd* U) {
+// bp: propagation distance of applyBackpropagation (microscope.cu:423-470,
+// 592-605), or null: the spectrum times -exp(i kz d), kz = sqrt(k^2 - kx^2 - ky^2)
+// with k = 2 PI / lambda and kx = 2 PI u on the band-pass frequency grid, zero
+// where kx^2 + ky^2 >= k^2.
+std::vector<cd> bandpassed(const bs_params& p, const Geom& g, const cd* U, const double* bp = nullptr) {
     const int R = g.R;
     std::vector<cd> f(U, U + (size_t)R * R);
     fft2(f, R, -1);
     double du = 1.0 / len(g.nf.X), dv = 1.0 / len(g.nf.Y);
     double lo = p.objective[0] / p.lambda, hi = p.objective[1] / p.lambda;
+    const double k = 2 * PI_REF / p.lambda;
     for (int iv = 0; iv < R; iv++) {
         double v = (iv <= R / 2) ? iv * dv : -(double)(R - 1 - iv) * dv;
         for (int iu = 0; iu < R; iu++) {
             double u = (iu <= R / 2) ? iu * du : -(double)(R - 1 - iu) * du;
+            if (bp) {
+                const double kx = 2 * PI_REF * u, ky = 2 * PI_REF * v;
+                if (kx * kx + ky * ky < k * k) {
+                    const double kz = std::sqrt(k * k - kx * kx - ky * ky);
+                    f[(size_t)iv * R + iu] *= -std::exp(cd(0, kz * *bp));
+                } else {
+                    f[(size_t)iv * R + iu] = 0.0;
+                }
+            }
             double fm = std::sqrt(u * u + v * v);
             if (fm < lo || fm > hi) f[(size_t)iv * R + iu] = 0.0;
         }
@@ -1018,9 +1032,9 @@ std::vector<cd> bandpassed(const bs_params& p, const Geom& g, const cd* U) {
     return f;
 }
 
-void detector(const bs_params& p, const Geom& g, const cd* U, double* D) {
+void detector(const bs_params& p, const Geom& g, const cd* U, double* D, const double* bp = nullptr) {
     const int R = g.R;
-    std::vector<cd> f = bandpassed(p, g, U);
+    std::vector<cd> f = bandpassed(p, g, U, bp);
     double sc = 1.0 / ((double)R * R);
     int cr = g.crop_res, off = g.crop_off, ss = g.ss, res = g.res;
     for (int iv = 0; iv < res; iv++)
@@ -1509,6 +1523,14 @@ int bso_far_field(const bs_params* p, const double* U, double* out) {
 int bso_detector(const bs_params* p, const double* U, const double* Uf, double* D, double* Di) {
     Geom g = derive(*p);
     if (D) detector(*p, g, reinterpret_cast<const cd*>(U), D);
+    if (Di) detector(*p, g, reinterpret_cast<const cd*>(Uf), Di);
+    return 0;
+}
+
+// The detector with applyBackpropagation over distance d on U (Uf is not propagated).
+int bso_detector_bp(const bs_params* p, const double* U, const double* Uf, double d, double* D, double* Di) {
+    Geom g = derive(*p);
+    if (D) detector(*p, g, reinterpret_cast<const cd*>(U), D, &d);
     if (Di) detector(*p, g, reinterpret_cast<const cd*>(Uf), Di);
     return 0;
 }

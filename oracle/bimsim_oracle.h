@@ -102,6 +102,10 @@ int bso_simulate_rings(const bs_params* p, const bs_sphere* s, int ns, const dou
  * (material::computeN, rts/optics/material.h:257-432): n_out[N]. */
 int bso_kk_transform(int N, int pf, double n0, const double* lambdas, const double* kappas, double* n_out);
 
+/* Detector with applyBackpropagation (microscope.cu:423-470, 592-605) over
+ * distance d applied to U before the band-pass. */
+int bso_detector_bp(const bs_params* p, const double* U, const double* Uf, double d, double* D, double* Di);
+
 /* Forward (sign=-1) or inverse (sign=+1, unnormalised) 1-D DFT of n complex. */
 int bso_fft(int n, int sign, double* data);
 

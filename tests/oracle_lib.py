@@ -52,6 +52,7 @@ def load():
     lib.bso_nearfield_rows.argtypes = [vp, vp, C.c_int, vp, C.c_int, C.c_int, C.c_int, C.c_int, vp]
     lib.bso_nearfield_rows_timed.argtypes = [vp, vp, C.c_int, vp, C.c_int, C.c_int, C.c_int, C.c_int, vp, vp]
     lib.bso_detector.argtypes = [vp, vp, vp, vp, vp]
+    lib.bso_detector_bp.argtypes = [vp, vp, vp, C.c_double, vp, vp]
     lib.bso_kk_transform.argtypes = [C.c_int, C.c_int, C.c_double, vp, vp, vp]
     lib.bso_simulate_rings.argtypes = [vp, vp, C.c_int, vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, vp, vp]
     lib.bso_far_field.argtypes = [vp, vp, vp]
