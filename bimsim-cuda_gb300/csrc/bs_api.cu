@@ -187,6 +187,7 @@ struct bs_ctx {
     bool bp_on = false;   // bs_set_backpropagation
     double bp_d = 0;
     DevBuf d_bp;          // back-propagation phase on the passband grid
+    DevBuf d_shrec, d_shtab, d_shcoef;  // direct method: harmonic recurrences, per-wave and per-sphere tables
     bool lut_valid = false;
     std::vector<double> lut_key;
 };
@@ -197,7 +198,7 @@ static std::vector<DevBuf*> ctx_bufs(bs_ctx* c) {
             &c->d_tabscr, &c->d_legP, &c->d_lut, &c->d_uft, &c->d_uftscr, &c->d_fields, &c->d_su,
             &c->d_sv, &c->d_mask, &c->d_wx, &c->d_wy, &c->d_wix, &c->d_wiy, &c->d_f1, &c->d_f2,
             &c->d_g1, &c->d_I, &c->d_D, &c->d_img, &c->d_cones, &c->d_cnt, &c->d_far,
-            &c->d_starts, &c->d_fsave, &c->d_dacc, &c->d_line, &c->d_ringcs, &c->d_bp};
+            &c->d_starts, &c->d_fsave, &c->d_dacc, &c->d_line, &c->d_ringcs, &c->d_bp, &c->d_shrec, &c->d_shtab, &c->d_shcoef};
 }
 
 static void release_all(bs_ctx* c) {
@@ -900,8 +901,16 @@ static bs_status run_nearfield(bs_ctx* c) {
         if (ns == 0) {
             CK(cudaMemcpyAsync(U, Uf, (size_t)R * R * sizeof(cpx<T>), cudaMemcpyDeviceToDevice, c->st));
         } else {
-            launch_us_direct<T>(sc, c->d_sph.as<Sphere>(), c->Lmax, c->d_A.as<zd>(), c->d_B.as<zd>(),
-                                c->d_waves.as<double>(), c->d_ph.as<cpx<T>>(), Uf, U, c->st);
+            // the addition theorem turns the per-wave Legendre sums into per-sphere coefficients
+            const int L = c->Lmax, nlm = L * (L + 1) / 2;
+            CK(c->d_shrec.ensure((size_t)nlm * sizeof(double2)));
+            CK(c->d_shtab.ensure((size_t)nk * nlm * sizeof(double2)));
+            CK(c->d_shcoef.ensure((size_t)ns * nlm * 2 * sizeof(zd)));
+            launch_sh_tables(sc, c->d_sph.as<Sphere>(), L, c->d_waves.as<double>(), c->d_shrec.as<double2>(),
+                             c->d_shtab.as<double2>(), c->d_shcoef.as<zd>(), c->st);
+            c->launches += 3;
+            launch_us_sh<T>(sc, c->d_sph.as<Sphere>(), L, c->d_A.as<zd>(), c->d_B.as<zd>(), c->d_shrec.as<double2>(),
+                            c->d_shcoef.as<zd>(), Uf, U, c->st);
             LAUNCHED(c);
         }
         c->interactions = (long long)R * R * ns * nk;
@@ -1063,6 +1072,10 @@ static size_t estimate_bytes(bs_ctx* c, bool fp64, size_t lut_budget) {
         for (const Sphere& S : c->hs) ncoef += S.Nl + 1;
         b += 2 * B(ncoef * sizeof(zd)) + B(ns * 6 * (size_t)c->Lmax * sizeof(zd));
         b += B(ns * nk * cT) + B(nk * sizeof(float4));        // phases, float directions
+        if (!p.lut_us) {  // direct method: harmonic recurrences, per-wave and per-sphere tables
+            const size_t nlm = (size_t)c->Lmax * (c->Lmax + 1) / 2;
+            b += B(nlm * sizeof(double2)) + B(nk * nlm * sizeof(double2)) + B(ns * nlm * 2 * sizeof(zd));
+        }
     }
     if (p.scalar && p.lut_us && ns > 0) {
         std::vector<Sphere> hs = c->hs;

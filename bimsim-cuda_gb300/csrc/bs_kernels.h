@@ -67,9 +67,15 @@ void launch_us_lut_tex(const Scene& sc, const Sphere* sph, int s0, int s1, int a
 void launch_lut_build_tex(const zd* tab, int rows, int L, const double* P, int Pstride, int thetaR,
                           cudaSurfaceObject_t sre, cudaSurfaceObject_t sim, float2* lin, int lin_stride,
                           cudaStream_t st);
+
+// Direct scattered field through the addition theorem of spherical harmonics:
+// recurrence factors rec, per-wave tables tab (nk x L(L+1)/2), per-sphere
+// coefficients coef (ns x L(L+1)/2 x 2 complex), then the per-pixel sum.
+void launch_sh_tables(const Scene& sc, const Sphere* sph, int L, const double* waves, double2* rec, double2* tab,
+                      zd* coef, cudaStream_t st);
 template <class T>
-void launch_us_direct(const Scene& sc, const Sphere* sph, int lstride, const zd* A, const zd* B, const double* waves,
-                      const cpx<T>* ph, const cpx<T>* Uf, cpx<T>* U, cudaStream_t st);
+void launch_us_sh(const Scene& sc, const Sphere* sph, int L, const zd* A, const zd* B, const double2* rec,
+                  const zd* coef, const cpx<T>* Uf, cpx<T>* U, cudaStream_t st);
 template <class T>
 void launch_sum_only(const Scene& sc, const Sphere* sph, const cpx<T>* Uf, cpx<T>* U, cudaStream_t st);
 // U and Uf (src: U then Uf, R x R each) rotated about the slice centre into dst;

@@ -818,57 +818,148 @@ __global__ void __launch_bounds__(256) lut_build_tex_kernel(const zd* __restrict
 }
 
 // ---------------------------------------------------------------------------
-// Scattered field by recurrences (--recursive; nfScalarUs.cu:17-95, 201-245,
-// 333-491).  The Bessel recurrences depend on (pixel, sphere) only, so they
-// run once per pair in double and give coefficients c_l:
+// Direct scattered field through the addition theorem of spherical harmonics.
+// The per-pixel sum over waves, sum_w pw_w sum_l c_l P_l(k_w . r^), is
+// sum_l c_l Q_l(r^) with Q_l(r^) = sum_w pw_w P_l(k_w . r^).  With the Schmidt
+// semi-normalised associated Legendre functions S_l^m (S_l^m = sqrt(e_m (l-m)!
+// / (l+m)!) P_l^m, e_0 = 1, e_m = 2), P_l(cos g) = sum_{m<=l} S_l^m(cos t1)
+// S_l^m(cos t2) cos(m (f1 - f2)), so
+//   Q_l(r^) = sum_m S_l^m(r_z) (cos(m f_r) C_lm + sin(m f_r) S_lm),
+//   (C_lm, S_lm) = sum_w pw_w S_l^m(k_wz) (cos, sin)(m f_w)   per sphere,
+// with f the azimuth about z.  A (pixel, sphere) pair then costs L (L + 1) / 2
+// terms instead of nk L, and the result is the same sum up to rounding.
+// Tables are in (m, l) order: index(m, l) = m L - m (m - 1) / 2 + (l - m).
+// ---------------------------------------------------------------------------
+__host__ __device__ __forceinline__ int sh_index(int L, int m, int l) { return m * L - m * (m - 1) / 2 + (l - m); }
+
+// Recurrence factors: rec[index(m, l)] = (a, b) with S_l^m = a x S_{l-1}^m - b S_{l-2}^m
+// for l >= m + 2 (a = (2l - 1) / sqrt(l^2 - m^2), b = sqrt((l-1)^2 - m^2) / sqrt(l^2 - m^2)),
+// a = sqrt(2m + 1) for l = m + 1, and for l = m the diagonal factor
+// S_m^m = a sin(t) S_{m-1}^{m-1} (a = 1 for m = 1, sqrt((2m - 1) / (2m)) above).
+__global__ void sh_recur_kernel(int L, double2* __restrict__ rec) {
+    const int m = blockIdx.x, l = m + threadIdx.x;
+    if (m >= L || l >= L) return;
+    double a = 0, b = 0;
+    if (l == m) a = m == 0 ? 1.0 : (m == 1 ? 1.0 : sqrt((2.0 * m - 1.0) / (2.0 * m)));
+    else if (l == m + 1) a = sqrt(2.0 * m + 1.0);
+    else {
+        const double den = sqrt((double)l * l - (double)m * m);
+        a = (2.0 * l - 1.0) / den;
+        b = sqrt((double)(l - 1) * (l - 1) - (double)m * m) / den;
+    }
+    rec[sh_index(L, m, l)] = make_double2(a, b);
+}
+
+// Per wave: tab[w][index(m, l)] = S_l^m(k_z) (cos, sin)(m f_k).
+__global__ void sh_wave_kernel(int nk, int L, const double* __restrict__ waves, const double2* __restrict__ rec,
+                               double2* __restrict__ tab) {
+    const int w = blockIdx.x * blockDim.x + threadIdx.x;
+    if (w >= nk) return;
+    const double kx = waves[3 * w], ky = waves[3 * w + 1], kz = waves[3 * w + 2];
+    const double rho = sqrt(kx * kx + ky * ky);
+    const double cf = rho > 0 ? kx / rho : 1.0, sf = rho > 0 ? ky / rho : 0.0;
+    double2* out = tab + (size_t)w * (L * (L + 1) / 2);
+    double cm = 1, sm = 0, smm = 1;  // cos(m f), sin(m f), S_m^m
+    for (int m = 0; m < L; m++) {
+        if (m > 0) {
+            smm *= rec[sh_index(L, m, m)].x * rho;
+            const double c2 = cm * cf - sm * sf;
+            sm = sm * cf + cm * sf;
+            cm = c2;
+        }
+        double p2 = 0, p1 = smm;
+        for (int l = m; l < L; l++) {
+            double v;
+            if (l == m) v = smm;
+            else if (l == m + 1) v = rec[sh_index(L, m, l)].x * kz * smm;
+            else {
+                const double2 ab = rec[sh_index(L, m, l)];
+                v = ab.x * kz * p1 - ab.y * p2;
+            }
+            if (l > m) {
+                p2 = p1;
+                p1 = v;
+            }
+            out[sh_index(L, m, l)] = make_double2(v * cm, v * sm);
+        }
+    }
+}
+
+// Per sphere s and table index: coef[s][index] = (C, S) = sum_w pw_{s,w} tab[w][index], with the
+// phase pw of phase_kernel in double precision.
+constexpr int SH_WAVES = 128;
+__global__ void sh_coef_kernel(Scene sc, const Sphere* __restrict__ sph, int L, const double* __restrict__ waves,
+                               const double2* __restrict__ tab, zd* __restrict__ coef) {
+    __shared__ zd s_pw[SH_WAVES];
+    const int s = blockIdx.y, nlm = L * (L + 1) / 2;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const double c0 = sph[s].p[0] - sc.focus[0], c1 = sph[s].p[1] - sc.focus[1], c2 = sph[s].p[2] - sc.focus[2];
+    zd ac = mk(0.0, 0.0), as = mk(0.0, 0.0);
+    for (int w0 = 0; w0 < sc.nk; w0 += SH_WAVES) {
+        const int nw = min(SH_WAVES, sc.nk - w0);
+        __syncthreads();
+        for (int t = threadIdx.x; t < nw; t += blockDim.x) {
+            const double* k = waves + 3 * (w0 + t);
+            const double arg = sc.kmag * (k[0] * c0 + k[1] * c1 + k[2] * c2);
+            double sn, cs;
+            sincos(arg, &sn, &cs);
+            s_pw[t] = mk(sc.wave_amp * cs, sc.wave_amp * sn);
+        }
+        __syncthreads();
+        if (i < nlm)
+            for (int t = 0; t < nw; t++) {
+                const double2 v = tab[(size_t)(w0 + t) * nlm + i];
+                ac = ac + s_pw[t] * v.x;
+                as = as + s_pw[t] * v.y;
+            }
+    }
+    if (i < nlm) {
+        coef[((size_t)s * nlm + i) * 2] = ac;
+        coef[((size_t)s * nlm + i) * 2 + 1] = as;
+    }
+}
+
+// Per pixel: U = sum_s sum_l c_l(r) Q_l(r^) (+ Uf outside every sphere)
+// (--recursive; nfScalarUs.cu:17-95, 201-245, 333-491).  The Bessel recurrences
+// depend on (pixel, sphere) only, so they run once per pair in double and give
 //   outside (d > a):  c_l = B_l (j_l + i y_l)(k d)   with the reference clamps
 //   inside  (d <= a): c_l = A_l j_l(k n d)           (c_0 = A_0 only when
 //                                                      Re(k n d) < 1e-6)
-// The per-wave work is then sum_l c_l P_l(k_w . r^), with the Legendre
-// recurrence P_l = ((2l-1) x P_{l-1} - (l-1) P_{l-2}) / l written as
-// a_l x P_{l-1} - b_l P_{l-2} from a per-block table of a_l = (2l-1)/l and
-// b_l = (l-1)/l, which takes the division out of the inner loop.
-// ---------------------------------------------------------------------------
+// where the reference re-runs them for every wave (nfScalarUs.cu:69-93).  All
+// in double precision, stored as T.
+constexpr int SH_BLOCK = 64;
 template <class T>
-__global__ void __launch_bounds__(64) us_direct_kernel(Scene sc, const Sphere* __restrict__ sph, int lstride,
-                                                       const zd* __restrict__ A, const zd* __restrict__ B,
-                                                       const double* __restrict__ waves,
-                                                       const cpx<T>* __restrict__ ph, const cpx<T>* __restrict__ Uf,
-                                                       cpx<T>* __restrict__ U) {
+__global__ void __launch_bounds__(SH_BLOCK) us_sh_kernel(Scene sc, const Sphere* __restrict__ sph, int L,
+                                                         const zd* __restrict__ A, const zd* __restrict__ B,
+                                                         const double2* __restrict__ rec, const zd* __restrict__ coef,
+                                                         const cpx<T>* __restrict__ Uf, cpx<T>* __restrict__ U) {
     extern __shared__ unsigned char smem_raw[];
-    cpx<T>* cl = reinterpret_cast<cpx<T>*>(smem_raw);  // [lstride][blockDim.x]
-    T* la = reinterpret_cast<T*>(cl + (size_t)lstride * blockDim.x);  // [lstride] (2l-1)/l
-    T* lb = la + lstride;                                               // [lstride] (l-1)/l
-    const int tid = threadIdx.x;
-    for (int l = tid; l < lstride; l += blockDim.x) {
-        la[l] = l ? (T)((2.0 * l - 1.0) / l) : (T)0;
-        lb[l] = l ? (T)((l - 1.0) / l) : (T)0;
-    }
-    __syncthreads();
-    int idx = blockIdx.x * blockDim.x + tid;
-    bool valid = idx < sc.R * sc.R;
+    zd* cl = reinterpret_cast<zd*>(smem_raw);  // [L][SH_BLOCK]
+    const int tid = threadIdx.x, nlm = L * (L + 1) / 2;
+    int idx = blockIdx.x * SH_BLOCK + tid;
+    const bool valid = idx < sc.R * sc.R;
     if (!valid) idx = sc.R * sc.R - 1;
     double p[3];
     pixel_pos(sc, idx % sc.R, idx / sc.R, p);
-    T tot_r = 0, tot_i = 0, cmp_r = 0, cmp_i = 0;
+    zd tot = mk(0.0, 0.0), cmp = mk(0.0, 0.0);
     bool outside = true;
     for (int s = 0; s < sc.ns; s++) {
         const Sphere& S = sph[s];
         double r[3];
-        double d = dist_exact(p, S.p, r);
+        const double d = dist_exact(p, S.p, r);
         if (d < S.a) outside = false;
-        int L = S.Nl + 1, Leff = L;
-        const zd* coef;
+        const int Ls = S.Nl + 1;
+        int Leff = Ls;
         if (d <= S.a) {
-            coef = A + S.coef_off;
-            zd knd = mk(sc.kmag * d * S.n_re, sc.kmag * d * S.n_im);
+            const zd* co = A + S.coef_off;
+            const zd knd = mk(sc.kmag * d * S.n_re, sc.kmag * d * S.n_im);
             if (knd.re < EPS_FLOAT) {
                 Leff = 1;
-                cl[tid] = mk((T)coef[0].re, (T)coef[0].im);
+                cl[tid] = co[0];
             } else {
                 zd j0 = zsin(knd) / knd;
                 zd j1 = j0 / knd - zcos(knd) / knd;
-                for (int l = 0; l < L; l++) {
+                for (int l = 0; l < Ls; l++) {
                     zd jl;
                     if (l == 0) {
                         jl = j0;
@@ -876,18 +967,17 @@ __global__ void __launch_bounds__(64) us_direct_kernel(Scene sc, const Sphere* _
                         if (l > 1) sbesselj_step_c(l, knd, j0, j1);
                         jl = j1;
                     }
-                    zd c = coef[l] * jl;
-                    cl[l * blockDim.x + tid] = mk((T)c.re, (T)c.im);
+                    cl[l * SH_BLOCK + tid] = co[l] * jl;
                 }
             }
         } else {
-            coef = B + S.coef_off;
-            double kd = sc.kmag * d;
+            const zd* co = B + S.coef_off;
+            const double kd = sc.kmag * d;
             double sn, cs;
             sincos(kd, &sn, &cs);
             double j0 = sn / kd, j1 = j0 / kd - cs / kd;
             double y0 = -cs / kd, y1 = y0 / kd - sn / kd;
-            for (int l = 0; l < L; l++) {
+            for (int l = 0; l < Ls; l++) {
                 double jl, yl;
                 if (l == 0) {
                     jl = j0;
@@ -900,55 +990,58 @@ __global__ void __launch_bounds__(64) us_direct_kernel(Scene sc, const Sphere* _
                     jl = j1;
                     yl = y1;
                 }
-                zd c = coef[l] * mk(jl, yl);
-                cl[l * blockDim.x + tid] = mk((T)c.re, (T)c.im);
+                cl[l * SH_BLOCK + tid] = co[l] * mk(jl, yl);
             }
         }
-        // direction cosines; at d == 0 only the l = 0 term remains (inside)
-        T rx = 0, ry = 0, rz = 0;
+        // direction of the pixel from the sphere; at d == 0 only l = 0 remains
+        double x = 0, rho = 0, cf = 1, sf = 0;
         if (d != 0) {
-            rx = (T)(r[0] / d);
-            ry = (T)(r[1] / d);
-            rz = (T)(r[2] / d);
-        }
-        const cpx<T>* phs = ph + (size_t)s * sc.nk;
-        T sr = 0, si = 0;
-        for (int w = 0; w < sc.nk; w++) {
-            const double* k = waves + 3 * w;
-            T x = (T)k[0] * rx + (T)k[1] * ry + (T)k[2] * rz;
-            T Pa = 1, Pb = x;
-            cpx<T> c0 = cl[tid];
-            T ur = c0.re, ui = c0.im;
-            if (Leff > 1) {
-                cpx<T> c1 = cl[blockDim.x + tid];
-                ur += c1.re * Pb;
-                ui += c1.im * Pb;
-                for (int l = 2; l < Leff; l++) {
-                    T Pn = la[l] * x * Pb - lb[l] * Pa;
-                    Pa = Pb;
-                    Pb = Pn;
-                    cpx<T> cc = cl[l * blockDim.x + tid];
-                    ur += cc.re * Pb;
-                    ui += cc.im * Pb;
-                }
+            const double rx = r[0] / d, ry = r[1] / d;
+            x = r[2] / d;
+            rho = sqrt(rx * rx + ry * ry);
+            if (rho > 0) {
+                cf = rx / rho;
+                sf = ry / rho;
             }
-            cpx<T> pw = phs[w];
-            sr += pw.re * ur - pw.im * ui;
-            si += pw.re * ui + pw.im * ur;
         }
-        T yr = sr - cmp_r, yi = si - cmp_i;
-        T tr = tot_r + yr, ti = tot_i + yi;
-        cmp_r = (tr - tot_r) - yr;
-        cmp_i = (ti - tot_i) - yi;
-        tot_r = tr;
-        tot_i = ti;
+        const zd* cs_ = coef + (size_t)s * nlm * 2;
+        zd acc = mk(0.0, 0.0);
+        double cm = 1, sm = 0, smm = 1;
+        for (int m = 0; m < Leff; m++) {
+            if (m > 0) {
+                smm *= rec[sh_index(L, m, m)].x * rho;
+                const double c2 = cm * cf - sm * sf;
+                sm = sm * cf + cm * sf;
+                cm = c2;
+            }
+            double p2 = 0, p1 = smm;
+            for (int l = m; l < Leff; l++) {
+                double v;
+                if (l == m) v = smm;
+                else if (l == m + 1) v = rec[sh_index(L, m, l)].x * x * smm;
+                else {
+                    const double2 ab = rec[sh_index(L, m, l)];
+                    v = ab.x * x * p1 - ab.y * p2;
+                }
+                if (l > m) {
+                    p2 = p1;
+                    p1 = v;
+                }
+                const int k = sh_index(L, m, l);
+                const zd C = cs_[2 * k], Sn = cs_[2 * k + 1];
+                const zd q = mk(cm * C.re + sm * Sn.re, cm * C.im + sm * Sn.im) * v;
+                acc = acc + cl[l * SH_BLOCK + tid] * q;
+            }
+        }
+        // Kahan over spheres
+        const zd y = acc - cmp;
+        const zd t = tot + y;
+        cmp = (t - tot) - y;
+        tot = t;
     }
     if (!valid) return;
-    if (outside) {
-        tot_r += Uf[idx].re - cmp_r;
-        tot_i += Uf[idx].im - cmp_i;
-    }
-    U[idx] = mk(tot_r, tot_i);
+    if (outside) tot = tot + (mk((double)Uf[idx].re, (double)Uf[idx].im) - cmp);
+    U[idx] = mk((T)tot.re, (T)tot.im);
 }
 
 // Vector stub of the reference: no scattered field, U = Uf outside every sphere.
@@ -1044,16 +1137,25 @@ void launch_lut_build_tex(const zd* tab, int rows, int L, const double* P, int P
     lut_build_tex_kernel<<<grid, 256, 0, st>>>(tab, rows, L, P, Pstride, thetaR, sre, sim, lin, lin_stride);
 }
 
-template <class T>
-void launch_us_direct(const Scene& sc, const Sphere* sph, int lstride, const zd* A, const zd* B,
-                      const double* waves, const cpx<T>* ph, const cpx<T>* Uf, cpx<T>* U, cudaStream_t st) {
-    const int bt = 64;
-    size_t smem = (size_t)lstride * bt * sizeof(cpx<T>) + 2 * (size_t)lstride * sizeof(T);
-    if (smem > 48 * 1024)
-        cudaFuncSetAttribute(us_direct_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    long long n = (long long)sc.R * sc.R;
-    us_direct_kernel<T><<<blocks_for(n, bt), bt, smem, st>>>(sc, sph, lstride, A, B, waves, ph, Uf, U);
+void launch_sh_tables(const Scene& sc, const Sphere* sph, int L, const double* waves, double2* rec, double2* tab,
+                      zd* coef, cudaStream_t st) {
+    sh_recur_kernel<<<L, ((L + 31) / 32) * 32, 0, st>>>(L, rec);
+    sh_wave_kernel<<<blocks_for(sc.nk, 64), 64, 0, st>>>(sc.nk, L, waves, rec, tab);
+    const int nlm = L * (L + 1) / 2;
+    dim3 grid(blocks_for(nlm, 128), sc.ns);
+    sh_coef_kernel<<<grid, 128, 0, st>>>(sc, sph, L, waves, tab, coef);
 }
+
+template <class T>
+void launch_us_sh(const Scene& sc, const Sphere* sph, int L, const zd* A, const zd* B, const double2* rec,
+                  const zd* coef, const cpx<T>* Uf, cpx<T>* U, cudaStream_t st) {
+    const size_t smem = (size_t)L * SH_BLOCK * sizeof(zd);
+    if (smem > 48 * 1024)
+        cudaFuncSetAttribute(us_sh_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    const long long n = (long long)sc.R * sc.R;
+    us_sh_kernel<T><<<blocks_for(n, SH_BLOCK), SH_BLOCK, smem, st>>>(sc, sph, L, A, B, rec, coef, Uf, U);
+}
+
 
 template <class T>
 void launch_sum_only(const Scene& sc, const Sphere* sph, const cpx<T>* Uf, cpx<T>* U, cudaStream_t st) {
@@ -1105,8 +1207,8 @@ void launch_rotate_fields(int R, float c, float s, const cpx<T>* src, cpx<T>* ds
     template void launch_uf<T>(const Scene&, const double*, cpx<T>*, cudaStream_t);                             \
     template void launch_lut_build<T>(const zd*, int, int, const double*, int, int, Patch<T>*, cudaStream_t);   \
     template void launch_phase<T>(const Scene&, const Sphere*, const double*, cpx<T>*, float4*, cudaStream_t);  \
-    template void launch_us_direct<T>(const Scene&, const Sphere*, int, const zd*, const zd*, const double*,    \
-                                      const cpx<T>*, const cpx<T>*, cpx<T>*, cudaStream_t);                     \
+    template void launch_us_sh<T>(const Scene&, const Sphere*, int, const zd*, const zd*, const double2*,       \
+                                  const zd*, const cpx<T>*, cpx<T>*, cudaStream_t);                           \
     template void launch_sum_only<T>(const Scene&, const Sphere*, const cpx<T>*, cpx<T>*, cudaStream_t);
 BS_INST(float)
 BS_INST(double)
