@@ -188,6 +188,7 @@ struct bs_ctx {
     double bp_d = 0;
     DevBuf d_bp;          // back-propagation phase on the passband grid
     DevBuf d_shrec, d_shtab, d_shcoef;  // direct method: harmonic recurrences, per-wave and per-sphere tables
+    DevBuf d_gscr;        // split-K parts of the detector GEMMs
     bool lut_valid = false;
     std::vector<double> lut_key;
 };
@@ -198,7 +199,7 @@ static std::vector<DevBuf*> ctx_bufs(bs_ctx* c) {
             &c->d_tabscr, &c->d_legP, &c->d_lut, &c->d_uft, &c->d_uftscr, &c->d_fields, &c->d_su,
             &c->d_sv, &c->d_mask, &c->d_wx, &c->d_wy, &c->d_wix, &c->d_wiy, &c->d_f1, &c->d_f2,
             &c->d_g1, &c->d_I, &c->d_D, &c->d_img, &c->d_cones, &c->d_cnt, &c->d_far,
-            &c->d_starts, &c->d_fsave, &c->d_dacc, &c->d_line, &c->d_ringcs, &c->d_bp, &c->d_shrec, &c->d_shtab, &c->d_shcoef};
+            &c->d_starts, &c->d_fsave, &c->d_dacc, &c->d_line, &c->d_ringcs, &c->d_bp, &c->d_shrec, &c->d_shtab, &c->d_shcoef, &c->d_gscr};
 }
 
 static void release_all(bs_ctx* c) {
@@ -463,11 +464,16 @@ static bs_status run_detector(bs_ctx* c, bool accumulate) {
     cpx<T>* g1 = c->d_g1.as<cpx<T>>();
     T* I = c->d_I.as<T>();
     long long RR = (long long)R * R;
-    launch_cgemm<T>(R, Nu, R, 2, fields, R, RR, wx, Nu, 0, f1, Nu, (long long)R * Nu, 0, nullptr, (T)1, nullptr,
-                    c->st);
+    // split-K scratch for the GEMMs with few output tiles
+    const size_t scr = std::max(std::max(cgemm_scratch_elems(R, Nu, R, 2), cgemm_scratch_elems(Nv, Nu, R, 2)),
+                                std::max(cgemm_scratch_elems(Nv, C, Nu, 2), cgemm_scratch_elems(C, C, Nv, 2)));
+    CK(c->d_gscr.ensure(std::max<size_t>(scr, 1) * ce));
+    cpx<T>* gs = c->d_gscr.as<cpx<T>>();
+    launch_cgemm<T>(R, Nu, R, 2, fields, R, RR, wx, Nu, 0, f1, Nu, (long long)R * Nu, 0, nullptr, (T)1, nullptr, gs,
+                    scr, c->st);
     LAUNCHED(c);
     launch_cgemm<T>(Nv, Nu, R, 2, wy, R, 0, f1, Nu, (long long)R * Nu, f2, Nu, (long long)Nv * Nu, 1,
-                    c->d_mask.as<float>(), (T)1, nullptr, c->st);
+                    c->d_mask.as<float>(), (T)1, nullptr, gs, scr, c->st);
     LAUNCHED(c);
     if (c->bp_on) {
         // applyBackpropagation (microscope.cu:423-470, 592-605) on U only: -exp(i kz d) with
@@ -488,11 +494,11 @@ static bs_status run_detector(bs_ctx* c, bool accumulate) {
         CK(cudaStreamSynchronize(c->st));  // bp is a host vector of this scope
     }
     launch_cgemm<T>(Nv, C, Nu, 2, f2, Nu, (long long)Nv * Nu, wix, C, 0, g1, C, (long long)Nv * C, 0, nullptr, (T)1,
-                    nullptr, c->st);
+                    nullptr, gs, scr, c->st);
     LAUNCHED(c);
     T scale = (T)(1.0 / ((double)R * (double)R));
     launch_cgemm<T>(C, C, Nv, 2, wiy, Nv, 0, g1, C, (long long)Nv * C, nullptr, C, (long long)C * C, 2, nullptr,
-                    scale, I, c->st);
+                    scale, I, gs, scr, c->st);
     LAUNCHED(c);
     launch_bin<T>(res, c->ss, 2, accumulate ? 1 : 0, I, c->d_D.as<T>(), c->st);
     LAUNCHED(c);
@@ -1120,6 +1126,10 @@ static size_t estimate_bytes(bs_ctx* c, bool fp64, size_t lut_budget) {
         b += B(Nu * sizeof(int)) + B(Nv * sizeof(int)) + B(Nv * Nu * sizeof(float));
         b += B(R * Nu * cT) + B(Nv * R * cT) + B(Nu * C * cT) + B(C * Nv * cT);
         b += B(2 * R * Nu * cT) + B(2 * Nv * Nu * cT) + B(2 * Nv * C * cT) + B(2 * C * C * rT);
+        const int Ri = (int)R, Ui = (int)Nu, Vi = (int)Nv, Ci = (int)C;
+        const size_t scr = std::max(std::max(cgemm_scratch_elems(Ri, Ui, Ri, 2), cgemm_scratch_elems(Vi, Ui, Ri, 2)),
+                                    std::max(cgemm_scratch_elems(Vi, Ci, Ui, 2), cgemm_scratch_elems(Ci, Ci, Vi, 2)));
+        b += B(std::max<size_t>(scr, 1) * cT);  // split-K parts
     }
     b += B(res * res * rT);                                   // image staging
     return b;
@@ -1288,7 +1298,7 @@ static bs_status far_field(bs_ctx* c, int which, double* host) {
     const T scale = (T)(1.0 / ((double)c->R * (double)c->R));
     const cpx<T>* g1 = c->d_g1.as<cpx<T>>() + (size_t)which * Nv * C;
     launch_cgemm<T>(C, C, Nv, 1, c->d_wiy.as<cpx<T>>(), Nv, 0, g1, C, 0, c->d_far.as<cpx<T>>(), C, 0, 3, nullptr,
-                    scale, nullptr, c->st);
+                    scale, nullptr, c->d_gscr.as<cpx<T>>(), c->d_gscr.n / sizeof(cpx<T>), c->st);
     LAUNCHED(c);
     std::vector<cpx<T>> t(n);
     CK(cudaMemcpyAsync(t.data(), c->d_far.p, n * sizeof(cpx<T>), cudaMemcpyDeviceToHost, c->st));

@@ -13,6 +13,8 @@
 // at the end.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "bs_kernels.h"
 #include "bs_math.cuh"
 
@@ -35,33 +37,61 @@ __global__ void twiddle_kernel(int ni, int nj, const int* __restrict__ freq, int
 // partial sums combined with Kahan compensation.
 constexpr int GB_M = 64, GB_N = 32, GB_K = 16;
 
+// Epilogue of one output element c of batch b: epi 0 store, 1 store times the
+// band-pass mask, 2 |scale c|^2 into I, 3 store scale c.
+template <class T>
+__device__ __forceinline__ void cgemm_store(int epi, long long o, int gm, int gn, int N, T vr, T vi,
+                                            cpx<T>* __restrict__ C, const float* __restrict__ mask, T scale,
+                                            T* __restrict__ I) {
+    if (epi == 2) {
+        vr *= scale;
+        vi *= scale;
+        I[o] = vr * vr + vi * vi;
+    } else if (epi == 3) {  // scaled field (the far field Ud, Ufd)
+        C[o] = mk(vr * scale, vi * scale);
+    } else {
+        if (epi == 1) {
+            T mval = (T)mask[(long long)gm * N + gn];
+            vr *= mval;
+            vi *= mval;
+        }
+        C[o] = mk(vr, vi);
+    }
+}
+
+// ksplit > 1 (few output tiles, long K): block z = b * ksplit + ks sums the
+// ks-th of ksplit equal K ranges into part[b][ks][M][N]; cgemm_reduce_kernel
+// adds the ranges in order (deterministic) and applies the epilogue.
 template <class T>
 __global__ void __launch_bounds__(256) cgemm_kernel(int M, int N, int K, const cpx<T>* __restrict__ A, int lda,
                                                     long long sA, const cpx<T>* __restrict__ B, int ldb, long long sB,
                                                     cpx<T>* __restrict__ C, int ldc, long long sC, int epi,
-                                                    const float* __restrict__ mask, T scale, T* __restrict__ I) {
+                                                    const float* __restrict__ mask, T scale, T* __restrict__ I,
+                                                    int ksplit, cpx<T>* __restrict__ part) {
     __shared__ cpx<T> As[GB_K][GB_M + 1];
     __shared__ cpx<T> Bs[GB_K][GB_N + 1];
-    const int b = blockIdx.z;
+    const int b = blockIdx.z / ksplit, ks = blockIdx.z % ksplit;
     A += b * sA;
     B += b * sB;
     const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
     const int m0 = blockIdx.y * GB_M, n0 = blockIdx.x * GB_N;
+    const int kc = ((K + ksplit - 1) / ksplit + GB_K - 1) / GB_K * GB_K;  // K range per split, whole tiles
+    const int kbeg = ks * kc, kend = min(K, kbeg + kc);
     T accr[4][2], acci[4][2], cr[4][2], ci[4][2];
 #pragma unroll
     for (int i = 0; i < 4; i++)
 #pragma unroll
         for (int j = 0; j < 2; j++) accr[i][j] = acci[i][j] = cr[i][j] = ci[i][j] = 0;
-    for (int k0 = 0; k0 < K; k0 += GB_K) {
+    for (int k0 = kbeg; k0 < kend; k0 += GB_K) {
         for (int e = threadIdx.x; e < GB_K * GB_M; e += 256) {
             int kk = e % GB_K, mm = e / GB_K;
             int gm = m0 + mm, gk = k0 + kk;
-            As[kk][mm] = (gm < M && gk < K) ? A[(long long)gm * lda + gk] : mk((T)0, (T)0);
+            As[kk][mm] = (gm < M && gk < kend) ? A[(long long)gm * lda + gk] : mk((T)0, (T)0);
         }
         for (int e = threadIdx.x; e < GB_K * GB_N; e += 256) {
             int nn = e % GB_N, kk = e / GB_N;
             int gn = n0 + nn, gk = k0 + kk;
-            Bs[kk][nn] = (gn < N && gk < K) ? B[(long long)gk * ldb + gn] : mk((T)0, (T)0);
+            Bs[kk][nn] = (gn < N && gk < kend) ? B[(long long)gk * ldb + gn] : mk((T)0, (T)0);
         }
         __syncthreads();
         T pr[4][2], pi[4][2];
@@ -103,23 +133,32 @@ __global__ void __launch_bounds__(256) cgemm_kernel(int M, int N, int K, const c
         for (int j = 0; j < 2; j++) {
             int gm = m0 + ty + 16 * i, gn = n0 + tx + 16 * j;
             if (gm >= M || gn >= N) continue;
-            T vr = accr[i][j], vi = acci[i][j];
-            long long o = b * sC + (long long)gm * ldc + gn;
-            if (epi == 2) {
-                vr *= scale;
-                vi *= scale;
-                I[o] = vr * vr + vi * vi;
-            } else if (epi == 3) {  // scaled field (the far field Ud, Ufd)
-                C[o] = mk(vr * scale, vi * scale);
-            } else {
-                if (epi == 1) {
-                    T mval = (T)mask[(long long)gm * N + gn];
-                    vr *= mval;
-                    vi *= mval;
-                }
-                C[o] = mk(vr, vi);
-            }
+            if (ksplit > 1)
+                part[((long long)blockIdx.z * M + gm) * N + gn] = mk(accr[i][j], acci[i][j]);
+            else
+                cgemm_store(epi, b * sC + (long long)gm * ldc + gn, gm, gn, N, accr[i][j], acci[i][j], C, mask, scale,
+                            I);
         }
+}
+
+template <class T>
+__global__ void cgemm_reduce_kernel(int M, int N, int batch, int ksplit, const cpx<T>* __restrict__ part,
+                                    cpx<T>* __restrict__ C, int ldc, long long sC, int epi,
+                                    const float* __restrict__ mask, T scale, T* __restrict__ I) {
+    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= (long long)batch * M * N) return;
+    const int b = (int)(e / ((long long)M * N)), gm = (int)(e / N % M), gn = (int)(e % N);
+    T sr = 0, si = 0, cr = 0, ci = 0;  // Kahan over the K ranges, in order
+    for (int ks = 0; ks < ksplit; ks++) {
+        const cpx<T> v = part[(((long long)b * ksplit + ks) * M + gm) * N + gn];
+        const T yr = v.re - cr, yi = v.im - ci;
+        const T tr = sr + yr, ti = si + yi;
+        cr = (tr - sr) - yr;
+        ci = (ti - si) - yi;
+        sr = tr;
+        si = ti;
+    }
+    cgemm_store(epi, b * sC + (long long)gm * ldc + gn, gm, gn, N, sr, si, C, mask, scale, I);
 }
 
 template <class T>
@@ -156,12 +195,40 @@ void launch_twiddle(int ni, int nj, const int* freq, int off_i, int R, int sign,
     twiddle_kernel<T><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(ni, nj, freq, off_i, R, sign, ld_i, ld_j, out);
 }
 
+// Splits of K for a GEMM with few output tiles: enough blocks for about two per
+// SM, each split at least 4 K tiles long, at most 64 splits.
+int cgemm_ksplit(int M, int N, int K, int batch) {
+    static int sms[64] = {0};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    int& n_sm = sms[dev & 63];
+    if (n_sm == 0 && cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) n_sm = 1;
+    const long long tiles = (long long)((N + GB_N - 1) / GB_N) * ((M + GB_M - 1) / GB_M) * batch;
+    if (tiles <= 0 || tiles >= n_sm) return 1;
+    long long ks = (2LL * n_sm + tiles - 1) / tiles;
+    ks = std::min<long long>(ks, std::max(1, K / (4 * GB_K)));
+    return (int)std::min<long long>(ks, 64);
+}
+
+size_t cgemm_scratch_elems(int M, int N, int K, int batch) {
+    const int ks = cgemm_ksplit(M, N, K, batch);
+    return ks > 1 ? (size_t)batch * ks * M * N : 0;
+}
+
 template <class T>
 void launch_cgemm(int M, int N, int K, int batch, const cpx<T>* A, int lda, long long sA, const cpx<T>* B, int ldb,
                   long long sB, cpx<T>* C, int ldc, long long sC, int epi, const float* mask, T scale, T* I,
-                  cudaStream_t st) {
-    dim3 grid((N + GB_N - 1) / GB_N, (M + GB_M - 1) / GB_M, batch);
-    cgemm_kernel<T><<<grid, 256, 0, st>>>(M, N, K, A, lda, sA, B, ldb, sB, C, ldc, sC, epi, mask, scale, I);
+                  cpx<T>* scratch, size_t scratch_elems, cudaStream_t st) {
+    int ks = cgemm_ksplit(M, N, K, batch);
+    if ((size_t)batch * ks * M * N > scratch_elems || !scratch) ks = 1;
+    dim3 grid((N + GB_N - 1) / GB_N, (M + GB_M - 1) / GB_M, batch * ks);
+    cgemm_kernel<T><<<grid, 256, 0, st>>>(M, N, K, A, lda, sA, B, ldb, sB, C, ldc, sC, epi, mask, scale, I, ks,
+                                          scratch);
+    if (ks > 1) {
+        const long long n = (long long)batch * M * N;
+        cgemm_reduce_kernel<T><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(M, N, batch, ks, scratch, C, ldc, sC, epi,
+                                                                            mask, scale, I);
+    }
 }
 
 template <class T>
@@ -323,7 +390,8 @@ void launch_cmul(int n, const cpx<T>* a, cpx<T>* x, cudaStream_t st) {
 #define BS_DET_INST(T)                                                                                          \
     template void launch_twiddle<T>(int, int, const int*, int, int, int, int, int, cpx<T>*, cudaStream_t);      \
     template void launch_cgemm<T>(int, int, int, int, const cpx<T>*, int, long long, const cpx<T>*, int,       \
-                                  long long, cpx<T>*, int, long long, int, const float*, T, T*, cudaStream_t); \
+                                  long long, cpx<T>*, int, long long, int, const float*, T, T*, cpx<T>*,       \
+                                  size_t, cudaStream_t);                                                        \
     template void launch_bin<T>(int, int, int, int, const T*, T*, cudaStream_t);                                    \
     template void launch_image<T>(int, int, const T*, const T*, T*, cudaStream_t);                             \
     template void launch_rotate_add_images<T>(int, float, float, const T*, T*, cudaStream_t);                 \

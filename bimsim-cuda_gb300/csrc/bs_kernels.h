@@ -93,10 +93,14 @@ void launch_twiddle(int ni, int nj, const int* freq, int off_i, int R, int sign,
 // blockIdx.z with element strides sA, sB, sC (0 = shared operand).
 // epi 0: store; epi 1: multiply by mask[m*N + n]; epi 2: store |scale * c|^2
 // into the real array I[b] (M x N, batch stride sC); epi 3: store scale * c.
+// GEMMs with fewer output tiles than SMs split K over more blocks and add the
+// parts in a fixed order (deterministic) when `scratch` holds
+// cgemm_scratch_elems(M, N, K, batch) elements; else one block per tile.
+size_t cgemm_scratch_elems(int M, int N, int K, int batch);
 template <class T>
 void launch_cgemm(int M, int N, int K, int batch, const cpx<T>* A, int lda, long long sA, const cpx<T>* B, int ldb,
                   long long sB, cpx<T>* C, int ldc, long long sC, int epi, const float* mask, T scale, T* I,
-                  cudaStream_t st);
+                  cpx<T>* scratch, size_t scratch_elems, cudaStream_t st);
 
 // D[b][iv][iu] (+)= sum over the ss x ss block of I[b] / ss^2 (fieldslice.cu:71-108);
 // accumulate adds to D (the detector sums point sources)
