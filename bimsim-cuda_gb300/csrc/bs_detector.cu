@@ -198,11 +198,10 @@ void launch_twiddle(int ni, int nj, const int* freq, int off_i, int R, int sign,
 // Splits of K for a GEMM with few output tiles: enough blocks for about two per
 // SM, each split at least 4 K tiles long, at most 64 splits.
 int cgemm_ksplit(int M, int N, int K, int batch) {
-    static int sms[64] = {0};
-    int dev = 0;
-    cudaGetDevice(&dev);
-    int& n_sm = sms[dev & 63];
-    if (n_sm == 0 && cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) n_sm = 1;
+    int dev = 0, n_sm = 1;  // attribute queries are cheap host calls; no shared cache between threads
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev) !=
+                                                   cudaSuccess)
+        n_sm = 1;
     const long long tiles = (long long)((N + GB_N - 1) / GB_N) * ((M + GB_M - 1) / GB_M) * batch;
     if (tiles <= 0 || tiles >= n_sm) return 1;
     long long ks = (2LL * n_sm + tiles - 1) / tiles;
