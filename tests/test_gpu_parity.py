@@ -44,6 +44,19 @@ def scene(name):
                             lut_us=False, lut_uf=True)
         s = [(0.3, -0.2, 0, 2.2, 1.5, 0.04), (5.0, 4.0, 1.0, 1.0, 1.3, 0.0)]
         return p, s, w(20, 0, 0.6, seed=5)
+    if name == "direct_large":
+        # ka = 62.8 (81 orders) through the sphere's centre plane: the harmonic recurrences to l = 81
+        p = abi.make_params(lam=2.0, condenser=(0, 0.5), objective=(0, 0.5), xy=(60, 0), resolution=16, padding=1,
+                            lut_us=False)
+        return p, [(1.0, -2.0, 0.0, 20.0, 1.4, 0.02)], w(24, 0, 0.5, seed=13)
+    if name == "direct_oblique":
+        # oblique incidence and an xz plane: pixel and wave directions far from the harmonic axis
+        k = (np.sin(0.4), 0.2, np.cos(0.4))
+        k = tuple(np.array(k) / np.linalg.norm(k))
+        p = abi.make_params(lam=2.5, k_dir=k, condenser=(0.1, 0.45), objective=(0, 0.5),
+                            plane=((-6, 0, -6), (6, 0, 6), (0, -1, 0)), resolution=12, padding=1, lut_us=False)
+        return p, [(0.5, 1.0, -0.5, 1.6, 1.35, 0.02), (-2.0, -1.5, 2.0, 1.1, 1.5, 0.0)], w(28, 0.1, 0.45, seed=16,
+                                                                                           kdir=k)
     if name == "plane_wave":
         p = abi.make_params(lam=2.0, condenser=(0, 0.5), objective=(0, 0.8), xy=(12, 0), resolution=16, padding=1,
                             plane_wave=True, us_lut_theta=256)
@@ -82,8 +95,8 @@ def scene(name):
     raise KeyError(name)
 
 
-ALL = ["lut", "lut_ufLUT", "direct_cfg1", "direct_multi", "plane_wave", "oblique_xz", "vector", "no_spheres",
-       "supersample", "lut_staged", "lut_many_rows"]
+ALL = ["lut", "lut_ufLUT", "direct_cfg1", "direct_multi", "direct_large", "direct_oblique", "plane_wave",
+       "oblique_xz", "vector", "no_spheres", "supersample", "lut_staged", "lut_many_rows"]
 _oracle_cache = {}
 
 
