@@ -1351,6 +1351,7 @@ bs_status bs_material_kk(const char* path, double n0, int32_t n_samples, int32_t
     const int N = n_samples ? n_samples : (int)lam.size();
     if (N < 2 || N > BS_KK_MAX_SAMPLES)
         return fail(BS_ERR_ARG, "bs_material_kk: %d samples (2 to %d)", N, BS_KK_MAX_SAMPLES);
+    if (pf > 16) return fail(BS_ERR_ARG, "bs_material_kk: padding factor %d above 16", pf);
     const int M = N * pf;
     // resample kappa at evenly spaced wavenumbers, from the shortest wavelength up (material.h:294-316)
     const double nu_min = 10000.0 / (double)lam.back(), nu_max = 10000.0 / (double)lam.front();
