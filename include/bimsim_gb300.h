@@ -234,7 +234,7 @@ bs_status bs_material_eval(const char* path, const double* lambdas, int32_t n, d
  * at most BS_KK_MAX_SAMPLES) wavenumbers evenly spaced from 1e4 / lambda_min
  * down to 1e4 / lambda_max; chi2 = -alpha n0 / k with k = 2 pi / lambda and
  * alpha = 2 k kappa in single precision (the reference's float k and alpha);
- * chi2 zero-padded to pf * n_samples points goes through the reference's FFT
+ * chi2 zero-padded to pf * n_samples points (pf 1 to 16) goes through the reference's FFT
  * Hilbert transform (x i for 0 < f < M/2, x -i for f >= M/2, DC removed,
  * inverse / M), here as the equivalent circular convolution on the GPU in
  * double precision; n = Re(chi1) / (2 n0) + n0.  Outputs: the sample

@@ -88,3 +88,5 @@ def test_gpu_kk_rejects_bad_arguments(tmp_path):
         lib.material_kk(path, 1.5, 16385, 2)
     with pytest.raises(BimsimError):
         lib.material_kk(tmp_path / "missing.txt", 1.5)
+    with pytest.raises(BimsimError):
+        lib.material_kk(path, 1.5, 64, 17)
