@@ -887,11 +887,13 @@ static bs_status run_nearfield(bs_ctx* c) {
         launch_mie(c->d_sph.as<Sphere>(), ns, sc.kmag, c->d_mie.as<zd>(), c->Lmax, c->d_A.as<zd>(),
                    c->d_B.as<zd>(), c->st);
         LAUNCHED(c);
-        CK(c->d_ph.ensure((size_t)ns * nk * sizeof(cpx<T>)));
-        CK(c->d_kw4.ensure((size_t)nk * sizeof(float4)));
-        launch_phase<T>(sc, c->d_sph.as<Sphere>(), c->d_waves.as<double>(), c->d_ph.as<cpx<T>>(),
-                        c->d_kw4.as<float4>(), c->st);
-        LAUNCHED(c);
+        if (p.lut_us) {  // the LUT kernels' phases and float directions (the direct method forms its own)
+            CK(c->d_ph.ensure((size_t)ns * nk * sizeof(cpx<T>)));
+            CK(c->d_kw4.ensure((size_t)nk * sizeof(float4)));
+            launch_phase<T>(sc, c->d_sph.as<Sphere>(), c->d_waves.as<double>(), c->d_ph.as<cpx<T>>(),
+                            c->d_kw4.as<float4>(), c->st);
+            LAUNCHED(c);
+        }
     } else if (ns > 0) {
         CK(cudaMemcpyAsync(c->d_sph.p, c->hs.data(), ns * sizeof(Sphere), cudaMemcpyHostToDevice, c->st));
     }
@@ -1077,7 +1079,7 @@ static size_t estimate_bytes(bs_ctx* c, bool fp64, size_t lut_budget) {
         size_t ncoef = 0;
         for (const Sphere& S : c->hs) ncoef += S.Nl + 1;
         b += 2 * B(ncoef * sizeof(zd)) + B(ns * 6 * (size_t)c->Lmax * sizeof(zd));
-        b += B(ns * nk * cT) + B(nk * sizeof(float4));        // phases, float directions
+        if (p.lut_us) b += B(ns * nk * cT) + B(nk * sizeof(float4));  // phases, float directions
         if (!p.lut_us) {  // direct method: harmonic recurrences, per-wave and per-sphere tables
             const size_t nlm = (size_t)c->Lmax * (c->Lmax + 1) / 2;
             b += B(nlm * sizeof(double2)) + B(nk * nlm * sizeof(double2)) + B(ns * nlm * 2 * sizeof(zd));
