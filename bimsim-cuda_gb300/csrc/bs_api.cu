@@ -189,6 +189,7 @@ struct bs_ctx {
     DevBuf d_bp;          // back-propagation phase on the passband grid
     DevBuf d_shrec, d_shtab, d_shcoef;  // direct method: harmonic recurrences, per-wave and per-sphere tables
     DevBuf d_gscr;        // split-K parts of the detector GEMMs
+    DevBuf d_ufw;         // condenser aperture factor per order of the incident field
     bool lut_valid = false;
     std::vector<double> lut_key;
 };
@@ -199,7 +200,7 @@ static std::vector<DevBuf*> ctx_bufs(bs_ctx* c) {
             &c->d_tabscr, &c->d_legP, &c->d_lut, &c->d_uft, &c->d_uftscr, &c->d_fields, &c->d_su,
             &c->d_sv, &c->d_mask, &c->d_wx, &c->d_wy, &c->d_wix, &c->d_wiy, &c->d_f1, &c->d_f2,
             &c->d_g1, &c->d_I, &c->d_D, &c->d_img, &c->d_cones, &c->d_cnt, &c->d_far,
-            &c->d_starts, &c->d_fsave, &c->d_dacc, &c->d_line, &c->d_ringcs, &c->d_bp, &c->d_shrec, &c->d_shtab, &c->d_shcoef, &c->d_gscr};
+            &c->d_starts, &c->d_fsave, &c->d_dacc, &c->d_line, &c->d_ringcs, &c->d_bp, &c->d_shrec, &c->d_shtab, &c->d_shcoef, &c->d_gscr, &c->d_ufw};
 }
 
 static void release_all(bs_ctx* c) {
@@ -861,8 +862,30 @@ static bs_status run_nearfield(bs_ctx* c) {
         launch_uf_table(sc, c->d_uft.as<double>(), c->d_uftscr.as<double>(), c->st);
         LAUNCHED(c);
     }
-    launch_uf<T>(sc, c->d_uft.as<double>(), Uf, c->st);
-    LAUNCHED(c);
+    {
+        // condenser aperture factor of each order, the same for every pixel (nfScalarUf.cu:46-175)
+        std::vector<double> w(sc.m + 1);
+        double a0 = 1, a1 = sc.cos_a, a2 = 1, b0 = 1, b1 = sc.cos_b, b2 = 1;
+        auto step = [](int n, double x, double& q0, double& q1) {  // rts/math/legendre.h:17-25
+            const double qn = ((2 * n - 1) * x * q1 - (n - 1) * q0) / n;
+            q0 = q1;
+            q1 = qn;
+        };
+        for (int l = 0; l <= sc.m; l++) {
+            if (l > 0) {
+                a2 = a0;
+                step(l + 1, sc.cos_a, a0, a1);
+                b2 = b0;
+                step(l + 1, sc.cos_b, b0, b1);
+            }
+            w[l] = a1 - a2 - b1 + b2;
+        }
+        CK(c->d_ufw.ensure(w.size() * sizeof(double)));
+        CK(cudaMemcpyAsync(c->d_ufw.p, w.data(), w.size() * sizeof(double), cudaMemcpyHostToDevice, c->st));
+        launch_uf<T>(sc, c->d_uft.as<double>(), c->d_ufw.as<double>(), Uf, c->st);
+        LAUNCHED(c);
+        CK(cudaStreamSynchronize(c->st));  // w is a host vector of this scope
+    }
     cudaEventRecord(c->ev[1], c->st);
 
     // ---- LUT placement (before the sphere table goes to the device) ----
@@ -1075,6 +1098,7 @@ static size_t estimate_bytes(bs_ctx* c, bool fp64, size_t lut_budget) {
     b += B(std::max<size_t>(1, ns) * sizeof(Sphere));
     b += B((p.plane_wave ? 1 : nk) * 3 * sizeof(double));     // directions
     if (p.lut_uf && !p.plane_wave && p.scalar) b += 2 * B((size_t)sc.uf_dR * (sc.m + 1) * sizeof(double));
+    b += B((size_t)(sc.m + 1) * sizeof(double));               // incident-field aperture factors
     if (p.scalar && ns > 0) {
         size_t ncoef = 0;
         for (const Sphere& S : c->hs) ncoef += S.Nl + 1;

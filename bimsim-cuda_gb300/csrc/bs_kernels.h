@@ -37,7 +37,7 @@ struct alignas(8 * sizeof(T)) Patch {
 
 // ---- near field ----
 template <class T>
-void launch_uf(const Scene& sc, const double* tab, cpx<T>* Uf, cudaStream_t st);
+void launch_uf(const Scene& sc, const double* tab, const double* w, cpx<T>* Uf, cudaStream_t st);
 void launch_uf_table(const Scene& sc, double* tab, double* scratch, cudaStream_t st);
 void launch_mie(const Sphere* sph, int ns, double k, zd* scratch, int lstride, zd* A, zd* B, cudaStream_t st);
 // spheres [s0, s0 + n) in one launch; starts (device): first global row of each

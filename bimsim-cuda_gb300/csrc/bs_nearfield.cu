@@ -36,7 +36,9 @@ __device__ __forceinline__ double dist_exact(const double p[3], const double c[3
 // ---------------------------------------------------------------------------
 // gpuScalarUf, nfScalarUf.cu:46-175: Debye-focused field as a Legendre series
 // over l = 0..m with the clamped upward j_l recurrence.
-__device__ zd uf_direct(const Scene& sc, const double p[3]) {
+// w[l] = (P_{l+1} - P_{l-1})(cos a) - (P_{l+1} - P_{l-1})(cos b) of the condenser
+// aperture does not depend on the pixel: the host computes it once per run.
+__device__ zd uf_direct(const Scene& sc, const double* __restrict__ w, const double p[3]) {
     double r[3];
     double d = dist_exact(p, sc.focus, r);
     if (d < EPS_FLOAT) return mk(sc.amp * 2 * PI_REF * (sc.cos_a - sc.cos_b), 0.0);
@@ -47,7 +49,6 @@ __device__ zd uf_direct(const Scene& sc, const double p[3]) {
     sincos(kd, &s, &c);
     double j0 = s / kd, j1 = j0 / kd - c / kd;
     double P0 = 1, P1 = cth;
-    double a0 = 1, a1 = sc.cos_a, a2 = 1, b0 = 1, b1 = sc.cos_b, b2 = 1;
     zd sum = mk(0.0, 0.0), il = mk(1.0, 0.0);
     for (int l = 0; l <= sc.m; l++) {
         double jl, Pl;
@@ -57,22 +58,13 @@ __device__ zd uf_direct(const Scene& sc, const double p[3]) {
         } else if (l == 1) {
             jl = j1;
             Pl = P1;
-            a2 = a0;
-            legendre_step(l + 1, sc.cos_a, a0, a1);
-            b2 = b0;
-            legendre_step(l + 1, sc.cos_b, b0, b1);
         } else {
             sbesselj_step(l, kd, j0, j1);
             legendre_step(l, cth, P0, P1);
             jl = j1;
             Pl = P1;
-            a2 = a0;
-            legendre_step(l + 1, sc.cos_a, a0, a1);
-            b2 = b0;
-            legendre_step(l + 1, sc.cos_b, b0, b1);
         }
-        double w = jl * Pl * (a1 - a2 - b1 + b2);
-        sum = sum + il * w;
+        sum = sum + il * (jl * Pl * w[l]);
         il = il * mk(0.0, 1.0);
     }
     return sum * (2.0 * PI_REF * sc.amp);
@@ -80,7 +72,8 @@ __device__ zd uf_direct(const Scene& sc, const double p[3]) {
 
 // gpuScalarUfLut, nfScalarUfLut.cu:11-123: j_l(k d) read from the table with
 // linear filtering along d (texture y) and exact order (texture x = l + 0.5).
-__device__ zd uf_lut(const Scene& sc, const double* __restrict__ tab, const double p[3]) {
+__device__ zd uf_lut(const Scene& sc, const double* __restrict__ tab, const double* __restrict__ w,
+                     const double p[3]) {
     double r[3];
     double d = dist_exact(p, sc.focus, r);
     if (d == 0) return mk(sc.amp * 2 * PI_REF * (sc.cos_a - sc.cos_b), 0.0);
@@ -95,7 +88,6 @@ __device__ zd uf_lut(const Scene& sc, const double* __restrict__ tab, const doub
     const double* t0 = tab + (size_t)i0 * L;
     const double* t1 = tab + (size_t)i1 * L;
     double P0 = 1, P1 = cth;
-    double a0 = 1, a1 = sc.cos_a, a2 = 1, b0 = 1, b1 = sc.cos_b, b2 = 1;
     zd sum = mk(0.0, 0.0), il = mk(1.0, 0.0);
     for (int l = 0; l <= sc.m; l++) {
         double jl = (1 - be) * t0[l] + be * t1[l];
@@ -105,20 +97,16 @@ __device__ zd uf_lut(const Scene& sc, const double* __restrict__ tab, const doub
         } else {
             if (l > 1) legendre_step(l, cth, P0, P1);
             Pl = P1;
-            a2 = a0;
-            legendre_step(l + 1, sc.cos_a, a0, a1);
-            b2 = b0;
-            legendre_step(l + 1, sc.cos_b, b0, b1);
         }
-        double w = jl * Pl * (a1 - a2 - b1 + b2);
-        sum = sum + il * w;
+        sum = sum + il * (jl * Pl * w[l]);
         il = il * mk(0.0, 1.0);
     }
     return sum * (2.0 * PI_REF * sc.amp);
 }
 
 template <class T>
-__global__ void uf_kernel(Scene sc, const double* __restrict__ tab, cpx<T>* __restrict__ Uf) {
+__global__ void uf_kernel(Scene sc, const double* __restrict__ tab, const double* __restrict__ w,
+                          cpx<T>* __restrict__ Uf) {
     int idx = blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= sc.R * sc.R) return;
     double p[3];
@@ -134,9 +122,9 @@ __global__ void uf_kernel(Scene sc, const double* __restrict__ tab, cpx<T>* __re
         sincos(kr, &s, &c);
         v = mk(c * sc.amp, s * sc.amp);
     } else if (sc.lut_uf) {
-        v = uf_lut(sc, tab, p);
+        v = uf_lut(sc, tab, w, p);
     } else {
-        v = uf_direct(sc, p);
+        v = uf_direct(sc, w, p);
     }
     Uf[idx] = mk((T)v.re, (T)v.im);
 }
@@ -1068,9 +1056,9 @@ __global__ void sum_only_kernel(Scene sc, const Sphere* __restrict__ sph, const 
 static inline unsigned blocks_for(long long n, int b) { return (unsigned)((n + b - 1) / b); }
 
 template <class T>
-void launch_uf(const Scene& sc, const double* tab, cpx<T>* Uf, cudaStream_t st) {
+void launch_uf(const Scene& sc, const double* tab, const double* w, cpx<T>* Uf, cudaStream_t st) {
     long long n = (long long)sc.R * sc.R;
-    uf_kernel<T><<<blocks_for(n, 128), 128, 0, st>>>(sc, tab, Uf);
+    uf_kernel<T><<<blocks_for(n, 128), 128, 0, st>>>(sc, tab, w, Uf);
 }
 
 void launch_uf_table(const Scene& sc, double* tab, double* scratch, cudaStream_t st) {
@@ -1205,7 +1193,7 @@ void launch_rotate_fields(int R, float c, float s, const cpx<T>* src, cpx<T>* ds
 
 #define BS_INST(T)                                                                                              \
     template void launch_rotate_fields<T>(int, float, float, const cpx<T>*, cpx<T>*, cudaStream_t);             \
-    template void launch_uf<T>(const Scene&, const double*, cpx<T>*, cudaStream_t);                             \
+    template void launch_uf<T>(const Scene&, const double*, const double*, cpx<T>*, cudaStream_t);              \
     template void launch_lut_build<T>(const zd*, int, int, const double*, int, int, Patch<T>*, cudaStream_t);   \
     template void launch_phase<T>(const Scene&, const Sphere*, const double*, cpx<T>*, float4*, cudaStream_t);  \
     template void launch_us_sh<T>(const Scene&, const Sphere*, int, const zd*, const zd*, const double2*,       \
