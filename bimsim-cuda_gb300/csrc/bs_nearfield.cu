@@ -537,7 +537,7 @@ __global__ void __launch_bounds__(UST_BLOCK, STAGE ? 4 : 6) us_lut_tex_kernel(Sc
                                                                     int chunk) {
     extern __shared__ float2 s_stage[];
     __shared__ float4 s_k[UST_CHUNK];
-    __shared__ float4 s_p[UST_CHUNK];  // phase (x, x, y, y): lane pairs for the packed products
+    __shared__ float2 s_p[UST_CHUNK];
     __shared__ int s_red[4][UST_BLOCK / 32];
     __shared__ TileSphere s_ts;
     __shared__ int2 s_plan;  // staged window of the next chunk: first column, width (0: texture path)
@@ -668,12 +668,7 @@ __global__ void __launch_bounds__(UST_BLOCK, STAGE ? 4 : 6) us_lut_tex_kernel(Sc
             const bool staged = STAGE && W > 0;
             if (threadIdx.x < nw) {
                 copy_async16(&s_k[threadIdx.x], kw4 + w0 + threadIdx.x);
-                const float* pv = reinterpret_cast<const float*>(ph + (size_t)s * sc.nk + w0 + threadIdx.x);
-                float* dp = reinterpret_cast<float*>(&s_p[threadIdx.x]);
-                copy_async4(dp, pv);
-                copy_async4(dp + 1, pv);
-                copy_async4(dp + 2, pv + 1);
-                copy_async4(dp + 3, pv + 1);
+                copy_async8(&s_p[threadIdx.x], reinterpret_cast<const float2*>(ph + (size_t)s * sc.nk + w0) + threadIdx.x);
             }
             if (STAGE && staged) {
                 // asynchronous copies, one table row per warp at a time, all in flight together
@@ -716,9 +711,9 @@ __global__ void __launch_bounds__(UST_BLOCK, STAGE ? 4 : 6) us_lut_tex_kernel(Sc
                     const f32x2 a0 = f2_fma(bep, f2_sub(e01, e00), e00);
                     const f32x2 a1 = f2_fma(bep, f2_sub(e11, e10), e10);
                     const f32x2 v = f2_fma(alp, f2_sub(a1, a0), a0);
-                    const ulonglong2 pw = reinterpret_cast<const ulonglong2*>(s_p)[w];  // (x, x), (y, y)
-                    ax = f2_fma(pw.x, v, ax);
-                    ay = f2_fma(pw.y, v, ay);
+                    const float2 pw = s_p[w];
+                    ax = f2_fma(f2_splat(pw.x), v, ax);
+                    ay = f2_fma(f2_splat(pw.y), v, ay);
                 }
                 sx = f2_unpack(ax);
                 sy = f2_unpack(ay);
@@ -737,11 +732,11 @@ __global__ void __launch_bounds__(UST_BLOCK, STAGE ? 4 : 6) us_lut_tex_kernel(Sc
                     const float ai0 = fmaf(be, gi.z - gi.w, gi.w), ai1 = fmaf(be, gi.y - gi.x, gi.x);
                     const float vr = fmaf(al, ar1 - ar0, ar0);
                     const float vi = fmaf(al, ai1 - ai0, ai0);
-                    const float4 pw = s_p[w];
+                    const float2 pw = s_p[w];
                     sx.x = fmaf(pw.x, vr, sx.x);
                     sx.y = fmaf(pw.x, vi, sx.y);
-                    sy.x = fmaf(pw.z, vr, sy.x);
-                    sy.y = fmaf(pw.z, vi, sy.y);
+                    sy.x = fmaf(pw.y, vr, sy.x);
+                    sy.y = fmaf(pw.y, vi, sy.y);
                 }
             }
             const float ar = sx.x - sy.y, ai = sx.y + sy.x;
