@@ -359,7 +359,7 @@ def run_gb300(args):
                      "hbm_peak_gbs": peaks.get("hbm_gbs"), "fp64_peak_tflops": fp64_tf,
                      "why_not_hbm_or_tensor": "no step is a dense contraction (no tensor-core use) and the kernel "
                                               "reads ~0.13 TB/s of DRAM: it is bound by the shared-memory (L1TEX) "
-                                              "pipe feeding its FP32 arithmetic (ncu: L1TEX 92 %, FMA pipe 42 %), so "
+                                              "pipe feeding its FP32 arithmetic (ncu: L1TEX 90 %, FMA pipe 45 %), so "
                                               "the roofline is the measured FP32 FMA peak; the DRAM view is "
                                               "roofline_hbm"},
         "roofline_hbm": (None if not (profile_traffic() and peaks.get("hbm_gbs")) else
