@@ -175,6 +175,27 @@ def test_staged_and_texture_kernels_give_identical_bits(name, chunk):
     assert np.array_equal(a["U"], b["U"]) and np.array_equal(a["D"], b["D"])
 
 
+@pytest.mark.parametrize("chunk", [16, 32, 64])
+def test_wave_groups_with_a_short_last_chunk(chunk):
+    """150 waves: full chunks plus one short group (22 or 6 waves) last, staged and texture kernels
+    alike, within the mixed tolerance of the oracle."""
+    p, s, _ = scene("lut_staged")
+    w = scenes.mc_waves(150, 0, 0.5, seed=17)
+    U, _, D, _ = oracle_lib.simulate(p, *abi.sphere_array(s), w)
+    out = {}
+    for staging in (1, 2):
+        with Context(p) as ctx:
+            ctx.set_spheres(s)
+            ctx.set_waves(w)
+            ctx.set_lut_staging(staging)
+            ctx.set_lut_wave_chunk(chunk)
+            ctx.simulate(BS_PREC_MIXED)
+            out[staging] = (ctx.field(BS_FIELD_TOTAL), ctx.image(BS_IMG_INTENSITY, f64=True), ctx.stats())
+    assert out[1][2].lut_chunks_staged > 0
+    assert np.array_equal(out[1][0], out[2][0])
+    assert rel(out[1][0], U) <= TOL_MIXED_FIELD and rel(out[1][1], D) <= TOL_MIXED_IMG
+
+
 def test_wave_chunk_choice():
     """The run's chunk is one of 64, 32, 16 (64 when the texture-only kernel runs); a fixed chunk is kept;
     every chunk size gives the oracle's result within the mixed tolerance."""
