@@ -407,8 +407,9 @@ __global__ void __launch_bounds__(128) us_lut_f64_kernel(Scene sc, const Sphere*
 // float, per-chunk partial sums combined with Kahan compensation.
 //
 // A block owns a 16 x 16 pixel tile, one pixel per thread.  The waves arrive
-// sorted along a Hilbert curve and are processed in chunks of UST_CHUNK; the
-// host gives each chunk a bounding cone (axis c_k, half-angle beta_k).  For a
+// grouped by direction into compact chunks of `chunk` waves (64, 32 or 16) and
+// are processed chunk by chunk; the host gives each chunk a bounding cone
+// (axis c_k, half-angle beta_k).  For a
 // tile whose pixels all lie outside the sphere and see it within an angle
 // gamma of the tile-centre direction r_c, every lookup angle of a chunk lies
 // in angle(c_k, r_c) +- (beta_k + gamma) (triangle inequality on the sphere of
