@@ -245,6 +245,7 @@ def run_gb300(args):
         launches += st.kernel_launches
     clocks = sampler.stop()
     staged = st.lut_chunks_staged / st.lut_chunks_total if st.lut_chunks_total else 0.0
+    wave_chunk = st.lut_wave_chunk
     total = sum(times)
     if dist:
         t = torch.tensor([total], device=dev)
@@ -355,7 +356,7 @@ def run_gb300(args):
                      "peak_source": "measured FP32 FMA loop on this GPU (bs_measure_fma_peak)",
                      "work": f"{FLOP_PER_LOOKUP} flop x {lookups} (pixel, sphere, wave) lookups per launch",
                      "launch_ms": us_s * 1e3, "lookups_per_s": lookups / us_s,
-                     "staged_fraction": staged,
+                     "staged_fraction": staged, "wave_chunk": wave_chunk,
                      "hbm_peak_gbs": peaks.get("hbm_gbs"), "fp64_peak_tflops": fp64_tf,
                      "why_not_hbm_or_tensor": "no step is a dense contraction (no tensor-core use) and the kernel "
                                               "reads ~0.13 TB/s of DRAM: it is bound by the shared-memory (L1TEX) "
