@@ -101,6 +101,16 @@ def profile_traffic():
         return None
 
 
+def profile_wavefronts():
+    """Shared-memory wavefronts per launch of the dominant kernel from the committed ncu summary."""
+    path = os.path.join(REPO, "profiles", "us_lut_tex_config2.md")
+    try:
+        m = re.search(r"shared_wavefronts_per_launch:\s*([0-9.eE+]+)", open(path).read())
+        return float(m.group(1)) if m else None
+    except OSError:
+        return None
+
+
 def measured_peaks():
     try:
         return json.load(open(os.path.join(REPO, "MEASURED_PEAKS.json")))
@@ -244,6 +254,7 @@ def run_gb300(args):
         us_ms.append(st.ms_us)
         launches += st.kernel_launches
     clocks = sampler.stop()
+    n_sm = torch.cuda.get_device_properties(dev).multi_processor_count
     staged = st.lut_chunks_staged / st.lut_chunks_total if st.lut_chunks_total else 0.0
     wave_chunk = st.lut_wave_chunk
     total = sum(times)
@@ -370,6 +381,16 @@ def run_gb300(args):
                           "traffic": profile_traffic(), "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)",
                           "note": "DRAM bytes of one full launch (ncu, profiles/us_lut_tex_config2.md) over this "
                                   "run's launch time"}),
+        # the shared-memory (L1TEX data) pipe retires one 128-byte wavefront per SM per cycle
+        "roofline_l1": (None if not (profile_wavefronts() and not args.small and clocks.get("sm_mhz")) else
+                        {"bound": "shared-memory wavefronts", "kernel": "us_lut_tex_kernel",
+                         "unit": "wavefronts per SM per cycle",
+                         "achieved": profile_wavefronts() / (us_s * clocks["sm_mhz"] * 1e6 * n_sm),
+                         "peak": 1.0,
+                         "frac": profile_wavefronts() / (us_s * clocks["sm_mhz"] * 1e6 * n_sm),
+                         "wavefronts": profile_wavefronts(),
+                         "note": "shared wavefronts of one full launch (ncu, profiles/us_lut_tex_config2.md) "
+                                 "over this run's launch time at the sampled SM clock"}),
         "mixed_vs_fp64_rel_l2": {"value": rel, "absorbance": rel_a, "tolerance": 1e-5, "case": case},
         "fp64_plain": fp64,
         "clocks": clocks,
