@@ -341,21 +341,35 @@ void launch_line_image(int res, int L, const T* line, T* D, cudaStream_t st) {
 // reference multiplies the FFT of the zero-padded chi2 (M points) by i for
 // 0 < f < M/2, by -i for f >= M/2 and by 0 at f = 0, transforms back and
 // divides by M.  For real chi2 the real part of that is a circular convolution
-// with g(m) = (1/M) (sum_{0<f<M/2} -sin(2 pi f m / M) + sum_{f>=M/2} sin(2 pi f m / M)),
-// computed here directly in double precision (sinpi of the exactly reduced
-// argument 2 (f m mod M) / M).
+// with g(m) = (1/M) (sum_{0<f<M/2} -sin(2 pi f m / M) + sum_{f>=M/2} sin(2 pi f m / M)).
+// The sines of a whole period add to zero, so g(m) = -(2/M) sum_{f=1}^{K} sin(2 pi f m / M)
+// with K = ceil(M/2) - 1, and the finite sum has the closed form
+// sin(K t) sin((K+1) t) / sin(t), t = pi m / M (g(0) = 0).  Each sine is reduced in
+// integers to sinpi of a ratio in [0, 1/2], so that rounding the ratio costs one ulp
+// relative (near a / M = 1 the rounded ratio would lose the small distance to 1,
+// and sin(t) for m = M - 1 is the divisor).  Double precision throughout.
 // ---------------------------------------------------------------------------
+__device__ __forceinline__ double sinpi_ratio(long long a, long long M) {  // sin(pi a / M), a >= 0
+    long long r = a % (2 * M);
+    double sign = 1.0;
+    if (r >= M) {
+        r -= M;
+        sign = -1.0;
+    }
+    if (2 * r > M) r = M - r;
+    return sign * sinpi((double)r / (double)M);
+}
+
 __global__ void kk_kernel_g(int M, double* __restrict__ g) {
     const int m = blockIdx.x * blockDim.x + threadIdx.x;
     if (m >= M) return;
-    const int half = (M + 1) / 2;  // f < M / 2.0  <=>  f < half
-    double acc = 0;
-    for (int f = 1; f < M; f++) {
-        const long long r = ((long long)f * m) % M;
-        const double sn = sinpi(2.0 * (double)r / (double)M);
-        acc += f < half ? -sn : sn;
+    if (m == 0) {
+        g[0] = 0;
+        return;
     }
-    g[m] = acc / (double)M;
+    const long long K = (M + 1) / 2 - 1;
+    const double num = sinpi_ratio(K * m, M) * sinpi_ratio((K + 1) * m, M);
+    g[m] = -2.0 * (num / sinpi_ratio(m, M)) / (double)M;
 }
 
 __global__ void kk_kernel_conv(int N, int M, const double* __restrict__ chi2, const double* __restrict__ g,

@@ -65,7 +65,7 @@ def test_oracle_absorption_band_gives_dispersion():
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("n_samples,pf", [(0, 2), (256, 2), (300, 3), (64, 1)])
+@pytest.mark.parametrize("n_samples,pf", [(0, 2), (256, 2), (300, 3), (64, 1), (16384, 16), (16384, 3)])
 def test_gpu_kk_matches_oracle(tmp_path, n_samples, pf):
     path = tmp_path / "band.txt"
     lam_f, _ = lorentz_file(path)
