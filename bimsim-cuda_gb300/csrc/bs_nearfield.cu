@@ -423,7 +423,10 @@ __global__ void __launch_bounds__(128) us_lut_f64_kernel(Scene sc, const Sphere*
 // (i, j) in x, y, z, w.  Both paths interpolate with the same single-precision
 // formula, so they give the same bits; edge cells clamp like the reference's
 // texture fetch.
-constexpr int UST_BLOCK = 256;      // 16 x 16 pixel tile
+constexpr int UST_TILE = 256;           // 16 x 16 pixel tile
+// pixels per thread of the staged kernel: 128 threads at 128 registers, 4 blocks per SM (one pixel
+// per thread: 2 % slower; four: 19 %; two at 96 registers and 5 blocks per SM: 11 %)
+constexpr int UST_STAGED_PPT = 2;
 
 // Fractional LUT angle index t = acos(c) tsc for c in [-1, 1] (c is clamped),
 // tsc = (thetaR - 1) / PI_REF, tscpi = tsc * pi.  acos(x) = sqrt(1 - x) g(x)
@@ -523,9 +526,12 @@ __device__ __forceinline__ int2 chunk_plan(const float4 cone, const TileSphere& 
 }
 
 // STAGE = false: texture path only, no dynamic shared memory (the L1 keeps
-// its full size for the texture cache) and 6 blocks per SM.
-template <bool STAGE>
-__global__ void __launch_bounds__(UST_BLOCK, STAGE ? 4 : 6) us_lut_tex_kernel(Scene sc, const Sphere* __restrict__ sph, int s0, int s1,
+// its full size for the texture cache) and 6 blocks per SM.  PPT pixels per
+// thread: the tile's eight 4 x 8 warp blocks are spread over 8 / PPT warps, and
+// each wave's direction and phase (shared-memory broadcasts) are read once for
+// the thread's PPT pixels.  Every pixel's arithmetic is the same for any PPT.
+template <bool STAGE, int PPT>
+__global__ void __launch_bounds__(UST_TILE / PPT, STAGE ? 4 : 6) us_lut_tex_kernel(Scene sc, const Sphere* __restrict__ sph, int s0, int s1,
                                                                     int accumulate, int finalize,
                                                                     const float4* __restrict__ kw4,
                                                                     const float4* __restrict__ cones,
@@ -536,21 +542,32 @@ __global__ void __launch_bounds__(UST_BLOCK, STAGE ? 4 : 6) us_lut_tex_kernel(Sc
                                                                     cpx<float>* __restrict__ U,
                                                                     unsigned long long* __restrict__ counters,
                                                                     int chunk) {
+    constexpr int NT = UST_TILE / PPT, NWARP = NT / 32;
+    static_assert(NT >= UST_CHUNK && NT % 32 == 0, "one thread per wave of a chunk");
     extern __shared__ float2 s_stage[];
     __shared__ float4 s_k[UST_CHUNK];
     __shared__ float2 s_p[UST_CHUNK];
-    __shared__ int s_red[4][UST_BLOCK / 32];
+    __shared__ int s_red[4][NWARP];
     __shared__ TileSphere s_ts;
     __shared__ int2 s_plan;  // staged window of the next chunk: first column, width (0: texture path)
     __shared__ double s_pa[3][16], s_pb[3][16];  // pixel position = s_pa[.][column] + s_pb[.][row]
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    // each warp covers a 4 x 8 pixel block of the 16 x 16 tile, its half-warps 4 x 4: the compact
-    // footprint has the fewest shared-memory bank conflicts (8 x 4 blocks: 1 % slower, 16 x 2: 22 %)
+    // the tile is covered by eight 4 x 8 pixel blocks (half-warps 4 x 4): the compact footprint of
+    // one load instruction has the fewest shared-memory bank conflicts (8 x 4 blocks: 1 % slower,
+    // 16 x 2: 22 %).  Pixel j of a thread lies in block warp + NWARP j.
     const int tiles_u = (sc.R + 15) / 16;
     const int tu = (blockIdx.x % tiles_u) * 16, tv = (blockIdx.x / tiles_u) * 16;
-    const int iu = tu + (lane & 3) + 4 * (warp & 3);
-    const int iv = tv + (lane >> 2) + 8 * (warp >> 2);
-    const bool valid = iu < sc.R && iv < sc.R;
+    int iu[PPT], iv[PPT], lu[PPT], lv[PPT];
+    bool valid[PPT];
+#pragma unroll
+    for (int j = 0; j < PPT; j++) {
+        const int blk = warp + NWARP * j;
+        iu[j] = tu + (lane & 3) + 4 * (blk & 3);
+        iv[j] = tv + (lane >> 2) + 8 * (blk >> 2);
+        valid[j] = iu[j] < sc.R && iv[j] < sc.R;
+        lu[j] = min(iu[j], sc.R - 1) - tu;
+        lv[j] = min(iv[j], sc.R - 1) - tv;
+    }
     // pixel_pos computes (A + X u) + Y v: the terms of the tile's 16 columns and 16 rows, once
     if (threadIdx.x < 32) {
         const int k = threadIdx.x & 15;
@@ -562,34 +579,46 @@ __global__ void __launch_bounds__(UST_BLOCK, STAGE ? 4 : 6) us_lut_tex_kernel(Sc
         }
     }
     __syncthreads();
-    const int lu = min(iu, sc.R - 1) - tu, lv = min(iv, sc.R - 1) - tv;
-    float tot_r = 0.f, tot_i = 0.f, cmp_r = 0.f, cmp_i = 0.f;  // Kahan sum over chunk partials
-    if (accumulate && valid) {
-        tot_r = U[iv * sc.R + iu].re;
-        tot_i = U[iv * sc.R + iu].im;
+    float tot_r[PPT], tot_i[PPT], cmp_r[PPT], cmp_i[PPT];  // Kahan sums over chunk partials
+#pragma unroll
+    for (int j = 0; j < PPT; j++) {
+        tot_r[j] = tot_i[j] = cmp_r[j] = cmp_i[j] = 0.f;
+        if (accumulate && valid[j]) {
+            tot_r[j] = U[iv[j] * sc.R + iu[j]].re;
+            tot_i[j] = U[iv[j] * sc.R + iu[j]].im;
+        }
     }
     const int nchunks = (sc.nk + chunk - 1) / chunk;
     unsigned staged_chunks = 0;
     for (int s = s0; s < s1; s++) {
         const Sphere& S = sph[s];
-        double p[3], r[3];
+        float rx[PPT], ry[PPT], rz[PPT], cb[PPT], al[PPT], y[PPT];
+        int ir[PPT], ktex[PPT];
+        bool far[PPT];  // outside the sphere, d > 0
 #pragma unroll
-        for (int c = 0; c < 3; c++) p[c] = __dadd_rn(s_pa[c][lu], s_pb[c][lv]);
-        const double d = dist_exact(p, S.p, r);
-        const TableSel ts = select_table_scaled(S, d);
-        const int ir = (int)floor(ts.x);
-        const float al = (float)(ts.x - ir);
-        const float y = (float)ir + 1.0f;  // gather footprint rows ir, ir + 1
-        const int k = 4 * (s - s0) + (d < S.a ? 2 : 0);
-        const cudaTextureObject_t tre = tex[k], tim = tex[k + 1];
-        float rx = 0.f, ry = 0.f, rz = 0.f, cb = 1.f;  // d == 0: cos(theta) := 1
-        if (d != 0) {
-            const float inv = 1.f / (float)d;
-            rx = (float)r[0] * inv;
-            ry = (float)r[1] * inv;
-            rz = (float)r[2] * inv;
-            cb = 0.f;
+        for (int j = 0; j < PPT; j++) {
+            double p[3], r[3];
+#pragma unroll
+            for (int c = 0; c < 3; c++) p[c] = __dadd_rn(s_pa[c][lu[j]], s_pb[c][lv[j]]);
+            const double d = dist_exact(p, S.p, r);
+            const TableSel ts = select_table_scaled(S, d);
+            ir[j] = (int)floor(ts.x);
+            al[j] = (float)(ts.x - ir[j]);
+            y[j] = (float)ir[j] + 1.0f;  // gather footprint rows ir, ir + 1
+            ktex[j] = 4 * (s - s0) + (d < S.a ? 2 : 0);
+            rx[j] = ry[j] = rz[j] = 0.f;
+            cb[j] = 1.f;  // d == 0: cos(theta) := 1
+            if (d != 0) {
+                const float inv = 1.f / (float)d;
+                rx[j] = (float)r[0] * inv;
+                ry[j] = (float)r[1] * inv;
+                rz[j] = (float)r[2] * inv;
+                cb[j] = 0.f;
+            }
+            far[j] = d >= S.a && d != 0;
         }
+        // every pixel of a staged tile lies outside the sphere: its table is Usp (dR rows)
+        const int rows = S.dR;
         // ---- tile bounds: table rows and angular radius gamma ----
         int rlo = 0, rhi = 0, ok = 0;
         if (!STAGE) {
@@ -606,18 +635,24 @@ __global__ void __launch_bounds__(UST_BLOCK, STAGE ? 4 : 6) us_lut_tex_kernel(Sc
             float cy = (float)sc.A[1] + (float)sc.X[1] * u + (float)sc.Y[1] * v - (float)S.p[1];
             float cz = (float)sc.A[2] + (float)sc.X[2] * u + (float)sc.Y[2] * v - (float)S.p[2];
             const float cl = sqrtf(cx * cx + cy * cy + cz * cz);
-            bool far_ok = valid ? (d >= S.a && d != 0) : true;
+            bool far_ok = cl > 0.f;
             float gam = 0.f;
             if (cl > 0.f) {
                 cx /= cl;
                 cy /= cl;
                 cz /= cl;
-                if (valid) gam = acosf(fminf(fmaxf(rx * cx + ry * cy + rz * cz, -1.f), 1.f));
-            } else {
-                far_ok = false;
             }
-            rlo = valid ? ir : INT_MAX;
-            rhi = valid ? ir : INT_MIN;
+            rlo = INT_MAX;
+            rhi = INT_MIN;
+#pragma unroll
+            for (int j = 0; j < PPT; j++) {
+                if (!valid[j]) continue;
+                far_ok = far_ok && far[j];
+                if (cl > 0.f)
+                    gam = fmaxf(gam, acosf(fminf(fmaxf(rx[j] * cx + ry[j] * cy + rz[j] * cz, -1.f), 1.f)));
+                rlo = min(rlo, ir[j]);
+                rhi = max(rhi, ir[j]);
+            }
             rlo = __reduce_min_sync(0xffffffffu, rlo);
             rhi = __reduce_max_sync(0xffffffffu, rhi);
             int gbits = (int)__reduce_max_sync(0xffffffffu, (unsigned)__float_as_int(gam));
@@ -631,7 +666,7 @@ __global__ void __launch_bounds__(UST_BLOCK, STAGE ? 4 : 6) us_lut_tex_kernel(Sc
             }
             __syncthreads();
 #pragma unroll
-            for (int w = 0; w < UST_BLOCK / 32; w++) {
+            for (int w = 0; w < NWARP; w++) {
                 rlo = min(rlo, s_red[0][w]);
                 rhi = max(rhi, s_red[1][w]);
                 gbits = max(gbits, s_red[2][w]);
@@ -646,17 +681,21 @@ __global__ void __launch_bounds__(UST_BLOCK, STAGE ? 4 : 6) us_lut_tex_kernel(Sc
                 s_ts.tscpi = (float)((S.thetaR - 1) / PI_REF * TRUE_PI);
                 // staged rows: [rlo, rhi + 1] clamped to the table
                 s_ts.rlo = rlo;
-                s_ts.nrows = ok ? min(rhi + 1, ts.rows - 1) - rlo + 1 : 0;
+                s_ts.nrows = ok ? min(rhi + 1, rows - 1) - rlo + 1 : 0;
                 s_ts.thetaR = S.thetaR;
                 s_ts.lin_stride = S.lin_stride;
-                s_ts.off = ts.off;
+                s_ts.off = S.usp_off;
                 s_plan = chunk_plan(cones[0], s_ts);
             }
         }
-        // local rows of this pixel in the staged block (clamped, so always in bounds)
-        const int nrows_b = ok ? min(rhi + 1, ts.rows - 1) - rlo + 1 : 1;
-        const int lr0 = min(max(ir - rlo, 0), max(nrows_b, 1) - 1);
-        const int lr1 = min(max(min(ir + 1, ts.rows - 1) - rlo, 0), max(nrows_b, 1) - 1);
+        // local rows of each pixel in the staged block (clamped, so always in bounds)
+        const int nrows_b = ok ? min(rhi + 1, rows - 1) - rlo + 1 : 1;
+        int lr0[PPT], drow0[PPT];
+#pragma unroll
+        for (int j = 0; j < PPT; j++) {
+            lr0[j] = min(max(ir[j] - rlo, 0), max(nrows_b, 1) - 1);
+            drow0[j] = min(max(min(ir[j] + 1, rows - 1) - rlo, 0), max(nrows_b, 1) - 1) - lr0[j];
+        }
         for (int ch = 0; ch < nchunks; ch++) {
             const int w0 = ch * chunk;
             const int nw = min(chunk, sc.nk - w0);
@@ -675,7 +714,7 @@ __global__ void __launch_bounds__(UST_BLOCK, STAGE ? 4 : 6) us_lut_tex_kernel(Sc
                 // asynchronous copies, one table row per warp at a time, all in flight together
                 const float2* table = lin + s_ts.off + (size_t)s_ts.rlo * s_ts.lin_stride + t_lo;
                 const int ls = s_ts.lin_stride;
-                for (int rr = warp; rr < nrows; rr += UST_BLOCK / 32) {
+                for (int rr = warp; rr < nrows; rr += NWARP) {
                     const float2* src = table + (size_t)rr * ls;
                     float2* dst = s_stage + rr * Ws;
                     for (int tt = lane; tt < W; tt += 32) copy_async8(dst + tt, src + tt);
@@ -689,93 +728,121 @@ __global__ void __launch_bounds__(UST_BLOCK, STAGE ? 4 : 6) us_lut_tex_kernel(Sc
             const float tsc = s_ts.tsc, tscpi = s_ts.tscpi;
             // the chunk's sum of pw v as sum(pw.x v) and sum(pw.y v), each a (re, im) pair:
             // Re = x.re - y.im, Im = x.im + y.re
-            float2 sx, sy;
+            float2 sx[PPT], sy[PPT];
             if (STAGE && staged) {
                 staged_chunks++;
-                const float2* row0 = s_stage + lr0 * Ws;
-                const int drow = (lr1 - lr0) * Ws;
                 const unsigned lt_max = (unsigned)(W - 2);
-                const f32x2 alp = f2_splat(al);
-                f32x2 ax = 0ull, ay = 0ull;
-#pragma unroll 8
+                const float2* row0[PPT];
+                int drow[PPT];
+                f32x2 alp[PPT], ax[PPT], ay[PPT];
+#pragma unroll
+                for (int j = 0; j < PPT; j++) {
+                    row0[j] = s_stage + lr0[j] * Ws;
+                    drow[j] = drow0[j] * Ws;
+                    alp[j] = f2_splat(al[j]);
+                    ax[j] = ay[j] = 0ull;
+                }
+#pragma unroll(8 / PPT)
                 for (int w = 0; w < nw; w++) {
                     const float4 kk = s_k[w];
-                    const float c = fmaf(kk.x, rx, fmaf(kk.y, ry, kk.z * rz));  // cb = 0: every d > 0 here
-                    const float t = theta_index(c, tsc, tscpi);
-                    const float tf = floorf(t);
-                    const float be = t - tf;
-                    // in the window by construction; the unsigned clamp only keeps a bad bound in bounds
-                    const unsigned lt = min((unsigned)((int)tf - t_lo), lt_max);
-                    const f32x2* q = reinterpret_cast<const f32x2*>(row0 + lt);
-                    const f32x2 e00 = q[0], e01 = q[1], e10 = q[drow], e11 = q[drow + 1];
-                    const f32x2 bep = f2_splat(be);
-                    const f32x2 a0 = f2_fma(bep, f2_sub(e01, e00), e00);
-                    const f32x2 a1 = f2_fma(bep, f2_sub(e11, e10), e10);
-                    const f32x2 v = f2_fma(alp, f2_sub(a1, a0), a0);
                     const float2 pw = s_p[w];
-                    ax = f2_fma(f2_splat(pw.x), v, ax);
-                    ay = f2_fma(f2_splat(pw.y), v, ay);
+                    const f32x2 pwx = f2_splat(pw.x), pwy = f2_splat(pw.y);
+#pragma unroll
+                    for (int j = 0; j < PPT; j++) {
+                        const float c = fmaf(kk.x, rx[j], fmaf(kk.y, ry[j], kk.z * rz[j]));  // cb = 0: every d > 0 here
+                        const float t = theta_index(c, tsc, tscpi);
+                        const float tf = floorf(t);
+                        const float be = t - tf;
+                        // in the window by construction; the unsigned clamp only keeps a bad bound in bounds
+                        const unsigned lt = min((unsigned)((int)tf - t_lo), lt_max);
+                        const f32x2* q = reinterpret_cast<const f32x2*>(row0[j] + lt);
+                        const f32x2 e00 = q[0], e01 = q[1], e10 = q[drow[j]], e11 = q[drow[j] + 1];
+                        const f32x2 bep = f2_splat(be);
+                        const f32x2 a0 = f2_fma(bep, f2_sub(e01, e00), e00);
+                        const f32x2 a1 = f2_fma(bep, f2_sub(e11, e10), e10);
+                        const f32x2 v = f2_fma(alp[j], f2_sub(a1, a0), a0);
+                        ax[j] = f2_fma(pwx, v, ax[j]);
+                        ay[j] = f2_fma(pwy, v, ay[j]);
+                    }
                 }
-                sx = f2_unpack(ax);
-                sy = f2_unpack(ay);
+#pragma unroll
+                for (int j = 0; j < PPT; j++) {
+                    sx[j] = f2_unpack(ax[j]);
+                    sy[j] = f2_unpack(ay[j]);
+                }
             } else {
-                sx = sy = make_float2(0.f, 0.f);
+                cudaTextureObject_t tre[PPT], tim[PPT];
+#pragma unroll
+                for (int j = 0; j < PPT; j++) {
+                    sx[j] = sy[j] = make_float2(0.f, 0.f);
+                    tre[j] = tex[ktex[j]];
+                    tim[j] = tex[ktex[j] + 1];
+                }
 #pragma unroll 1
                 for (int w = 0; w < nw; w++) {
                     const float4 kk = s_k[w];
-                    const float c = fmaf(kk.x, rx, fmaf(kk.y, ry, fmaf(kk.z, rz, cb)));
-                    const float t = theta_index(c, tsc, tscpi);
-                    const float tf = floorf(t);
-                    const float be = t - tf;
-                    const float4 gr = tex2Dgather<float4>(tre, tf + 1.0f, y, 0);
-                    const float4 gi = tex2Dgather<float4>(tim, tf + 1.0f, y, 0);
-                    const float ar0 = fmaf(be, gr.z - gr.w, gr.w), ar1 = fmaf(be, gr.y - gr.x, gr.x);
-                    const float ai0 = fmaf(be, gi.z - gi.w, gi.w), ai1 = fmaf(be, gi.y - gi.x, gi.x);
-                    const float vr = fmaf(al, ar1 - ar0, ar0);
-                    const float vi = fmaf(al, ai1 - ai0, ai0);
                     const float2 pw = s_p[w];
-                    sx.x = fmaf(pw.x, vr, sx.x);
-                    sx.y = fmaf(pw.x, vi, sx.y);
-                    sy.x = fmaf(pw.y, vr, sy.x);
-                    sy.y = fmaf(pw.y, vi, sy.y);
+#pragma unroll
+                    for (int j = 0; j < PPT; j++) {
+                        const float c = fmaf(kk.x, rx[j], fmaf(kk.y, ry[j], fmaf(kk.z, rz[j], cb[j])));
+                        const float t = theta_index(c, tsc, tscpi);
+                        const float tf = floorf(t);
+                        const float be = t - tf;
+                        const float4 gr = tex2Dgather<float4>(tre[j], tf + 1.0f, y[j], 0);
+                        const float4 gi = tex2Dgather<float4>(tim[j], tf + 1.0f, y[j], 0);
+                        const float ar0 = fmaf(be, gr.z - gr.w, gr.w), ar1 = fmaf(be, gr.y - gr.x, gr.x);
+                        const float ai0 = fmaf(be, gi.z - gi.w, gi.w), ai1 = fmaf(be, gi.y - gi.x, gi.x);
+                        const float vr = fmaf(al[j], ar1 - ar0, ar0);
+                        const float vi = fmaf(al[j], ai1 - ai0, ai0);
+                        sx[j].x = fmaf(pw.x, vr, sx[j].x);
+                        sx[j].y = fmaf(pw.x, vi, sx[j].y);
+                        sy[j].x = fmaf(pw.y, vr, sy[j].x);
+                        sy[j].y = fmaf(pw.y, vi, sy[j].y);
+                    }
                 }
             }
-            const float ar = sx.x - sy.y, ai = sx.y + sy.x;
-            // Kahan: add the chunk partial to the running total
-            const float yr = ar - cmp_r, yi = ai - cmp_i;
-            const float tr = tot_r + yr, ti = tot_i + yi;
-            cmp_r = (tr - tot_r) - yr;
-            cmp_i = (ti - tot_i) - yi;
-            tot_r = tr;
-            tot_i = ti;
+#pragma unroll
+            for (int j = 0; j < PPT; j++) {
+                const float ar = sx[j].x - sy[j].y, ai = sx[j].y + sy[j].x;
+                // Kahan: add the chunk partial to the running total
+                const float yr = ar - cmp_r[j], yi = ai - cmp_i[j];
+                const float tr = tot_r[j] + yr, ti = tot_i[j] + yi;
+                cmp_r[j] = (tr - tot_r[j]) - yr;
+                cmp_i[j] = (ti - tot_i[j]) - yi;
+                tot_r[j] = tr;
+                tot_i[j] = ti;
+            }
         }
     }
     if (threadIdx.x == 0 && counters) {
         atomicAdd(counters, (unsigned long long)staged_chunks);
         atomicAdd(counters + 1, (unsigned long long)(s1 - s0) * nchunks);
     }
-    if (!valid) return;
-    const int idx = iv * sc.R + iu;
-    if (finalize) {
-        double p[3];
 #pragma unroll
-        for (int c = 0; c < 3; c++) p[c] = __dadd_rn(s_pa[c][lu], s_pb[c][lv]);
-        bool outside = true;
-        for (int s = 0; s < sc.ns && outside; s++) {
-            const Sphere& S = sph[s];
-            // clearly outside in single precision (0.1 % margin on d^2), else the exact test
-            const float dx = (float)(p[0] - S.p[0]), dy = (float)(p[1] - S.p[1]), dz = (float)(p[2] - S.p[2]);
-            const float af = (float)S.a;
-            if (dx * dx + dy * dy + dz * dz > 1.001f * af * af) continue;
-            double r[3];
-            if (dist_exact(p, S.p, r) < S.a) outside = false;
+    for (int j = 0; j < PPT; j++) {
+        if (!valid[j]) continue;
+        const int idx = iv[j] * sc.R + iu[j];
+        if (finalize) {
+            double p[3];
+#pragma unroll
+            for (int c = 0; c < 3; c++) p[c] = __dadd_rn(s_pa[c][lu[j]], s_pb[c][lv[j]]);
+            bool outside = true;
+            for (int s = 0; s < sc.ns && outside; s++) {
+                const Sphere& S = sph[s];
+                // clearly outside in single precision (0.1 % margin on d^2), else the exact test
+                const float dx = (float)(p[0] - S.p[0]), dy = (float)(p[1] - S.p[1]), dz = (float)(p[2] - S.p[2]);
+                const float af = (float)S.a;
+                if (dx * dx + dy * dy + dz * dz > 1.001f * af * af) continue;
+                double r[3];
+                if (dist_exact(p, S.p, r) < S.a) outside = false;
+            }
+            if (outside) {
+                tot_r[j] += Uf[idx].re - cmp_r[j];
+                tot_i[j] += Uf[idx].im - cmp_i[j];
+            }
         }
-        if (outside) {
-            tot_r += Uf[idx].re - cmp_r;
-            tot_i += Uf[idx].im - cmp_i;
-        }
+        U[idx] = mk(tot_r[j], tot_i[j]);
     }
-    U[idx] = mk(tot_r, tot_i);
 }
 
 // LUT build into the real and imaginary planes of a CUDA array pair (same
@@ -1102,15 +1169,16 @@ void launch_us_lut_tex(const Scene& sc, const Sphere* sph, int s0, int s1, int a
                        bool stage, int chunk, cudaStream_t st) {
     int tiles = (sc.R + 15) / 16;
     if (!stage) {
-        us_lut_tex_kernel<false><<<(unsigned)tiles * tiles, UST_BLOCK, 0, st>>>(sc, sph, s0, s1, accumulate, finalize,
+        us_lut_tex_kernel<false, 1><<<(unsigned)tiles * tiles, UST_TILE, 0, st>>>(sc, sph, s0, s1, accumulate, finalize,
                                                                                  kw4, cones, ph, tex, lin, Uf, U,
                                                                                  counters, chunk);
         return;
     }
     const int smem = UST_STAGE * (int)sizeof(float2);
     // per device and cheap; a failure shows up as the launch error
-    cudaFuncSetAttribute(us_lut_tex_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    us_lut_tex_kernel<true><<<(unsigned)tiles * tiles, UST_BLOCK, smem, st>>>(sc, sph, s0, s1, accumulate, finalize,
+    auto kernel = us_lut_tex_kernel<true, UST_STAGED_PPT>;
+    cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    kernel<<<(unsigned)tiles * tiles, UST_TILE / UST_STAGED_PPT, smem, st>>>(sc, sph, s0, s1, accumulate, finalize,
                                                                                kw4, cones, ph, tex, lin, Uf, U,
                                                                                counters, chunk);
 }
