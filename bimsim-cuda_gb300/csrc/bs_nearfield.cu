@@ -424,9 +424,12 @@ __global__ void __launch_bounds__(128) us_lut_f64_kernel(Scene sc, const Sphere*
 // formula, so they give the same bits; edge cells clamp like the reference's
 // texture fetch.
 constexpr int UST_TILE = 256;           // 16 x 16 pixel tile
-// pixels per thread of the staged kernel: 128 threads at 128 registers, 4 blocks per SM (one pixel
-// per thread: 2 % slower; four: 19 %; two at 96 registers and 5 blocks per SM: 11 %)
-constexpr int UST_STAGED_PPT = 2;
+// Pixels per thread of the staged kernel.  With 64-wave chunks two pixels per thread (128 threads
+// at 128 registers, 4 blocks per SM) are fastest: 730 ms on the 1024^2, 50-sphere slice against
+// 755 ms for one pixel (four: 19 % slower; two at 96 registers and 5 blocks per SM: 11 %).  With
+// 16-wave chunks the per-chunk barriers and window copies weigh more and one pixel per thread on
+// 8 warps is faster (512^2 slice at 3x the table rows per tile: 307 against 366 ms).
+constexpr int UST_TWO_PIXEL_MIN_CHUNK = 64;
 
 // Fractional LUT angle index t = acos(c) tsc for c in [-1, 1] (c is clamped),
 // tsc = (thetaR - 1) / PI_REF, tscpi = tsc * pi.  acos(x) = sqrt(1 - x) g(x)
@@ -1176,9 +1179,10 @@ void launch_us_lut_tex(const Scene& sc, const Sphere* sph, int s0, int s1, int a
     }
     const int smem = UST_STAGE * (int)sizeof(float2);
     // per device and cheap; a failure shows up as the launch error
-    auto kernel = us_lut_tex_kernel<true, UST_STAGED_PPT>;
+    const bool two = chunk >= UST_TWO_PIXEL_MIN_CHUNK;
+    auto kernel = two ? us_lut_tex_kernel<true, 2> : us_lut_tex_kernel<true, 1>;
     cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    kernel<<<(unsigned)tiles * tiles, UST_TILE / UST_STAGED_PPT, smem, st>>>(sc, sph, s0, s1, accumulate, finalize,
+    kernel<<<(unsigned)tiles * tiles, two ? UST_TILE / 2 : UST_TILE, smem, st>>>(sc, sph, s0, s1, accumulate, finalize,
                                                                                kw4, cones, ph, tex, lin, Uf, U,
                                                                                counters, chunk);
 }
