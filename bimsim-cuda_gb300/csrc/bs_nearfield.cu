@@ -406,7 +406,7 @@ __global__ void __launch_bounds__(128) us_lut_f64_kernel(Scene sc, const Sphere*
 // Mixed precision: per-(pixel, sphere) geometry in double, per-wave work in
 // float, per-chunk partial sums combined with Kahan compensation.
 //
-// A block owns a 16 x 16 pixel tile, one pixel per thread.  The waves arrive
+// A block owns a 16 x 16 pixel tile, one or two pixels per thread.  The waves arrive
 // grouped by direction into compact chunks of `chunk` waves (64, 32 or 16) and
 // are processed chunk by chunk; the host gives each chunk a bounding cone
 // (axis c_k, half-angle beta_k).  For a
