@@ -53,6 +53,30 @@ def test_oracle_transform_matches_numpy(pf):
     assert np.max(np.abs(a - b)) <= 1e-12 * np.max(np.abs(b - 1.45))
 
 
+def _sin_pi_ratio(a, M):
+    """sin(pi a / M) with a reduced in integers to a ratio in [0, 1/2], as kk_kernel_g does."""
+    r = a % (2 * M)
+    sign = np.where(r >= M, -1.0, 1.0)
+    r = np.where(r >= M, r - M, r)
+    r = np.where(2 * r > M, M - r, r)
+    return sign * np.sin(np.pi * (r / M))
+
+
+@pytest.mark.parametrize("M", [2, 7, 8, 300, 1001, 16384 * 16 - 1, 16384 * 16])
+def test_closed_form_convolution_kernel(M):
+    """The GPU routine convolves with g(m) = -(2/M) sin(K t) sin((K+1) t) / sin(t), t = pi m / M,
+    K = ceil(M/2) - 1: the real part of the inverse FFT of the reference's multiplier (i below M/2,
+    -i from M/2, 0 at DC), to an ulp of its largest value at every m."""
+    m = np.arange(1, M, dtype=np.int64)
+    K = (M + 1) // 2 - 1
+    g = np.zeros(M)
+    g[1:] = -2.0 * (_sin_pi_ratio(K * m, M) * _sin_pi_ratio((K + 1) * m, M) / _sin_pi_ratio(m, M)) / M
+    f = np.arange(M)
+    H = np.where(f == 0, 0, np.where(f < M / 2.0, 1j, -1j))
+    ref = np.fft.ifft(H).real
+    assert np.max(np.abs(g - ref)) <= 4e-16 * max(np.max(np.abs(ref)), 1e-300) + 1e-17
+
+
 def test_oracle_absorption_band_gives_dispersion():
     # a Lorentzian band in kappa gives the familiar dispersive wiggle in n: above n0 on the long-wavelength
     # side of the band and below it on the short side
