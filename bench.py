@@ -11,8 +11,10 @@ padding 1 (near field 3072^2), mixed precision.  Seeded synthetic scene
 N > 1 runs under torch.distributed.run as independent replicas (one slice per
 rank per step, no collective in the data path; weak scaling).  `--impl
 reference` times the CPU implementation of the path (the double-precision
-restatement in oracle/; the reference's own GPU code cannot be built, see
-the design doc) on a bounded band of near-field rows and extrapolates.
+restatement in oracle/; the reference's own GPU code cannot be built: it is a
+CMake project that needs the STIM library, OpenCV and FFTW, and four of its
+.cu files use texture references that CUDA 12 removed) on a bounded band of
+near-field rows and extrapolates.
 """
 import argparse
 import json
