@@ -45,6 +45,7 @@ def library():
         "bs_get_image_f64": ([vp, C.c_int, vp, sz], C.c_int),
         "bs_get_field": ([vp, C.c_int, vp, sz], C.c_int),
         "bs_write_envi": ([vp, C.c_int, C.c_char_p, i32, C.c_double], C.c_int),
+        "bs_envi_add_band": ([C.c_char_p, vp, i32, i32, C.c_double, i32], C.c_int),
         "bs_get_info": ([vp, vp], C.c_int),
         "bs_get_stats": ([vp, vp], C.c_int),
         "bs_get_mie": ([vp, i32, vp, vp, i32], C.c_int),
@@ -242,6 +243,16 @@ class Context:
 
     def release_buffers(self):
         self._check(self.lib.bs_release_buffers(self.h))
+
+
+def envi_add_band(path, band, band_value, append):
+    """Write (append=False) or append one float32 band of a host image to an ENVI file."""
+    lib = library()
+    b = np.ascontiguousarray(band, dtype=np.float32)
+    lines, samples = b.shape
+    st = lib.bs_envi_add_band(str(path).encode(), _p(b), samples, lines, float(band_value), 1 if append else 0)
+    if st != 0:
+        raise BimsimError(st, lib.bs_last_error().decode())
 
 
 def material_eval(path, lambdas):

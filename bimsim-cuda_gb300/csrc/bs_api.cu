@@ -1711,6 +1711,15 @@ bs_status bs_write_envi(bs_ctx* c, bs_image_kind kind, const char* path, int32_t
     return BS_OK;
 }
 
+bs_status bs_envi_add_band(const char* path, const float* band, int32_t samples, int32_t lines, double band_value,
+                           int32_t append) {
+    if (!path || !band || samples < 1 || lines < 1) return fail(BS_ERR_ARG, "bs_envi_add_band: bad argument");
+    char err[512] = {0};
+    if (envi_add_band(path, band, samples, lines, band_value, append, err, sizeof(err)) != 0)
+        return fail(BS_ERR_IO, "%s", err);
+    return BS_OK;
+}
+
 bs_status bs_sweep(bs_ctx* c, const double* lambdas, int32_t nl, const double* n_table, bs_precision prec,
                    bs_image_kind kind, float* images, const char* envi_path, int32_t band_as_nu) {
     if (!c || !lambdas || nl < 1) return fail(BS_ERR_ARG, "bs_sweep: need at least one wavelength");

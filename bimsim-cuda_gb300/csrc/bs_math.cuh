@@ -123,7 +123,9 @@ __device__ __forceinline__ double digits_at(int n, double x) {
     return 0.5 * log10(6.28 * n) - n * log10(1.36 * x / n);
 }
 
-// order where J_n(x) ~ 10^-mp, by secant iteration on digits_at (Zhang & Jin, MSTA1)
+// Order where J_n(x) ~ 10^-mp, by secant iteration on digits_at: routine MSTA1 of
+// S. Zhang and J. Jin, Computation of Special Functions (Wiley, 1996), which the
+// reference's bessjy.cpp:268-290 also follows (its constants 6.28, 1.36, 1.1).
 __device__ inline int order_cutoff(double x, int mp) {
     double a = fabs(x);
     int lo = (int)(1.1 * a) + 1, hi = lo + 5;

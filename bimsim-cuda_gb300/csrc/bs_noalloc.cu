@@ -32,11 +32,33 @@ constexpr int NOALLOC_MAX_DEVICES = 64;
 // j, y, j', y' at k a and j, j' at k n a.  256 * 6 * 128 * 16 B = 3 MiB.
 static __device__ __align__(256) zd g_noalloc_bessel[NOALLOC_MAX_SPHERES * 6 * NOALLOC_L];
 
-__global__ void mie_noalloc_kernel(const double* __restrict__ sph, int ns, int nl, double k, zd* __restrict__ work,
-                                   zd* __restrict__ A, zd* __restrict__ B) {
+// The sphere's own order count Nl = ceil(ka + 4 (ka)^(1/3) + 2) in single
+// precision, in the order of sphere::calcNl (sphere.h:71-74) and of the host's
+// calc_nl, with lambda = 2 PI / k rounded to float.  powf on the GPU may differ
+// from the host's by an ulp, which changes Nl only when the sum lies within a
+// few ulps of an integer.
+__device__ int noalloc_calc_nl(double a_in, double k) {
+    const float lam = (float)(2.0 * (double)3.14159f / k);
+    const float pif = 3.14159f;
+    float ka = __fmul_rn(2.0f, pif);
+    ka = __fmul_rn(ka, (float)a_in);
+    ka = __fdiv_rn(ka, lam);
+    const float third = (float)(1.0 / 3.0);
+    float v = __fmul_rn(4.0f, powf(ka, third));
+    v = __fadd_rn(ka, v);
+    v = __fadd_rn(v, 2.0f);
+    return (int)ceilf(v);
+}
+
+__global__ void mie_noalloc_kernel(const double* __restrict__ sph, int ns, int nl_cap, double k,
+                                   zd* __restrict__ work, zd* __restrict__ A, zd* __restrict__ B) {
     int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= ns) return;
     const double a = sph[3 * s], n_re = sph[3 * s + 1], n_im = sph[3 * s + 2];
+    // Orders above the sphere's own Nl are not part of its series (the context
+    // path never computes them); they are returned as zeros.  Evaluating them
+    // would divide underflowed Bessel values (0/0, 0 * inf) for small spheres.
+    const int nl = min(nl_cap, noalloc_calc_nl(a, k));
     zd* ja = work + (size_t)s * 6 * NOALLOC_L;
     zd* ya = ja + NOALLOC_L;
     zd* jpa = ya + NOALLOC_L;
@@ -48,8 +70,9 @@ __global__ void mie_noalloc_kernel(const double* __restrict__ sph, int ns, int n
     const zd kna = (n * k) * a;
     sph_complex(nl, ka, true, ja, ya, jpa, ypa);
     sph_complex(nl, kna, true, jn, nullptr, jpn, nullptr);
-    zd* As = A + (size_t)s * (nl + 1);
-    zd* Bs = B + (size_t)s * (nl + 1);
+    zd* As = A + (size_t)s * (nl_cap + 1);
+    zd* Bs = B + (size_t)s * (nl_cap + 1);
+    for (int l = nl + 1; l <= nl_cap; l++) As[l] = Bs[l] = mk(0.0, 0.0);
     for (int l = 0; l <= nl; l++) {
         const zd h = mk(ja[l].re - ya[l].im, ja[l].im + ya[l].re);
         const zd hp = mk(jpa[l].re - ypa[l].im, jpa[l].im + ypa[l].re);

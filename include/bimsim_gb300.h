@@ -183,6 +183,14 @@ bs_status bs_get_far_field(bs_ctx* ctx, bs_field_kind kind, double* host, size_t
 bs_status bs_write_envi(bs_ctx* ctx, bs_image_kind kind, const char* path,
                         int32_t append, double band_value);
 
+/* The same ENVI writer for a caller's host image (samples x lines float32,
+ * row-major): EnviFile(path, append ? "a" : "w").addBand(...) then close()
+ * (rts/envi/envi.h:196-233, 325-343, 423-433; header envi_header.h:318-375).
+ * A band of another size than the file's bands is refused, as the reference's
+ * EnviFile refuses it. */
+bs_status bs_envi_add_band(const char* path, const float* band, int32_t samples, int32_t lines,
+                           double band_value, int32_t append);
+
 /* Upper bound on the bytes of per-sphere lookup tables held at once; spheres
  * beyond it are processed in successive chunks.  0 (default) = 80% of free HBM.
  * No reference counterpart: the reference allocated one cudaArray per sphere
@@ -404,7 +412,10 @@ bs_status bs_server_get_stats(bs_server* srv, bs_server_stats* out);
  * bs_simulate/bs_get_mie compute per sphere.
  *   spheres  device array, ns x {a, n_re, n_im} (radius um, complex index)
  *   ns       0..256;  nl: highest order, 0..127;  k: wavenumber 2*PI/lambda
- *   A, B     device arrays, ns x (nl + 1) interleaved complex doubles
+ *   A, B     device arrays, ns x (nl + 1) interleaved complex doubles; sphere
+ *            s fills orders 0..min(nl, Nl_s), Nl_s its own order count
+ *            (sphere::calcNl, sphere.h:71-74, with lambda = 2*PI/k), and
+ *            zeros above, as the context path computes no order beyond Nl_s
  *   stream   cudaStream_t to run on (NULL = legacy default stream); the call is
  *            asynchronous on it.
  * The Bessel work space is a fixed 3 MiB device array inside this library,
@@ -412,7 +423,9 @@ bs_status bs_server_get_stats(bs_server* srv, bs_server_stats* out);
  * so nothing needs clearing, but every call shares it: calls whose kernels
  * overlap on the GPU (different streams, or threads sharing a device) race.
  * The first call on a device resolves the array's device address, so make it
- * before any stream capture.  Sizes beyond the limits return BS_ERR_ARG. */
+ * before any stream capture.  That address is kept for the process: do not
+ * call cudaDeviceReset on the device after the first call.  Sizes beyond the
+ * limits return BS_ERR_ARG. */
 bs_status bs_mie_noalloc(const double* spheres, int32_t ns, int32_t nl, double k, double* A, double* B,
                          void* stream);
 

@@ -94,6 +94,19 @@ def simulate_rings(params, spheres, ns, waves, mode, points, rings, nthreads=0):
     return D.reshape(res, res), Di.reshape(res, res)
 
 
+def nearfield_rows(params, spheres, ns, waves, row0, row1, nthreads=0):
+    """Oracle near field U (after sumUf) of pixel rows [row0, row1): complex128 (row1 - row0, R)."""
+    lib = load()
+    R = geom(params).R
+    U = np.zeros(2 * (row1 - row0) * R)
+    w = np.ascontiguousarray(waves, dtype=np.float64).reshape(-1)
+    nk = len(w) // 3
+    rc = lib.bso_nearfield_rows(C.byref(params), C.byref(spheres), ns, P(w) if nk else None, nk, nthreads, row0,
+                                row1, P(U))
+    assert rc == 0, rc
+    return U.view(np.complex128).reshape(row1 - row0, R)
+
+
 def simulate(params, spheres, ns, waves, nthreads=0):
     """Full oracle path -> (U, Uf, D, Di) as numpy arrays (complex128 / float64)."""
     lib = load()

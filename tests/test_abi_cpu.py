@@ -97,3 +97,22 @@ def test_make_params_supersample_rule():
     # arguments.h:411-418: ss = ceil(2 s / (res lambda)) when s/res > lambda/2
     assert abi.make_params(lam=1.0, xy=(40, 0), resolution=256).supersample == 1
     assert abi.make_params(lam=0.1, xy=(40, 0), resolution=256).supersample == 4
+
+
+def test_envi_writer_bytes_match_the_references_envifile(so, golden):
+    """bs_envi_add_band (the writer behind bs_write_envi) against the bytes the reference's own
+    EnviFile::addBand + close wrote (golden envi.json): header text and data, write then append."""
+    import numpy as np
+    e = golden("envi")
+    with tempfile.TemporaryDirectory() as td:
+        path = os.path.join(td, "band")
+        b1 = np.array(e["b1"], dtype=np.float32).reshape(e["lines"], e["samples"])
+        b2 = np.array(e["b2"], dtype=np.float32).reshape(e["lines"], e["samples"])
+        lib.envi_add_band(path, b1, e["wl"][0], append=False)
+        assert open(path + ".hdr").read() == e["hdr_1"]
+        assert open(path, "rb").read().hex() == e["dat_1"]
+        lib.envi_add_band(path, b2, e["wl"][1], append=True)
+        assert open(path + ".hdr").read() == e["hdr_2"]
+        assert open(path, "rb").read().hex() == e["dat_2"]
+        with pytest.raises(lib.BimsimError):  # a band of another size is refused (envi.h:66-89)
+            lib.envi_add_band(path, np.zeros((2, 2), np.float32), 1.0, append=True)

@@ -1,0 +1,94 @@
+"""Benchmark scenes at their full shapes, GPU path vs the oracle on bands of near-field rows.
+
+The oracle needs minutes of host time per whole slice at these sizes, so it computes only a
+band of rows through every sphere and wave (`bso_nearfield_rows`); the GPU computes the whole
+slice exactly as the benchmark runs it (table sizes, staged windows, wave chunks, two pixels per
+thread, table budget), and the band of its near field U is compared.
+
+  * config 2 (the headline: 1024^2 detector over 100 um, near field 3072^2, 50 spheres,
+    1000 waves, tables of 4096 x 1024): rows [R/2 - 6, R/2 + 6), FP64 and mixed
+  * config 3 (512^2 over 100 um, near field 1536^2, 50 spheres with Lorentzian materials):
+    the first (2.5 um) and last (12.5 um) of the 512 bands, 8 rows each, FP64 and mixed
+  * config 5 at reduced resolution (512^2 over 400 um, near field 1536^2, 1000 spheres with
+    a up to 20 um: 81 orders): 4 rows, mixed with all 2000 waves, FP64 with the first 250
+
+Tolerances (relative L2 over the band): FP64 1e-10, mixed 1e-4 (near field).
+"""
+import numpy as np
+import pytest
+
+import oracle_lib
+from bimsim_gb300 import BS_FIELD_TOTAL, BS_PREC_FP64, BS_PREC_MIXED, Context, abi, scenes
+
+pytestmark = pytest.mark.gpu
+
+TOL64 = 1e-10
+TOL_MIXED_FIELD = 1e-4
+
+
+def rel(a, b):
+    return float(np.linalg.norm((a - b).ravel()) / np.linalg.norm(b.ravel()))
+
+
+def gpu_band(p, spheres, waves, prec, row0, row1):
+    with Context(p) as ctx:
+        ctx.set_spheres(spheres)
+        ctx.set_waves(waves)
+        ctx.simulate(prec)
+        st = ctx.stats()
+        U = ctx.field(BS_FIELD_TOTAL)
+    return U[row0:row1], st
+
+
+def oracle_band(p, spheres, waves, row0, row1):
+    arr, ns = abi.sphere_array(spheres)
+    return oracle_lib.nearfield_rows(p, arr, ns, waves, row0, row1)
+
+
+def test_config2_full_slice_band_matches_oracle():
+    p, s, w = scenes.config2()
+    R = oracle_lib.geom(p).R
+    assert R == 3072
+    r0, r1 = R // 2 - 6, R // 2 + 6
+    ref = oracle_band(p, s, w, r0, r1)
+    mixed, st = gpu_band(p, s, w, BS_PREC_MIXED, r0, r1)
+    assert st.lut_wave_chunk == 64 and st.lut_chunks_staged > 0.9 * st.lut_chunks_total  # the benchmark's kernel
+    f64, _ = gpu_band(p, s, w, BS_PREC_FP64, r0, r1)
+    errs = {"fp64": rel(f64, ref), "mixed": rel(mixed, ref)}
+    print("config 2 band errors", errs)
+    assert errs["fp64"] <= TOL64, errs
+    assert errs["mixed"] <= TOL_MIXED_FIELD, errs
+
+
+@pytest.mark.parametrize("band", [0, 511])
+def test_config3_band_matches_oracle(band):
+    p, s, w, lambdas, table = scenes.config3(n_lambda=512)
+    p.lambda_ = float(lambdas[band])
+    sb = [(x, y, z, a, float(n.real), float(n.imag)) for (x, y, z, a, _, _), n in zip(s, table[band])]
+    R = oracle_lib.geom(p).R
+    assert R == 1536
+    r0, r1 = R // 2 - 4, R // 2 + 4
+    ref = oracle_band(p, sb, w, r0, r1)
+    mixed, st = gpu_band(p, sb, w, BS_PREC_MIXED, r0, r1)
+    f64, _ = gpu_band(p, sb, w, BS_PREC_FP64, r0, r1)
+    errs = {"fp64": rel(f64, ref), "mixed": rel(mixed, ref), "chunk": st.lut_wave_chunk}
+    print(f"config 3 band {band} (lambda {lambdas[band]:.3f} um) errors", errs)
+    assert errs["fp64"] <= TOL64, errs
+    assert errs["mixed"] <= TOL_MIXED_FIELD, errs
+
+
+def test_config5_reduced_band_matches_oracle():
+    p, s, w = scenes.config5(resolution=512)
+    R = oracle_lib.geom(p).R
+    assert R == 1536 and len(s) == 1000 and len(w) == 2000
+    nl = max(oracle_lib.load().bso_calc_nl(sp[3], p.lambda_) for sp in s)
+    assert nl >= 80
+    r0, r1 = R // 2 - 2, R // 2 + 2
+    mixed, _ = gpu_band(p, s, w, BS_PREC_MIXED, r0, r1)
+    e_mixed = rel(mixed, oracle_band(p, s, w, r0, r1))
+    w64 = w[:250]
+    f64, _ = gpu_band(p, s, w64, BS_PREC_FP64, r0, r1)
+    e64 = rel(f64, oracle_band(p, s, w64, r0, r1))
+    print("config 5 (512^2) band errors", {"fp64_250_waves": e64, "mixed": e_mixed, "max_order": nl})
+    assert e64 <= TOL64
+    assert e_mixed <= TOL_MIXED_FIELD

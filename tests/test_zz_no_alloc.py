@@ -1,8 +1,8 @@
 """bs_mie_noalloc: Mie coefficients for callers that cannot allocate device
 memory (inside CUDA stream capture, allocation-free serving loops, frameworks
 owning device memory through their own pool).  Checked through the C ABI
-against the context path (bs_simulate + bs_get_mie) at the double-precision
-tolerance of the other parity tests, on two calls in a row."""
+against the context path (bs_simulate + bs_get_mie) and the oracle at the
+double-precision tolerance of the other parity tests, on two calls in a row."""
 import ctypes as C
 
 import numpy as np
@@ -59,6 +59,36 @@ def test_mie_noalloc_matches_context_path_twice():
             gb = b[i, :n, 0] + 1j * b[i, :n, 1]
             assert rel(ga, ra) <= TOL, (call, i, rel(ga, ra))
             assert rel(gb, rb) <= TOL, (call, i, rel(gb, rb))
+            oa, ob = oracle_mie(k, spheres[i], n - 1)
+            assert rel(ga, oa) <= TOL and rel(gb, ob) <= TOL, (call, i, rel(ga, oa), rel(gb, ob))
+            assert not np.any(a[i, n:]) and not np.any(b[i, n:])  # orders above the sphere's own Nl
+
+
+def test_mie_noalloc_small_sphere_beside_a_large_one_at_the_order_limit():
+    """k a from 0.25 to 63 in one call with nl = 127: every entry finite, each sphere's orders up to its
+    own Nl equal to the oracle's, zeros above."""
+    import torch
+
+    so = lib.library()
+    lam = 2.0
+    k = 2 * float(np.float32(3.14159)) / lam
+    spheres = [(0.08, 1.4, 0.05), (20.0, 1.4, 0.02), (0.5, 1.6, 0.0), (7.3, 1.2, 0.04)]
+    dev = torch.device("cuda")
+    sph = torch.tensor(spheres, dtype=torch.float64, device=dev)
+    A = torch.full((len(spheres), 128, 2), np.nan, dtype=torch.float64, device=dev)
+    B = torch.full_like(A, np.nan)
+    st = so.bs_mie_noalloc(C.c_void_p(sph.data_ptr()), len(spheres), 127, k, C.c_void_p(A.data_ptr()),
+                           C.c_void_p(B.data_ptr()), None)
+    assert st == 0, so.bs_last_error()
+    torch.cuda.synchronize()
+    a, b = A.cpu().numpy(), B.cpu().numpy()
+    assert np.all(np.isfinite(a)) and np.all(np.isfinite(b))
+    for i, (rad, nre, nim) in enumerate(spheres):
+        nl = abi_nl(rad, lam)
+        oa, ob = oracle_mie(k, (0, 0, 0, rad, nre, nim), nl)
+        assert rel(a[i, :nl + 1, 0] + 1j * a[i, :nl + 1, 1], oa) <= TOL
+        assert rel(b[i, :nl + 1, 0] + 1j * b[i, :nl + 1, 1], ob) <= TOL
+        assert not np.any(a[i, nl + 1:]) and not np.any(b[i, nl + 1:])
 
 
 def test_mie_noalloc_rejects_sizes_beyond_the_work_space():
@@ -73,3 +103,11 @@ def test_mie_noalloc_rejects_sizes_beyond_the_work_space():
 def abi_nl(a, lam):
     import oracle_lib
     return oracle_lib.load().bso_calc_nl(a, lam)
+
+
+def oracle_mie(k, sphere, nl):
+    import oracle_lib
+    A = np.zeros(2 * nl + 2)
+    B = np.zeros(2 * nl + 2)
+    oracle_lib.load().bso_mie(k, sphere[3], sphere[4], sphere[5], nl, oracle_lib.P(A), oracle_lib.P(B))
+    return A.view(np.complex128), B.view(np.complex128)
