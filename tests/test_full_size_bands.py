@@ -77,7 +77,20 @@ def test_config3_band_matches_oracle(band):
     assert errs["mixed"] <= TOL_MIXED_FIELD, errs
 
 
+def host_memory_available_gb():
+    try:
+        for line in open("/proc/meminfo"):
+            if line.startswith("MemAvailable:"):
+                return int(line.split()[1]) / 2**20
+    except OSError:
+        pass
+    return 0.0
+
+
 def test_config5_reduced_band_matches_oracle():
+    # the oracle fills the table entries the band touches: about 20 GB of host memory for 1000 spheres
+    if host_memory_available_gb() < 64:
+        pytest.skip("needs 64 GB of free host memory for the oracle's tables of 1000 spheres")
     p, s, w = scenes.config5(resolution=512)
     R = oracle_lib.geom(p).R
     assert R == 1536 and len(s) == 1000 and len(w) == 2000
