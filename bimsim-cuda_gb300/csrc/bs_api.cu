@@ -345,7 +345,9 @@ static bs_status derive(bs_ctx* c) {
             return fail(BS_ERR_STATE, "bs_simulate: no plane-wave directions (call bs_set_waves or bs_sample_waves_compat)");
         sc.nk = (int)(c->waves.size() / 3);
         double sub = 2 * PI_REF * p.amplitude * ((1 - sc.cos_b) - (1 - sc.cos_a));
-        sc.wave_amp = (1.0 / sc.nk) * sub;
+        // the Monte Carlo weight is the reference's single-precision quotient 1.0f/nk
+        // (nfScalarUs.cu:457, nfScalarUpLut.cu:83,89), kept in every precision
+        sc.wave_amp = (double)(1.0f / (float)sc.nk) * sub;
     }
     V3 f{p.focus[0], p.focus[1], p.focus[2]};
     sc.uf_dmin = quad_dist(nf, f);

@@ -223,11 +223,13 @@ __global__ void coef_rows_batch_kernel(const Sphere* __restrict__ sph, int s0, i
     }
 }
 
-// P_l(cos theta_t), theta_t = t * PI_REF / (thetaR - 1) (sphere.cu:16-21)
+// P_l(cos theta_t), theta_t = t * dtheta (sphere.cu:16-21).  The reference's step
+// (PI) / (thetaR - 1) divides the float literal PI by an int: a single-precision
+// quotient in every build, kept here.
 __global__ void legendre_table_kernel(int thetaR, int Lmax, double* __restrict__ P) {
     int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= thetaR) return;
-    double dtheta = PI_REF / (thetaR - 1);
+    double dtheta = (double)__fdiv_rn(3.14159f, (float)(thetaR - 1));
     double x = cos(dtheta * t);
     double* row = P + (size_t)t * Lmax;
     double P0 = 1, P1 = x;

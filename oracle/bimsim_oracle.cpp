@@ -525,9 +525,10 @@ struct SphereLut {
             sph_complex(sg.Nl, knr, true, cj.data(), cy.data(), cjp.data(), cyp.data());
             for (int l = 0; l < L; l++) jt[(size_t)ia * L + l] = cj[l];
         }
-        // theta samples, sphere.cu:16-21
+        // theta samples, sphere.cu:16-21: the step (PI) / (thetaR - 1) is the float literal PI
+        // over an int, a single-precision quotient even in the reference's double build
         ctheta.resize(sg.thetaR);
-        double dtheta = PI_REF / (sg.thetaR - 1);
+        double dtheta = (double)(3.14159f / (float)(sg.thetaR - 1));
         for (int it = 0; it < sg.thetaR; it++) ctheta[it] = std::cos(dtheta * it);
         size_t nu = (size_t)sg.dR * sg.thetaR, ni = (size_t)sg.aR * sg.thetaR;
         usp = (cd*)std::calloc(nu, sizeof(cd));
@@ -820,7 +821,9 @@ cd scattered(Scene& sc, V3 pt) {
     int ns = (int)sc.s.size();
     if (!p.scalar || ns == 0) return U;  // nearfield.cpp:160-165 (vector: nothing)
     V3 f = v3(p.focus);
-    double scale_amp = (1.0 / sc.nk) * g.sub_amp;
+    // the reference's weight 1.0f/nk is a single-precision quotient (nfScalarUs.cu:457,
+    // nfScalarUpLut.cu:83,89): in its own double-precision build it stays float-rounded
+    double scale_amp = (double)(1.0f / (float)sc.nk) * g.sub_amp;
     for (int is = 0; is < ns; is++) {
         const bs_sphere& s = sc.s[is];
         V3 ps{s.x, s.y, s.z};

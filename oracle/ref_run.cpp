@@ -1,0 +1,151 @@
+// ref_run.cpp -- TEST INFRASTRUCTURE.  Entry points of the host-run build of
+// the reference (oracle/_ref/libref_sim_f32.so and libref_sim_f64.so, made by
+// `make -C oracle ref-sim` from the reference's own sources, compiled in place
+// with the CUDA stand-ins of oracle/ref_cuda).  One call runs the reference's
+// CLI path for a list of its own flags:
+//     SetArguments, arglist::parse, LoadParameters   (arguments.h:27-90,564-593)
+//     microscopeStruct::init                         (microscope.cu:537)
+//     nearfieldStruct::Simulate, step by step         (nearfield.cpp:194-218)
+//     microscopeStruct::SimulateImaging              (microscope.cu:840)
+//     getIntensity / getIncidentFieldImage / getAbsorbance (microscope.cu:722-814)
+// and keeps its Monte Carlo directions, Mie coefficients, per-sphere tables,
+// near fields and detector images for the accessors below.  Simulate is taken
+// step by step only so that the tables can be read after calcSpheres; the
+// steps and their order are the reference's.  Only tests/golden/make_golden.py
+// loads this library, to record golden vectors.
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+// the reference's main.cpp includes these before arguments.h, which relies on
+// the `using namespace std` that rts/cuda/error.h (via fileout.h) brings in
+#include "sphere.h"
+#include "rts/optics/material.h"
+#include "nearfield.h"
+#include "microscope.h"
+#include "fieldslice.h"
+#include "fileout.h"
+#include "arguments.h"
+
+microscopeStruct* SCOPE = nullptr;
+// `extern __shared__ bsComplex sh_scaledPhase[]` of the reference's unused
+// optPc_gpuScalarUpLut (nfScalarUpLut.cu:220) resolves here; it never runs.
+bsComplex sh_scaledPhase[1 << 12];
+fileoutStruct gFileOut;
+bool verbose = false;
+bool gui = false;
+
+namespace {
+std::map<std::string, std::vector<double>> g_out;
+
+template <class T>
+void put_complex(const std::string& key, const rts::complex<T>* p, size_t n) {
+    std::vector<double>& v = g_out[key];
+    v.resize(2 * n);
+    for (size_t i = 0; i < n; i++) {
+        v[2 * i] = (double)p[i].r;
+        v[2 * i + 1] = (double)p[i].i;
+    }
+}
+
+template <class T>
+void put_real(const std::string& key, const T* p, size_t n) {
+    std::vector<double>& v = g_out[key];
+    v.assign(p, p + n);
+}
+}  // namespace
+
+extern "C" {
+
+// Run the reference on `argv` (argv[0] is the program name).  stop = 1 ends
+// after calcSpheres (tables only); 0 runs the whole single-source path.
+int ref_sim_run(int argc, const char** argv, int stop) {
+    g_out.clear();
+    std::vector<std::string> keep(argv, argv + argc);
+    std::vector<char*> av;
+    for (std::string& s : keep) av.push_back(&s[0]);
+    rts::arglist args;
+    SetArguments(args);
+    args.parse(argc, av.data());
+    SCOPE = new microscopeStruct();
+    LoadParameters(args);
+    SCOPE->init();
+    nearfieldStruct& nf = SCOPE->nf;
+
+    nf.t_Uf = 0;
+    nf.t_Us = 0;
+    nf.calcWaves();
+    nf.calcUf();
+    nf.calcSpheres();
+
+    std::vector<double> w;
+    for (const bsVector& k : nf.inWaves)
+        for (int c = 0; c < 3; c++) w.push_back((double)k[c]);
+    g_out["waves"] = w;
+    g_out["dims"] = {(double)nf.U.R[0], (double)nf.U.R[1], (double)SCOPE->Ud.R[0] / SCOPE->ss,
+                     (double)SCOPE->ss, (double)nf.sVector.size(), (double)nf.inWaves.size()};
+    // the inputs as the reference holds them after parsing (single-precision flag values)
+    g_out["scene"] = {(double)nf.lambda, (double)nf.A, (double)nf.k[0], (double)nf.k[1], (double)nf.k[2],
+                      (double)nf.focus[0], (double)nf.focus[1], (double)nf.focus[2], (double)nf.condenser[0],
+                      (double)nf.condenser[1], (double)SCOPE->objective[0], (double)SCOPE->objective[1],
+                      (double)SCOPE->padding, (double)SCOPE->ss, (double)nf.m, (double)nf.lut_us,
+                      (double)nf.lut_uf, (double)nf.planeWave, (double)nf.nWaves};
+    g_out["nf_quad"] = {(double)nf.pos.A[0], (double)nf.pos.A[1], (double)nf.pos.A[2], (double)nf.pos.X[0],
+                        (double)nf.pos.X[1], (double)nf.pos.X[2], (double)nf.pos.Y[0], (double)nf.pos.Y[1],
+                        (double)nf.pos.Y[2]};
+    for (size_t s = 0; s < nf.sVector.size(); s++) {
+        const sphere& S = nf.sVector[s];
+        const std::string p = "sphere" + std::to_string(s) + ".";
+        g_out[p + "geom"] = {(double)S.Nl, (double)S.d_min, (double)S.d_max, (double)S.Usp.R[0],
+                             (double)S.Usp.R[1], (double)S.Uip.R[0], (double)S.Uip.R[1]};
+        g_out[p + "in"] = {(double)S.p[0], (double)S.p[1], (double)S.p[2], (double)S.a, (double)S.n.real(),
+                           (double)S.n.imag()};
+        put_complex(p + "A", S.A.data(), S.A.size());
+        put_complex(p + "B", S.B.data(), S.B.size());
+        if (nf.lut_us) {
+            put_complex(p + "Usp", S.Usp.x_hat, (size_t)S.Usp.R[0] * S.Usp.R[1]);
+            put_complex(p + "Uip", S.Uip.x_hat, (size_t)S.Uip.R[0] * S.Uip.R[1]);
+        }
+    }
+    if (stop == 1) return 0;
+
+    nf.calcUs();
+    nf.sumUf();
+    const size_t nnf = (size_t)nf.U.R[0] * nf.U.R[1];
+    put_complex("U", nf.U.x_hat, nnf);
+    put_complex("Uf", nf.Uf.x_hat, nnf);
+
+    SCOPE->SimulateImaging();
+    scalarslice I = SCOPE->getIntensity();
+    scalarslice Ii = SCOPE->getIncidentFieldImage();
+    scalarslice Ab = SCOPE->getAbsorbance();
+    const size_t nd = (size_t)I.R[0] * I.R[1];
+    put_real("D", I.S, nd);
+    put_real("Di", Ii.S, nd);
+    put_real("Absorbance", Ab.S, nd);
+    put_complex("Ud", SCOPE->Ud.x_hat, (size_t)SCOPE->Ud.R[0] * SCOPE->Ud.R[1]);
+    return 0;
+}
+
+// Number of values stored under `key` (-1 if none).
+long ref_sim_size(const char* key) {
+    auto it = g_out.find(key);
+    return it == g_out.end() ? -1 : (long)it->second.size();
+}
+
+// Copy the values stored under `key` into out (ref_sim_size(key) doubles).
+int ref_sim_get(const char* key, double* out) {
+    auto it = g_out.find(key);
+    if (it == g_out.end()) return 1;
+    std::memcpy(out, it->second.data(), it->second.size() * sizeof(double));
+    return 0;
+}
+
+void bs_ref_set_tex_weight_bits(int bits);
+int ref_sim_set_tex_weight_bits(int bits) {
+    bs_ref_set_tex_weight_bits(bits);
+    return 0;
+}
+
+}  // extern "C"

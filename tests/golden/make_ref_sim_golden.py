@@ -1,0 +1,153 @@
+"""Record golden near fields and detector images from the reference's own path run on the CPU.
+
+    make -C oracle ref-sim REF_DIR=<reference checkout>
+    python tests/golden/make_ref_sim_golden.py
+
+oracle/_ref/libref_sim_f32.so and libref_sim_f64.so are the reference's sources (host .cpp and
+device .cu alike) compiled in place for the host with the CUDA stand-ins of oracle/ref_cuda
+(oracle/Makefile, target ref-sim; entry points in oracle/ref_run.cpp).  f32 is the reference as it
+ships (ptype float); f64 is the same sources with ptype double, which runs every path except the
+LUT apply and the incident-field LUT, whose texture copies are hard-coded for float
+(nfScalarUpLut.cu:414-415, nfScalarUfLut.cu:159).  For each scene below, a list of the reference's
+own flags, this writes into tests/golden/ref_sim.json the inputs as the reference holds them after
+parsing (wavelength, apertures, spheres, the near-field plane), its Monte Carlo directions, Mie
+coefficients, per-sphere tables (sampled rows), near fields U and Uf after sumUf, and the detector
+images D, Di and absorbance.  Arrays are little-endian float64, base64-encoded.
+"""
+import base64
+import contextlib
+import ctypes as C
+import json
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+
+TWO = ["--spheres", "0.3", "-0.2", "0", "2.2", "0", "5", "4", "1", "1", "1", "--materials", "1.5", "0.04", "1.3", "0"]
+
+# name: (build, stop after the tables?, flags)
+SCENES = {
+    # ptype double: direct (recursive) order sums, the whole path
+    "rec_two_spheres": ("f64", 0, TWO + ["--lambda", "3", "--condenser", "0", "0.6", "--objective", "0", "0.6",
+                                        "--resolution", "12", "--xy", "16", "0", "--samples", "20", "--recursive"]),
+    "rec_large_ka": ("f64", 0, ["--spheres", "0.1", "-0.05", "0", "5", "0", "--materials", "1.4", "0.05",
+                                "--lambda", "2.5", "--condenser", "0", "0.5", "--objective", "0", "0.5",
+                                "--resolution", "8", "--xy", "10", "0", "--padding", "2", "--samples", "16",
+                                "--recursive"]),
+    "rec_xz_focus": ("f64", 0, ["--spheres", "0.5", "1", "-0.5", "1.6", "0", "-2", "-1.5", "2", "1.1", "1",
+                                "--materials", "1.35", "0.02", "1.5", "0", "--lambda", "7", "--condenser", "0.1",
+                                "0.45", "--objective", "0", "0.5", "--xz", "12", "0.4", "--resolution", "12",
+                                "--focus", "0.5", "0", "0.3", "--amplitude", "2", "--samples", "16",
+                                "--field-order", "14", "--recursive"]),
+    "rec_supersample": ("f64", 0, ["--spheres", "0.23", "0.11", "0", "1.03", "0", "--materials", "1.4", "0.05",
+                                   "--lambda", "1.5", "--condenser", "0", "0.5", "--objective", "0", "0.5",
+                                   "--resolution", "6", "--xy", "6", "0", "--samples", "16", "--recursive"]),
+    # ptype double: the per-sphere tables of the LUT mode (sphere::calcUp and sphere.cu's sums)
+    "tables_two_spheres": ("f64", 1, TWO + ["--lambda", "3", "--resolution", "12", "--xy", "16", "0",
+                                           "--samples", "8"]),
+    # ptype float, as the reference ships: the default LUT path with its texture fetches
+    "lut_two_spheres": ("f32", 0, TWO + ["--lambda", "3", "--condenser", "0", "0.6", "--objective", "0", "0.6",
+                                        "--resolution", "12", "--xy", "16", "0", "--samples", "20"]),
+    "lut_uf_lut": ("f32", 0, ["--spheres", "1", "0.5", "0", "2", "0", "-4", "-3.5", "0.2", "1.3", "1",
+                              "--materials", "1.45", "0.03", "1.3", "0.02", "--lambda", "3", "--condenser", "0.1",
+                              "0.5", "--objective", "0.05", "0.45", "--resolution", "12", "--xy", "14", "0.5",
+                              "--samples", "24", "--lut-uf"]),
+    "lut_supersample_nu": ("f32", 0, ["--spheres", "0.23", "0.11", "0", "1.03", "0", "--materials", "1.4", "0.05",
+                                      "--nu", "6666.667", "--condenser", "0", "0.5", "--objective", "0", "0.5",
+                                      "--resolution", "6", "--xy", "6", "0", "--samples", "16"]),
+    "rec_two_spheres_f32": ("f32", 0, TWO + ["--lambda", "3", "--condenser", "0", "0.6", "--objective", "0", "0.6",
+                                            "--resolution", "12", "--xy", "16", "0", "--samples", "20",
+                                            "--recursive"]),
+}
+TABLE_THETA_ROWS = list(range(0, 1000, 37)) + [999]
+
+
+def enc(a):
+    return base64.b64encode(np.ascontiguousarray(a, dtype="<f8").tobytes()).decode()
+
+
+@contextlib.contextmanager
+def quiet():
+    """The reference prints progress to stdout; keep it out of this script's output."""
+    sys.stdout.flush()
+    fd = os.dup(1)
+    null = os.open(os.devnull, os.O_WRONLY)
+    os.dup2(null, 1)
+    try:
+        yield
+    finally:
+        sys.stdout.flush()
+        os.dup2(fd, 1)
+        os.close(fd)
+        os.close(null)
+
+
+def main():
+    libs = {}
+    for b in ("f32", "f64"):
+        path = os.path.join(REPO, "oracle", "_ref", f"libref_sim_{b}.so")
+        if not os.path.exists(path):
+            sys.exit("build the host-run reference first: make -C oracle ref-sim REF_DIR=<checkout>")
+        lib = C.CDLL(path)
+        lib.ref_sim_run.argtypes = [C.c_int, C.c_void_p, C.c_int]
+        lib.ref_sim_size.restype = C.c_long
+        lib.ref_sim_size.argtypes = [C.c_char_p]
+        lib.ref_sim_get.argtypes = [C.c_char_p, C.c_void_p]
+        libs[b] = lib
+    out = {}
+    for name, (b, stop, flags) in SCENES.items():
+        lib = libs[b]
+        argv = ["bimsim"] + flags
+        arr = (C.c_char_p * len(argv))(*[a.encode() for a in argv])
+        with quiet():
+            rc = lib.ref_sim_run(len(argv), arr, stop)
+        assert rc == 0, name
+
+        def get(key):
+            n = lib.ref_sim_size(key.encode())
+            if n < 0:
+                return None
+            v = np.zeros(n)
+            lib.ref_sim_get(key.encode(), v.ctypes.data_as(C.c_void_p))
+            return v
+
+        dims = get("dims")
+        # no near-field pixel within 1e-4 um of a sphere surface: there the single-precision
+        # inside test (d < a) of the float build and the double-precision one could disagree
+        q = get("nf_quad")
+        R0, R1 = int(dims[0]), int(dims[1])
+        u = np.arange(R0)[None, :, None] / R0
+        v = np.arange(R1)[:, None, None] / R1
+        pts = q[0:3] + q[3:6] * u + q[6:9] * v
+        for s in range(int(dims[4])):
+            sin = get(f"sphere{s}.in")
+            gap = np.abs(np.linalg.norm(pts - sin[:3], axis=2) - sin[3]).min()
+            assert gap > 1e-4, (name, s, gap)
+        rec = {"build": b, "flags": flags, "stop": stop, "dims": dims.tolist(), "scene": get("scene").tolist(),
+               "nf_quad": get("nf_quad").tolist(), "waves": enc(get("waves")), "spheres": []}
+        for s in range(int(dims[4])):
+            sp = {"in": get(f"sphere{s}.in").tolist(), "geom": get(f"sphere{s}.geom").tolist(),
+                  "A": enc(get(f"sphere{s}.A")), "B": enc(get(f"sphere{s}.B"))}
+            usp = get(f"sphere{s}.Usp")
+            if stop == 1 and usp is not None:
+                g = sp["geom"]
+                dR, thetaR, aR = int(g[3]), int(g[4]), int(g[5])
+                usp = usp.view(np.complex128).reshape(thetaR, dR)[TABLE_THETA_ROWS]
+                uip = get(f"sphere{s}.Uip").view(np.complex128).reshape(thetaR, aR)[TABLE_THETA_ROWS]
+                sp.update(theta_rows=TABLE_THETA_ROWS, Usp=enc(usp.view(np.float64)), Uip=enc(uip.view(np.float64)))
+            rec["spheres"].append(sp)
+        if stop == 0:
+            for key in ("U", "Uf", "D", "Di", "Absorbance"):
+                rec[key] = enc(get(key))
+        out[name] = rec
+        print(name, b, "R =", int(dims[0]), "res =", int(dims[2]), "ss =", int(dims[3]), "waves =", int(dims[5]))
+    with open(os.path.join(HERE, "ref_sim.json"), "w") as fh:
+        json.dump(out, fh, separators=(",", ":"))
+    print("wrote ref_sim.json", os.path.getsize(os.path.join(HERE, "ref_sim.json")), "bytes")
+
+
+if __name__ == "__main__":
+    main()

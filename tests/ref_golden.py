@@ -1,0 +1,83 @@
+"""Reader of tests/golden/ref_sim.json: golden outputs of the reference's own path run on the CPU
+(recorded by tests/golden/make_ref_sim_golden.py from the host-run build of the reference's
+sources).  Rebuilds each scene's bs_params and spheres from the inputs as the reference held them
+after parsing its flags."""
+import base64
+import json
+import os
+
+import numpy as np
+
+from bimsim_gb300 import abi
+
+PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ref_sim.json")
+_cache = None
+
+
+def load():
+    global _cache
+    if _cache is None:
+        with open(PATH) as fh:
+            _cache = json.load(fh)
+    return _cache
+
+
+def arr(b64):
+    return np.frombuffer(base64.b64decode(b64), dtype="<f8").copy()
+
+
+def flag(flags, name, n):
+    i = flags.index("--" + name)
+    return [float(np.float32(v)) for v in flags[i + 1:i + 1 + n]]
+
+
+def plane(flags):
+    """(pmin, pmax, normal) as lImagePlane builds them in single precision (arguments.h:340-407)."""
+    f = np.float32
+    if "--xy" in flags:
+        s, z = flag(flags, "xy", 2)
+        h = float(f(s) / f(2))
+        return (-h, -h, z), (h, h, z), (0.0, 0.0, 1.0)
+    if "--xz" in flags:
+        s, y = flag(flags, "xz", 2)
+        h = float(f(s) / f(2))
+        return (-h, y, -h), (h, y, h), (0.0, -1.0, 0.0)
+    if "--yz" in flags:
+        s, x = flag(flags, "yz", 2)
+        h = float(f(s) / f(2))
+        return (x, -h, -h), (x, h, h), (1.0, 0.0, 0.0)
+    raise ValueError("scene without an axis-aligned plane flag")
+
+
+def params(rec):
+    sc, dims = rec["scene"], rec["dims"]
+    pmin, pmax, nrm = plane(rec["flags"])
+    p = abi.make_params(lam=sc[0], amplitude=sc[1], k_dir=tuple(sc[2:5]), focus=tuple(sc[5:8]),
+                        condenser=tuple(sc[8:10]), objective=tuple(sc[10:12]), plane=(pmin, pmax, nrm),
+                        resolution=int(dims[2]), padding=int(sc[12]), supersample=int(sc[13]),
+                        field_order=int(sc[14]), lut_us=bool(sc[15]), lut_uf=bool(sc[16]), plane_wave=bool(sc[17]),
+                        scalar="--vector" not in rec["flags"])
+    return p
+
+
+def spheres(rec):
+    return [tuple(s["in"]) for s in rec["spheres"]]
+
+
+def waves(rec):
+    return arr(rec["waves"]).reshape(-1, 3)
+
+
+def field(rec, key):
+    R0, R1 = int(rec["dims"][0]), int(rec["dims"][1])
+    return arr(rec[key]).view(np.complex128).reshape(R1, R0)
+
+
+def image(rec, key):
+    res = int(rec["dims"][2])
+    return arr(rec[key]).reshape(res, res)
+
+
+def scenes(build=None, full=True):
+    d = load()
+    return sorted(n for n, r in d.items() if (build is None or r["build"] == build) and (r["stop"] == 0) == full)

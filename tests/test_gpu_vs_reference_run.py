@@ -1,0 +1,74 @@
+"""The GPU path through the C ABI, and the `bimsim` CLI run with the reference's own flags, against
+the reference's own path run on the CPU (golden ref_sim.json; see tests/golden/make_ref_sim_golden.py).
+
+  * double-precision build of the reference: the FP64 GPU path within 1e-10 relative L2 on U, Uf,
+    D, Di and absorbance; the mixed path within 1e-5 on the images and 1e-4 on the near field
+  * the reference as it ships (single precision, LUT mode): both GPU paths within 1e-5 on the
+    images and 1e-4 on the near field (the reference's own float rounding is ~2e-6)
+  * the CLI with the reference's flags (its Monte Carlo directions from the compat sampler): the
+    ENVI images within 1e-5 of the shipped reference's images
+"""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+import ref_golden as rg
+from bimsim_gb300 import (BS_FIELD_INCIDENT, BS_FIELD_TOTAL, BS_IMG_ABSORBANCE, BS_IMG_INCIDENT, BS_IMG_INTENSITY,
+                          BS_PREC_FP64, BS_PREC_MIXED, Context, lib)
+
+pytestmark = pytest.mark.gpu
+
+EXE = os.path.join(os.path.dirname(lib.library_path()), "bimsim")
+
+
+def rel(a, b):
+    return float(np.linalg.norm((np.asarray(a) - np.asarray(b)).ravel()) / np.linalg.norm(np.asarray(b).ravel()))
+
+
+def gpu_run(rec, prec):
+    with Context(rg.params(rec)) as ctx:
+        ctx.set_spheres(rg.spheres(rec))
+        ctx.set_waves(rg.waves(rec))
+        ctx.simulate(prec)
+        return {"U": ctx.field(BS_FIELD_TOTAL), "Uf": ctx.field(BS_FIELD_INCIDENT),
+                "D": ctx.image(BS_IMG_INTENSITY, f64=True), "Di": ctx.image(BS_IMG_INCIDENT, f64=True),
+                "Absorbance": ctx.image(BS_IMG_ABSORBANCE, f64=True)}
+
+
+def errors(out, rec):
+    return {k: rel(out[k], rg.field(rec, k) if k in ("U", "Uf") else rg.image(rec, k)) for k in out}
+
+
+@pytest.mark.parametrize("name", rg.scenes("f64"))
+def test_gpu_matches_the_references_double_precision_run(name):
+    rec = rg.load()[name]
+    e64 = errors(gpu_run(rec, BS_PREC_FP64), rec)
+    assert max(e64.values()) <= 1e-10, e64
+    emx = errors(gpu_run(rec, BS_PREC_MIXED), rec)
+    assert max(emx[k] for k in ("D", "Di", "Absorbance")) <= 1e-5, emx
+    assert max(emx[k] for k in ("U", "Uf")) <= 1e-4, emx
+
+
+@pytest.mark.parametrize("name", rg.scenes("f32"))
+def test_gpu_matches_the_shipped_references_run(name):
+    rec = rg.load()[name]
+    for prec in (BS_PREC_FP64, BS_PREC_MIXED):
+        e = errors(gpu_run(rec, prec), rec)
+        assert max(e[k] for k in ("D", "Di", "Absorbance")) <= 1e-5, (prec, e)
+        assert max(e[k] for k in ("U", "Uf")) <= 1e-4, (prec, e)
+
+
+@pytest.mark.parametrize("name", rg.scenes("f32"))
+def test_cli_with_the_references_flags_matches_its_run(name, tmp_path):
+    rec = rg.load()[name]
+    outs = {k: str(tmp_path / k) for k in ("D", "Di", "Absorbance")}
+    cmd = [EXE] + rec["flags"] + ["--intensity", outs["D"], "--incident", outs["Di"], "--absorbance",
+                                  outs["Absorbance"], "--absorbance-spec", ""]
+    r = subprocess.run(cmd, capture_output=True, text=True, cwd=str(tmp_path))
+    assert r.returncode == 0, r.stdout + r.stderr
+    res = int(rec["dims"][2])
+    for key, path in outs.items():
+        img = np.fromfile(path, dtype=np.float32).reshape(res, res)
+        assert rel(img, rg.image(rec, key)) <= 1e-5, (key, rel(img, rg.image(rec, key)))

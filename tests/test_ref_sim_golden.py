@@ -1,0 +1,151 @@
+"""The oracle against the reference's own path run on the CPU (golden ref_sim.json, recorded by
+tests/golden/make_ref_sim_golden.py from the reference's sources, .cu files included, compiled in
+place for the host with CUDA stand-ins).
+
+  * double-precision build of the reference (ptype double; every path except the LUT apply and the
+    incident-field LUT, whose texture copies are hard-coded for float): near fields U, Uf and
+    detector images D, Di within 1e-12 relative L2, Mie coefficients within 1e-12, the per-sphere
+    tables Usp/Uip of sphere::calcUp + sphere.cu within 1e-12
+  * the reference as it ships (ptype float, LUT apply through emulated texture fetches with exact
+    bilinear weights): within 1e-5, the single-precision rounding of its arithmetic
+  * the parsed plane, wavelength (--nu) and Monte Carlo directions as the reference derives them
+"""
+import os
+
+import numpy as np
+import pytest
+
+import oracle_lib
+import ref_golden as rg
+from bimsim_gb300 import abi
+
+TOL_F64 = 1e-12
+TOL_F32 = 1e-5
+
+
+def rel(a, b):
+    return float(np.linalg.norm((np.asarray(a) - np.asarray(b)).ravel()) / np.linalg.norm(np.asarray(b).ravel()))
+
+
+def oracle_run(rec):
+    p = rg.params(rec)
+    arr, ns = abi.sphere_array(rg.spheres(rec))
+    return p, oracle_lib.simulate(p, arr, ns, rg.waves(rec))
+
+
+@pytest.mark.parametrize("name", rg.scenes("f64"))
+def test_oracle_matches_the_references_double_precision_run(name):
+    rec = rg.load()[name]
+    p, (U, Uf, D, Di) = oracle_run(rec)
+    errs = {"U": rel(U, rg.field(rec, "U")), "Uf": rel(Uf, rg.field(rec, "Uf")), "D": rel(D, rg.image(rec, "D")),
+            "Di": rel(Di, rg.image(rec, "Di"))}
+    assert max(errs.values()) <= TOL_F64, errs
+    with np.errstate(divide="ignore", invalid="ignore"):
+        assert rel(-np.log10(D / Di), rg.image(rec, "Absorbance")) <= TOL_F64
+
+
+@pytest.mark.parametrize("name", rg.scenes("f32"))
+def test_oracle_within_single_precision_of_the_shipped_reference(name):
+    rec = rg.load()[name]
+    p, (U, Uf, D, Di) = oracle_run(rec)
+    errs = {"U": rel(U, rg.field(rec, "U")), "Uf": rel(Uf, rg.field(rec, "Uf")), "D": rel(D, rg.image(rec, "D")),
+            "Di": rel(Di, rg.image(rec, "Di"))}
+    assert max(errs.values()) <= TOL_F32, errs
+
+
+@pytest.mark.parametrize("name", rg.scenes())
+def test_mie_coefficients_match_the_reference_run(name):
+    rec = rg.load()[name]
+    p = rg.params(rec)
+    g = oracle_lib.geom(p)
+    for sp in rec["spheres"]:
+        A = rg.arr(sp["A"]).view(np.complex128)
+        B = rg.arr(sp["B"]).view(np.complex128)
+        nl = len(A) - 1
+        assert nl == int(sp["geom"][0]) == oracle_lib.load().bso_calc_nl(sp["in"][3], p.lambda_)
+        Ao, Bo = np.zeros(2 * nl + 2), np.zeros(2 * nl + 2)
+        oracle_lib.load().bso_mie(g.kmag, *sp["in"][3:6], nl, oracle_lib.P(Ao), oracle_lib.P(Bo))
+        tol = TOL_F64 if rec["build"] == "f64" else 1e-6  # the float build stores them as float
+        assert rel(Ao.view(np.complex128), A) <= tol and rel(Bo.view(np.complex128), B) <= tol
+
+
+@pytest.mark.parametrize("name", rg.scenes(full=False))
+def test_sphere_tables_match_the_reference_run(name):
+    rec = rg.load()[name]
+    p = rg.params(rec)
+    for sp in rec["spheres"]:
+        s = abi.Sphere(*sp["in"])
+        sg = oracle_lib.sphere_geom(p, s)
+        Nl, dmin, dmax, dR, thetaR, aR = (int(sp["geom"][0]), sp["geom"][1], sp["geom"][2], int(sp["geom"][3]),
+                                          int(sp["geom"][4]), int(sp["geom"][5]))
+        assert (sg.Nl, sg.dR, sg.thetaR, sg.aR) == (Nl, dR, thetaR, aR)
+        assert sg.d_min == pytest.approx(dmin, abs=1e-12) and sg.d_max == pytest.approx(dmax, rel=1e-14)
+        usp = np.zeros(2 * sg.dR * sg.thetaR)
+        uip = np.zeros(2 * sg.aR * sg.thetaR)
+        oracle_lib.load().bso_sphere_luts(oracle_lib.C.byref(p), oracle_lib.C.byref(s), oracle_lib.P(usp),
+                                          oracle_lib.P(uip))
+        rows = sp["theta_rows"]
+        mine_u = usp.view(np.complex128).reshape(dR, thetaR).T[rows]  # reference layout: [theta][r]
+        mine_i = uip.view(np.complex128).reshape(aR, thetaR).T[rows]
+        ref_u = rg.arr(sp["Usp"]).view(np.complex128).reshape(len(rows), dR)
+        ref_i = rg.arr(sp["Uip"]).view(np.complex128).reshape(len(rows), aR)
+        assert rel(mine_u, ref_u) <= TOL_F64 and rel(mine_i, ref_i) <= TOL_F64
+
+
+@pytest.mark.parametrize("name", rg.scenes() + rg.scenes(full=False))
+def test_parsed_geometry_matches(name):
+    """The near-field quad nf.pos and the derived sizes are the oracle's (arguments.h:340-438,
+    microscope.cu:700-718); --nu gives lambda = 1e4/nu in single precision (arguments.h:118-123)."""
+    rec = rg.load()[name]
+    p = rg.params(rec)
+    g = oracle_lib.geom(p)
+    np.testing.assert_allclose(list(g.A) + list(g.X) + list(g.Y), rec["nf_quad"], rtol=0, atol=1e-12)
+    assert (g.R, g.det_res) == (int(rec["dims"][0]), int(rec["dims"][2]))
+    # ss from the plane size, which only --xy sets (40 otherwise; arguments.h:346-418)
+    fl = rec["flags"]
+    kw = {"xy": tuple(rg.flag(fl, "xy", 2))} if "--xy" in fl else {"plane": rg.plane(fl)}
+    assert int(rec["scene"][13]) == abi.make_params(lam=p.lambda_, resolution=p.resolution, **kw).supersample
+    if "--nu" in rec["flags"]:
+        nu = np.float32(rec["flags"][rec["flags"].index("--nu") + 1])
+        assert rec["scene"][0] == float(np.float32(10000) / nu)
+
+
+@pytest.mark.parametrize("name", rg.scenes("f32"))
+def test_reference_directions_are_the_compat_sampler(name):
+    """The directions the shipped reference drew (srand(0) then mcSampleNA) are the oracle's
+    restatement, which bs_sample_waves_compat reproduces on the GPU."""
+    rec = rg.load()[name]
+    p = rg.params(rec)
+    nk = int(rec["dims"][5])
+    out = np.zeros(3 * nk)
+    kd = np.array(p.k_dir[:])
+    oracle_lib.load().bso_mc_sample(nk, oracle_lib.P(kd), p.condenser[0], p.condenser[1], oracle_lib.P(out))
+    np.testing.assert_allclose(out, rg.waves(rec).ravel(), rtol=0, atol=2e-7)
+
+
+@pytest.mark.parametrize("name", rg.scenes("f32"))
+def test_cli_parses_the_references_flags_into_its_state(name):
+    """The `bimsim` CLI of this project, given the reference's flags, derives the state the
+    shipped reference held after LoadParameters (single-precision values)."""
+    import json
+    import subprocess
+
+    from bimsim_gb300 import lib
+    exe = os.path.join(os.path.dirname(lib.library_path()), "bimsim")
+    if not os.path.exists(exe):
+        from bimsim_gb300 import build
+        build.build()
+    rec = rg.load()[name]
+    r = subprocess.run([exe, "--dry-run"] + rec["flags"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    d = json.loads(r.stdout.strip().splitlines()[-1])
+    sc = rec["scene"]
+    f = lambda v: float(np.float32(v))  # noqa: E731
+    assert f(d["lambda"]) == sc[0] and f(d["amplitude"]) == sc[1]
+    assert [f(v) for v in d["k"]] == sc[2:5] and [f(v) for v in d["focus"]] == sc[5:8]
+    assert [f(v) for v in d["condenser"]] == sc[8:10] and [f(v) for v in d["objective"]] == sc[10:12]
+    assert (d["padding"], d["supersample"], d["field_order"]) == (int(sc[12]), int(sc[13]), int(sc[14]))
+    assert (d["lut_us"], d["lut_uf"], d["plane_wave"], d["samples"]) == tuple(int(v) for v in sc[15:19])
+    assert d["resolution"] == int(rec["dims"][2])
+    for mine, theirs in zip(d["spheres"], rec["spheres"]):
+        assert [f(v) for v in mine] == [f(v) for v in theirs["in"]]
