@@ -166,6 +166,8 @@ struct bs_ctx {
 
     DevBuf d_sph, d_waves, d_kw4, d_ph, d_A, d_B, d_mie, d_tab, d_tabscr, d_legP, d_lut, d_uft, d_uftscr;
     DevBuf d_cones, d_cnt;  // per-chunk wave cones; staged / total counters of the mixed LUT kernel
+    std::unique_ptr<WaveDirs> wdirs;  // grouped directions as kernel parameters of the mixed LUT kernel
+    bool wdirs_ok = false;
     DevBuf d_far;           // far fields Ud, Ufd on request (bs_get_far_field)
     DevBuf d_starts;        // row / coefficient offsets of a coefficient batch
     DevBuf d_fsave;         // U, Uf of a ring's first source (bs_simulate_ring_interp)
@@ -853,6 +855,14 @@ static bs_status run_nearfield(bs_ctx* c) {
         sort_waves(w, chunk);
     }
     c->stats.lut_wave_chunk = chunk;
+    // the mixed LUT kernel reads the grouped directions, rounded to float as the phase
+    // kernel rounds them into kw4, from its parameters when they fit there
+    c->wdirs_ok = !fp64 && p.scalar && p.lut_us && ns > 0 && !p.plane_wave && nk <= LUT_PARAM_WAVES;
+    if (c->wdirs_ok) {
+        if (!c->wdirs) c->wdirs.reset(new WaveDirs());
+        for (int i = 0; i < nk; i++)
+            for (int k = 0; k < 3; k++) c->wdirs->k[k][i] = (float)w[3 * (size_t)i + k];
+    }
     CK(c->d_waves.ensure(w.size() * sizeof(double)));
     CK(cudaMemcpyAsync(c->d_waves.p, w.data(), w.size() * sizeof(double), cudaMemcpyHostToDevice, c->st));
 
@@ -1069,7 +1079,7 @@ static bs_status run_nearfield(bs_ctx* c) {
                                   c->d_cones.as<float4>(), c->d_ph.as<cpx<float>>(),
                                   c->d_texobj.as<unsigned long long>(), c->d_lut.as<float2>(), (const cpx<float>*)Uf,
                                   (cpx<float>*)U, ns > 0 ? c->d_cnt.as<unsigned long long>() : nullptr, use_stage,
-                                  chunk, c->st);
+                                  chunk, c->wdirs_ok ? c->wdirs.get() : nullptr, c->st);
             }
             LAUNCHED(c);
             // the handle list and the table slots are reused by the next chunk

@@ -3,10 +3,12 @@ the reference's own path run on the CPU (golden ref_sim.json; see tests/golden/m
 
   * double-precision build of the reference: the FP64 GPU path within 1e-10 relative L2 on U, Uf,
     D, Di and absorbance; the mixed path within 1e-5 on the images and 1e-4 on the near field
-  * the reference as it ships (single precision, LUT mode): both GPU paths within 1e-5 on the
-    images and 1e-4 on the near field (the reference's own float rounding is ~2e-6)
+  * the reference as it ships (single precision): both GPU paths within 1e-5 on D and Di, 5e-5 on
+    absorbance and 1e-4 on the near field.  The shipped build's own single-precision error against
+    the FP64 oracle is up to 2e-6 on D, Di and 1.3e-5 on absorbance (a log of a ratio of nearly equal
+    images, direct mode), hence the looser absorbance bound against it
   * the CLI with the reference's flags (its Monte Carlo directions from the compat sampler): the
-    ENVI images within 1e-5 of the shipped reference's images
+    ENVI images within the same bounds of the shipped reference's images
 """
 import os
 import subprocess
@@ -51,13 +53,15 @@ def test_gpu_matches_the_references_double_precision_run(name):
     assert max(emx[k] for k in ("U", "Uf")) <= 1e-4, emx
 
 
+TOL_F32 = {"D": 1e-5, "Di": 1e-5, "Absorbance": 5e-5, "U": 1e-4, "Uf": 1e-4}
+
+
 @pytest.mark.parametrize("name", rg.scenes("f32"))
 def test_gpu_matches_the_shipped_references_run(name):
     rec = rg.load()[name]
     for prec in (BS_PREC_FP64, BS_PREC_MIXED):
         e = errors(gpu_run(rec, prec), rec)
-        assert max(e[k] for k in ("D", "Di", "Absorbance")) <= 1e-5, (prec, e)
-        assert max(e[k] for k in ("U", "Uf")) <= 1e-4, (prec, e)
+        assert all(e[k] <= TOL_F32[k] for k in e), (prec, e)
 
 
 @pytest.mark.parametrize("name", rg.scenes("f32"))
@@ -71,4 +75,4 @@ def test_cli_with_the_references_flags_matches_its_run(name, tmp_path):
     res = int(rec["dims"][2])
     for key, path in outs.items():
         img = np.fromfile(path, dtype=np.float32).reshape(res, res)
-        assert rel(img, rg.image(rec, key)) <= 1e-5, (key, rel(img, rg.image(rec, key)))
+        assert rel(img, rg.image(rec, key)) <= TOL_F32[key], (key, rel(img, rg.image(rec, key)))
