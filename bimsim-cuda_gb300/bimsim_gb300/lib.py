@@ -63,6 +63,7 @@ def library():
         "bs_material_eval": ([C.c_char_p, vp, i32, vp], C.c_int),
     "bs_material_kk": ([C.c_char_p, C.c_double, i32, i32, vp, vp], C.c_int),
         "bs_set_lut_reuse": ([vp, i32], C.c_int),
+        "bs_set_stream_priority": ([vp, i32], C.c_int),
         "bs_set_lut_staging": ([vp, i32], C.c_int),
     "bs_set_lut_wave_chunk": ([vp, i32], C.c_int),
     "bs_set_backpropagation": ([vp, i32, C.c_double], C.c_int),

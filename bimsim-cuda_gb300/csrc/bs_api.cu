@@ -166,8 +166,6 @@ struct bs_ctx {
 
     DevBuf d_sph, d_waves, d_kw4, d_ph, d_A, d_B, d_mie, d_tab, d_tabscr, d_legP, d_lut, d_uft, d_uftscr;
     DevBuf d_cones, d_cnt;  // per-chunk wave cones; staged / total counters of the mixed LUT kernel
-    std::unique_ptr<WaveDirs> wdirs;  // grouped directions as kernel parameters of the mixed LUT kernel
-    bool wdirs_ok = false;
     DevBuf d_far;           // far fields Ud, Ufd on request (bs_get_far_field)
     DevBuf d_starts;        // row / coefficient offsets of a coefficient batch
     DevBuf d_fsave;         // U, Uf of a ring's first source (bs_simulate_ring_interp)
@@ -184,6 +182,7 @@ struct bs_ctx {
     bs_stats stats{};
     // table reuse between runs (bs_set_lut_reuse)
     bool reuse = false;
+    int stream_prio = 0;  // bs_set_stream_priority (0: the default priority)
     int lut_staging = 0;  // bs_set_lut_staging: 0 model-chosen, 1 staged kernel, 2 texture-only kernel
     int lut_chunk = 0;    // bs_set_lut_wave_chunk: 0 model-chosen, else waves per chunk
     bool bp_on = false;   // bs_set_backpropagation
@@ -855,14 +854,6 @@ static bs_status run_nearfield(bs_ctx* c) {
         sort_waves(w, chunk);
     }
     c->stats.lut_wave_chunk = chunk;
-    // the mixed LUT kernel reads the grouped directions, rounded to float as the phase
-    // kernel rounds them into kw4, from its parameters when they fit there
-    c->wdirs_ok = !fp64 && p.scalar && p.lut_us && ns > 0 && !p.plane_wave && nk <= LUT_PARAM_WAVES;
-    if (c->wdirs_ok) {
-        if (!c->wdirs) c->wdirs.reset(new WaveDirs());
-        for (int i = 0; i < nk; i++)
-            for (int k = 0; k < 3; k++) c->wdirs->k[k][i] = (float)w[3 * (size_t)i + k];
-    }
     CK(c->d_waves.ensure(w.size() * sizeof(double)));
     CK(cudaMemcpyAsync(c->d_waves.p, w.data(), w.size() * sizeof(double), cudaMemcpyHostToDevice, c->st));
 
@@ -1079,7 +1070,7 @@ static bs_status run_nearfield(bs_ctx* c) {
                                   c->d_cones.as<float4>(), c->d_ph.as<cpx<float>>(),
                                   c->d_texobj.as<unsigned long long>(), c->d_lut.as<float2>(), (const cpx<float>*)Uf,
                                   (cpx<float>*)U, ns > 0 ? c->d_cnt.as<unsigned long long>() : nullptr, use_stage,
-                                  chunk, c->wdirs_ok ? c->wdirs.get() : nullptr, c->st);
+                                  chunk, c->st);
             }
             LAUNCHED(c);
             // the handle list and the table slots are reused by the next chunk
@@ -1192,6 +1183,24 @@ bs_status bs_set_lut_wave_chunk(bs_ctx* c, int32_t chunk) {
 bs_status bs_set_lut_staging(bs_ctx* c, int32_t mode) {
     if (!c || mode < 0 || mode > 2) return fail(BS_ERR_ARG, "bs_set_lut_staging: mode must be 0, 1 or 2");
     c->lut_staging = mode;
+    return BS_OK;
+}
+
+bs_status bs_set_stream_priority(bs_ctx* c, int32_t priority) {
+    if (!c) return fail(BS_ERR_ARG, "bs_set_stream_priority: null context");
+    int least = 0, greatest = 0;
+    cudaError_t e = cudaDeviceGetStreamPriorityRange(&least, &greatest);
+    if (e != cudaSuccess) return fail(BS_ERR_CUDA, "bs_set_stream_priority: %s", cudaGetErrorString(e));
+    const int prio = std::min(least, std::max(greatest, (int)priority));
+    if (prio == c->stream_prio) return BS_OK;
+    // the context's work so far finishes on the old stream; later work goes to the new one
+    e = cudaStreamSynchronize(c->st);
+    cudaStream_t st = nullptr;
+    if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&st, cudaStreamNonBlocking, prio);
+    if (e != cudaSuccess) return fail(BS_ERR_CUDA, "bs_set_stream_priority: %s", cudaGetErrorString(e));
+    cudaStreamDestroy(c->st);
+    c->st = st;
+    c->stream_prio = prio;
     return BS_OK;
 }
 

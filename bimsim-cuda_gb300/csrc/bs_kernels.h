@@ -24,17 +24,6 @@ constexpr float LUT_STAGE_MARGIN = 2e-3f;
 // lanes reading the same column of different rows fall in different banks.
 __host__ __device__ constexpr int lut_stage_stride(int W) { return W | 1; }
 
-// Directions of up to LUT_PARAM_WAVES grouped plane waves, single precision,
-// passed to the mixed LUT kernel as a kernel parameter (24 KB of the 32 KB
-// parameter space): every thread of a block reads the same wave at the same
-// step, and a uniform read of the parameter (constant) space takes the
-// direction out of the shared-memory pipe that the table cells saturate.
-// Runs with more waves read the directions through shared memory.
-constexpr int LUT_PARAM_WAVES = 2048;
-struct WaveDirs {
-    float k[3][LUT_PARAM_WAVES];
-};
-
 template <class T>
 struct cpx;
 using zd = cpx<double>;
@@ -71,12 +60,10 @@ void launch_us_lut_f64(const Scene& sc, const Sphere* sph, int s0, int s1, int a
 // cones: one {axis, half-angle} per `chunk` waves; counters[0..1] receive
 // the staged and total (sphere, chunk) counts of every block (may be null);
 // stage = false runs the texture-only variant
-// dirs: the grouped directions as kernel parameters (nk <= LUT_PARAM_WAVES), or
-// null to read them from kw4 through shared memory
 void launch_us_lut_tex(const Scene& sc, const Sphere* sph, int s0, int s1, int accumulate, int finalize,
                        const float4* kw4, const float4* cones, const cpx<float>* ph, const unsigned long long* tex,
                        const float2* lin, const cpx<float>* Uf, cpx<float>* U, unsigned long long* counters,
-                       bool stage, int chunk, const WaveDirs* dirs, cudaStream_t st);
+                       bool stage, int chunk, cudaStream_t st);
 void launch_lut_build_tex(const zd* tab, int rows, int L, const double* P, int Pstride, int thetaR,
                           cudaSurfaceObject_t sre, cudaSurfaceObject_t sim, float2* lin, int lin_stride,
                           cudaStream_t st);

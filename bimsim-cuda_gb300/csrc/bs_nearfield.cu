@@ -4,8 +4,6 @@
 // into the epilogue.
 #include <cuda_runtime.h>
 
-#include <type_traits>
-
 #include <climits>
 
 #include "bs_kernels.h"
@@ -537,19 +535,9 @@ __device__ __forceinline__ int2 chunk_plan(const float4 cone, const TileSphere& 
 // thread: the tile's eight 4 x 8 warp blocks are spread over 8 / PPT warps, and
 // each wave's direction and phase (shared-memory broadcasts) are read once for
 // the thread's PPT pixels.  Every pixel's arithmetic is the same for any PPT.
-// WD: WaveDirs (directions read from the kernel parameters) or NoWaveDirs
-// (directions copied per chunk into shared memory from kw4).
-struct NoWaveDirs {};
-
-__device__ __forceinline__ float4 wave_dir(const WaveDirs& wd, const float4*, int w0, int w) {
-    return make_float4(wd.k[0][w0 + w], wd.k[1][w0 + w], wd.k[2][w0 + w], 0.f);
-}
-__device__ __forceinline__ float4 wave_dir(const NoWaveDirs&, const float4* s_k, int, int w) { return s_k[w]; }
-
-template <bool STAGE, int PPT, class WD>
+template <bool STAGE, int PPT>
 __global__ void __launch_bounds__(UST_TILE / PPT, STAGE ? 4 : 6) us_lut_tex_kernel(Scene sc, const Sphere* __restrict__ sph, int s0, int s1,
                                                                     int accumulate, int finalize,
-                                                                    const __grid_constant__ WD wd,
                                                                     const float4* __restrict__ kw4,
                                                                     const float4* __restrict__ cones,
                                                                     const cpx<float>* __restrict__ ph,
@@ -560,7 +548,6 @@ __global__ void __launch_bounds__(UST_TILE / PPT, STAGE ? 4 : 6) us_lut_tex_kern
                                                                     unsigned long long* __restrict__ counters,
                                                                     int chunk) {
     constexpr int NT = UST_TILE / PPT, NWARP = NT / 32;
-    constexpr bool KP = std::is_same<WD, WaveDirs>::value;
     static_assert(NT >= UST_CHUNK && NT % 32 == 0, "one thread per wave of a chunk");
     extern __shared__ float2 s_stage[];
     __shared__ float4 s_k[UST_CHUNK];
@@ -725,7 +712,7 @@ __global__ void __launch_bounds__(UST_TILE / PPT, STAGE ? 4 : 6) us_lut_tex_kern
             const int t_lo = pl.x, W = pl.y, Ws = lut_stage_stride(W);
             const bool staged = STAGE && W > 0;
             if (threadIdx.x < nw) {
-                if (!KP) copy_async16(&s_k[threadIdx.x], kw4 + w0 + threadIdx.x);
+                copy_async16(&s_k[threadIdx.x], kw4 + w0 + threadIdx.x);
                 copy_async8(&s_p[threadIdx.x], reinterpret_cast<const float2*>(ph + (size_t)s * sc.nk + w0) + threadIdx.x);
             }
             if (STAGE && staged) {
@@ -762,7 +749,7 @@ __global__ void __launch_bounds__(UST_TILE / PPT, STAGE ? 4 : 6) us_lut_tex_kern
                 }
 #pragma unroll(8 / PPT)
                 for (int w = 0; w < nw; w++) {
-                    const float4 kk = wave_dir(wd, s_k, w0, w);
+                    const float4 kk = s_k[w];
                     const float2 pw = s_p[w];
                     const f32x2 pwx = f2_splat(pw.x), pwy = f2_splat(pw.y);
 #pragma unroll
@@ -798,7 +785,7 @@ __global__ void __launch_bounds__(UST_TILE / PPT, STAGE ? 4 : 6) us_lut_tex_kern
                 }
 #pragma unroll 1
                 for (int w = 0; w < nw; w++) {
-                    const float4 kk = wave_dir(wd, s_k, w0, w);
+                    const float4 kk = s_k[w];
                     const float2 pw = s_p[w];
 #pragma unroll
                     for (int j = 0; j < PPT; j++) {
@@ -1181,36 +1168,25 @@ void launch_us_lut_f64(const Scene& sc, const Sphere* sph, int s0, int s1, int a
                                                            Uf, U);
 }
 
-template <class WD>
-void launch_us_lut_tex_wd(const Scene& sc, const Sphere* sph, int s0, int s1, int accumulate, int finalize,
-                          const WD& wd, const float4* kw4, const float4* cones, const cpx<float>* ph,
-                          const unsigned long long* tex, const float2* lin, const cpx<float>* Uf, cpx<float>* U,
-                          unsigned long long* counters, bool stage, int chunk, cudaStream_t st) {
+void launch_us_lut_tex(const Scene& sc, const Sphere* sph, int s0, int s1, int accumulate, int finalize,
+                       const float4* kw4, const float4* cones, const cpx<float>* ph, const unsigned long long* tex,
+                       const float2* lin, const cpx<float>* Uf, cpx<float>* U, unsigned long long* counters,
+                       bool stage, int chunk, cudaStream_t st) {
     int tiles = (sc.R + 15) / 16;
     if (!stage) {
-        us_lut_tex_kernel<false, 1, WD><<<(unsigned)tiles * tiles, UST_TILE, 0, st>>>(
-            sc, sph, s0, s1, accumulate, finalize, wd, kw4, cones, ph, tex, lin, Uf, U, counters, chunk);
+        us_lut_tex_kernel<false, 1><<<(unsigned)tiles * tiles, UST_TILE, 0, st>>>(sc, sph, s0, s1, accumulate, finalize,
+                                                                                 kw4, cones, ph, tex, lin, Uf, U,
+                                                                                 counters, chunk);
         return;
     }
     const int smem = UST_STAGE * (int)sizeof(float2);
     // per device and cheap; a failure shows up as the launch error
     const bool two = chunk >= UST_TWO_PIXEL_MIN_CHUNK;
-    auto kernel = two ? us_lut_tex_kernel<true, 2, WD> : us_lut_tex_kernel<true, 1, WD>;
+    auto kernel = two ? us_lut_tex_kernel<true, 2> : us_lut_tex_kernel<true, 1>;
     cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    kernel<<<(unsigned)tiles * tiles, two ? UST_TILE / 2 : UST_TILE, smem, st>>>(
-        sc, sph, s0, s1, accumulate, finalize, wd, kw4, cones, ph, tex, lin, Uf, U, counters, chunk);
-}
-
-void launch_us_lut_tex(const Scene& sc, const Sphere* sph, int s0, int s1, int accumulate, int finalize,
-                       const float4* kw4, const float4* cones, const cpx<float>* ph, const unsigned long long* tex,
-                       const float2* lin, const cpx<float>* Uf, cpx<float>* U, unsigned long long* counters,
-                       bool stage, int chunk, const WaveDirs* dirs, cudaStream_t st) {
-    if (dirs)
-        launch_us_lut_tex_wd(sc, sph, s0, s1, accumulate, finalize, *dirs, kw4, cones, ph, tex, lin, Uf, U, counters,
-                             stage, chunk, st);
-    else
-        launch_us_lut_tex_wd(sc, sph, s0, s1, accumulate, finalize, NoWaveDirs{}, kw4, cones, ph, tex, lin, Uf, U,
-                             counters, stage, chunk, st);
+    kernel<<<(unsigned)tiles * tiles, two ? UST_TILE / 2 : UST_TILE, smem, st>>>(sc, sph, s0, s1, accumulate, finalize,
+                                                                               kw4, cones, ph, tex, lin, Uf, U,
+                                                                               counters, chunk);
 }
 
 void launch_lut_build_tex(const zd* tab, int rows, int L, const double* P, int Pstride, int thetaR,

@@ -6,10 +6,13 @@
 // thread owns one bs_ctx (one CUDA stream), so admitted requests run
 // concurrently on the GPU.  Admission: a request goes to an idle worker when
 // the device bytes of all contexts, with that worker grown to the request's
-// estimate (bs_estimate_bytes), stay within the budget.  Requests start in
-// arrival order; a later request may start before a head request that does
-// not fit yet, at most 8 times per head request.  When the head fits nowhere,
-// idle workers give their buffers back.  Contexts keep their tables between
+// estimate (bs_estimate_bytes), stay within the budget.  Among the queued
+// requests that fit, the cheapest (pixels x spheres x directions) starts
+// first; a request passed by later ones 8 times starts next in any case.
+// Each context's stream gets a priority by the cost of its request, so that
+// the blocks of short requests are scheduled ahead of those of a long slice
+// already running.  When the oldest request fits nowhere, idle workers give
+// their buffers back.  Contexts keep their tables between
 // requests (bs_set_lut_reuse) and a request goes preferably to the worker
 // that last ran the same scene.  Every kernel is deterministic, so a result
 // does not depend on what else runs.
@@ -76,6 +79,7 @@ struct Request {
     int32_t prec = 0;
     int32_t image = 0;
     size_t est = 0;            // device bytes at its own table budget
+    double cost = 0;           // work estimate for the order and the stream priority
     uint64_t lut_budget = 0;   // table budget the request runs with (0 = all tables at once)
     uint64_t sig = 0;
     uint64_t shape = 0;        // sig, direction count and table budget: equal shapes allocate equal buffers
@@ -97,13 +101,30 @@ struct Worker {
     size_t bytes = 0;       // device bytes the context holds
     size_t run_bytes = 0;   // bound on the device bytes while the current job runs
     Request* job = nullptr;
+    int prio = 0;           // stream priority of the context
 };
+
+// Work of a request in (pixel, sphere, wave) interactions, near-field pixels
+// for a scene without spheres.
+double request_cost(const bs_params& p, size_t ns, int nk) {
+    const double R = (double)p.resolution * p.supersample * (2.0 * p.padding + 1.0);
+    return R * R * (double)std::max<size_t>(ns, 1) * (double)std::max(nk, 1);
+}
+
+// Stream priority tier of a request: 0 (scheduled first) for the cheapest,
+// one more per factor of ten of work above 1e10 interactions.
+int cost_tier(double cost) {
+    int t = 0;
+    for (double c = 1e10; cost > c && t < 8; c *= 10) t++;
+    return t;
+}
 
 }  // namespace
 
 struct bs_server {
     bs_server_config cfg{};
     int device = 0;
+    int prio_least = 0, prio_greatest = 0;  // stream priority range of the device
     size_t budget = 0;
     std::mutex mu;
     std::condition_variable cv_work, cv_done;
@@ -137,23 +158,31 @@ struct bs_server {
         return u <= budget;
     }
 
-    // Next request worker w may start (under mu), or nullptr.
+    // Can worker w start r now (under mu)?
+    bool usable(const Worker& w, const Request& r) const {
+        if (r.sig != w.sig) {
+            for (const auto& v : workers)  // an idle worker already holds this scene's tables
+                if (v.get() != &w && !v->job && v->sig == r.sig) return false;
+        }
+        return fits(w, r);
+    }
+
+    // Next request worker w may start (under mu), or nullptr: the cheapest
+    // that it can start, so that short requests do not queue behind long
+    // ones; a request passed MAX_SKIPS times by later ones is next in any case.
     Request* pick(Worker& w) {
+        size_t best = queue.size();
         for (size_t i = 0; i < queue.size(); i++) {
             Request* r = queue[i];
             if (i > 0 && queue[0]->skipped >= MAX_SKIPS) break;  // the head waits no longer
-            if (r->sig != w.sig) {
-                bool other = false;  // an idle worker already holds this scene's tables
-                for (const auto& v : workers)
-                    if (v.get() != &w && !v->job && v->sig == r->sig) other = true;
-                if (other) continue;
-            }
-            if (!fits(w, *r)) continue;
-            for (size_t j = 0; j < i; j++) queue[j]->skipped++;
-            queue.erase(queue.begin() + (long)i);
-            return r;
+            if (!usable(w, *r)) continue;
+            if (best == queue.size() || r->cost < queue[best]->cost) best = i;
         }
-        return nullptr;
+        if (best == queue.size()) return nullptr;
+        for (size_t j = 0; j < best; j++) queue[j]->skipped++;
+        Request* r = queue[best];
+        queue.erase(queue.begin() + (long)best);
+        return r;
     }
 
     // The head request fits no worker as things stand.
@@ -179,7 +208,15 @@ size_t bs_server::run(Worker& w, Request& r) {
     }
     bs_ctx* c = w.ctx;
     cudaSetDevice(device);
-    bs_status st = bs_set_params(c, &r.prm);
+    bs_status st = BS_OK;
+    // cheaper requests on higher-priority streams: their blocks are scheduled
+    // ahead of those of a long slice running on another worker
+    const int prio = prio_greatest + std::min(cost_tier(r.cost), prio_least - prio_greatest);
+    if (prio != w.prio) {
+        st = bs_set_stream_priority(c, prio);
+        if (st == BS_OK) w.prio = prio;
+    }
+    if (st == BS_OK) st = bs_set_params(c, &r.prm);
     if (st == BS_OK) st = bs_set_spheres(c, r.spheres.data(), (int32_t)r.spheres.size());
     if (st == BS_OK && !r.prm.plane_wave) {
         st = r.waves.empty() ? bs_sample_waves_compat(c, r.nk)
@@ -278,6 +315,8 @@ bs_status bs_server_create(const bs_server_config* cfg, bs_server** out) {
         if (e == cudaSuccess) e = cudaMemGetInfo(&free_b, &total_b);
         if (e != cudaSuccess) return set_error(BS_ERR_CUDA, std::string("bs_server_create: ") + cudaGetErrorString(e));
         s->budget = cfg->hbm_budget ? cfg->hbm_budget : (size_t)(0.80 * (double)free_b);
+        if (cudaDeviceGetStreamPriorityRange(&s->prio_least, &s->prio_greatest) != cudaSuccess)
+            s->prio_least = s->prio_greatest = 0;
     }
     bs_params p0{};
     p0.lambda = 1;
@@ -384,6 +423,7 @@ bs_status bs_submit(bs_server* s, const bs_request* q, uint64_t* ticket) {
         r->lut_budget = cap;
     }
     r->est = (size_t)est;
+    r->cost = request_cost(r->prm, r->spheres.size(), r->nk);
     r->sig = scene_signature(r->prm, r->spheres, r->prec);
     {
         uint64_t h = r->sig;

@@ -333,6 +333,15 @@ bs_status bs_set_lut_staging(bs_ctx* ctx, int32_t mode);
  * on for its contexts.  No reference counterpart. */
 bs_status bs_set_lut_reuse(bs_ctx* ctx, int32_t enable);
 
+/* Priority of the context's stream, as cudaStreamCreateWithPriority takes it:
+ * lower numbers are scheduled first when blocks of several streams wait for
+ * the GPU; clamped to the device's range (cudaDeviceGetStreamPriorityRange),
+ * default 0.  The context finishes its queued work, then continues on a new
+ * stream of that priority.  Results do not depend on it.  The serving front
+ * end gives cheap requests the higher priorities, so that their kernels are
+ * not queued behind the blocks of a long slice.  No reference counterpart. */
+bs_status bs_set_stream_priority(bs_ctx* ctx, int32_t priority);
+
 /* Return every device buffer of the context to the CUDA allocator (results of
  * the last run are dropped).  No reference counterpart. */
 bs_status bs_release_buffers(bs_ctx* ctx);

@@ -122,3 +122,21 @@ def test_a_failing_request_leaves_the_others_intact():
             assert np.array_equal(img, r, equal_nan=True)
         st = srv.stats()
         assert st.completed == 3 and st.failed == 1
+
+
+def test_stream_priority_keeps_results_identical():
+    """bs_set_stream_priority moves the context to a new stream of that priority (the server gives
+    cheap requests the higher ones); the slice's bits do not change."""
+    p, s, w, prec, kind = request(2)
+    with Context(p) as ctx:
+        ctx.set_spheres(s)
+        ctx.set_waves(w)
+        ctx.simulate(BS_PREC_MIXED)
+        a = ctx.image(BS_IMG_INTENSITY)
+        assert ctx.lib.bs_set_stream_priority(ctx.h, -1000) == 0  # clamped to the device's greatest
+        ctx.simulate(BS_PREC_MIXED)
+        b = ctx.image(BS_IMG_INTENSITY)
+        assert ctx.lib.bs_set_stream_priority(ctx.h, 0) == 0
+        ctx.simulate(BS_PREC_MIXED)
+        c = ctx.image(BS_IMG_INTENSITY)
+    assert np.array_equal(a, b) and np.array_equal(a, c)
