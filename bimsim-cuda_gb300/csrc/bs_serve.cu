@@ -11,7 +11,8 @@
 // first; a request passed by later ones 8 times starts next in any case.
 // Each context's stream gets a priority by the cost of its request, so that
 // the blocks of short requests are scheduled ahead of those of a long slice
-// already running.  When the oldest request fits nowhere, idle workers give
+// already running, and with two or more workers the last one is a fast lane
+// that only takes short requests.  When the oldest request fits nowhere, idle workers give
 // their buffers back.  Contexts keep their tables between
 // requests (bs_set_lut_reuse) and a request goes preferably to the worker
 // that last ran the same scene.  Every kernel is deterministic, so a result
@@ -47,6 +48,10 @@ double ms_between(Clock::time_point a, Clock::time_point b) {
 }
 
 constexpr int MAX_SKIPS = 8;  // a queued request is passed at most this often
+// With two or more workers the last one only takes requests of at most this
+// many (pixel, sphere, wave) interactions, so that a short request finds a
+// context even while long slices hold all the others.
+constexpr double FAST_LANE_COST = 1e11;
 
 bs_status set_error(bs_status st, const std::string& msg) {
     bs::set_last_error(msg.c_str());
@@ -170,11 +175,16 @@ struct bs_server {
     // Next request worker w may start (under mu), or nullptr: the cheapest
     // that it can start, so that short requests do not queue behind long
     // ones; a request passed MAX_SKIPS times by later ones is next in any case.
+    bool fast_lane(const Worker& w) const { return workers.size() >= 2 && w.index == (int)workers.size() - 1; }
+
     Request* pick(Worker& w) {
+        const bool fast = fast_lane(w);
         size_t best = queue.size();
         for (size_t i = 0; i < queue.size(); i++) {
             Request* r = queue[i];
-            if (i > 0 && queue[0]->skipped >= MAX_SKIPS) break;  // the head waits no longer
+            // the head waits no longer (the fast lane, which can never start a long head, goes on)
+            if (i > 0 && queue[0]->skipped >= MAX_SKIPS && !(fast && queue[0]->cost > FAST_LANE_COST)) break;
+            if (fast && r->cost > FAST_LANE_COST) continue;
             if (!usable(w, *r)) continue;
             if (best == queue.size() || r->cost < queue[best]->cost) best = i;
         }
