@@ -854,12 +854,10 @@ __global__ void __launch_bounds__(UST_TILE / PPT, STAGE ? 4 : 6) us_lut_tex_kern
 // sums as lut_build_kernel, written through surfaces) and into the linear
 // float2 table used for staging.  `rows` counts one spare row of the planes
 // that repeats the last table row.
-__global__ void __launch_bounds__(256) lut_build_tex_kernel(const zd* __restrict__ tab, int rows, int L,
-                                                              const double* __restrict__ P, int Pstride, int thetaR,
-                                                              cudaSurfaceObject_t sre, cudaSurfaceObject_t sim,
-                                                              float2* __restrict__ lin, int lin_stride) {
-    const int t = blockIdx.x * 32 + (threadIdx.x & 31);
-    const int r = blockIdx.y * 8 + (threadIdx.x >> 5);
+__device__ __forceinline__ void lut_build_tex_entry(const zd* __restrict__ tab, int rows, int L,
+                                                    const double* __restrict__ P, int Pstride, int thetaR,
+                                                    cudaSurfaceObject_t sre, cudaSurfaceObject_t sim,
+                                                    float2* __restrict__ lin, int lin_stride, int r, int t) {
     if (t >= thetaR || r >= rows) return;
     const zd* c = tab + (size_t)min(r, rows - 2) * L;  // the last row written repeats the one before
     const double* pl = P + (size_t)t * Pstride;
@@ -872,6 +870,25 @@ __global__ void __launch_bounds__(256) lut_build_tex_kernel(const zd* __restrict
         lin[(size_t)r * lin_stride + t] = v;
         if (t == thetaR - 1) lin[(size_t)r * lin_stride + thetaR] = v;  // clamped neighbour of the last column
     }
+}
+
+// Every table of a sphere batch in one launch: blockIdx.x runs over the
+// flattened blocks of 8 rows of all tables (the table found by binary search
+// on rb0), blockIdx.y over blocks of 32 angles.
+__global__ void __launch_bounds__(256) lut_build_tex_batch_kernel(const LutBuildJob* __restrict__ jobs, int njobs,
+                                                                    const zd* __restrict__ tab,
+                                                                    const double* __restrict__ P, int Pstride,
+                                                                    float2* __restrict__ lin) {
+    const long long rb = blockIdx.x;
+    int lo = 0, hi = njobs - 1;  // last job with rb0 <= rb
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (jobs[mid].rb0 <= rb) lo = mid;
+        else hi = mid - 1;
+    }
+    const LutBuildJob& j = jobs[lo];
+    lut_build_tex_entry(tab + j.tab_off, j.rows, j.L, P, Pstride, j.thetaR, j.sre, j.sim, lin + j.lin_off,
+                        j.lin_stride, (int)(rb - j.rb0) * 8 + (threadIdx.x >> 5), blockIdx.y * 32 + (threadIdx.x & 31));
 }
 
 // ---------------------------------------------------------------------------
@@ -1189,11 +1206,11 @@ void launch_us_lut_tex(const Scene& sc, const Sphere* sph, int s0, int s1, int a
                                                                                counters, chunk);
 }
 
-void launch_lut_build_tex(const zd* tab, int rows, int L, const double* P, int Pstride, int thetaR,
-                          cudaSurfaceObject_t sre, cudaSurfaceObject_t sim, float2* lin, int lin_stride,
-                          cudaStream_t st) {
-    dim3 grid(blocks_for(thetaR, 32), blocks_for(rows, 8));
-    lut_build_tex_kernel<<<grid, 256, 0, st>>>(tab, rows, L, P, Pstride, thetaR, sre, sim, lin, lin_stride);
+void launch_lut_build_tex_batch(const LutBuildJob* jobs, int njobs, long long total_rb, int max_theta, const zd* tab,
+                                const double* P, int Pstride, float2* lin, cudaStream_t st) {
+    if (njobs < 1 || total_rb < 1) return;
+    dim3 grid((unsigned)total_rb, blocks_for(max_theta, 32));
+    lut_build_tex_batch_kernel<<<grid, 256, 0, st>>>(jobs, njobs, tab, P, Pstride, lin);
 }
 
 void launch_sh_tables(const Scene& sc, const Sphere* sph, int L, const double* waves, double2* rec, double2* tab,
