@@ -495,7 +495,10 @@ def run_gb300(args):
         cpu = {"value": Rr * Rr / dt, "unit": "pixels/s", "cores": os.cpu_count() or 1, "kind": "port",
                "sample": f"double precision: scene set-up and the full lookup tables once, then {rows} of {Rr} "
                          f"near-field rows x 50 spheres x 1000 waves scaled by {Rr}/{rows} (extrapolated)",
-               "parts": parts}
+               "parts": parts,
+               # the reference's own host Bessel/Mie/table code, single-threaded as it runs it, measured
+               # where its checkout exists (oracle/time_reference_host.py), with the host named
+               "reference_host_special_functions": reference_host_timings()}
         nb = np.linalg.norm(band)
         vs_oracle = {"mixed": float(np.linalg.norm(mix_rows - band) / nb),
                      "fp64": None if f64_rows is None else float(np.linalg.norm(f64_rows - band) / nb),
