@@ -171,38 +171,14 @@ def run_served(args):
     on a fresh context as the reference runs one process per slice."""
     import numpy as np
 
-    from bimsim_gb300 import BS_IMG_INTENSITY, BS_PREC_FP64, BS_PREC_MIXED, Context, Server, scenes
+    from bimsim_gb300 import BS_IMG_INTENSITY, BS_PREC_FP64, BS_PREC_MIXED, Context, scenes
     trace = scenes.served_trace(args.serve_requests, seed=4, resolutions=(128, 256, 512, 1024, 2048),
                                 rate_hz=args.serve_rate)
-    lookups = sum(nf_pixels(p) * len(s) * len(w) for _, p, s, w in trace)
-    pixels = sum(nf_pixels(p) for _, p, _, _ in trace)
-    by_res = {}
-    with Server(workers=args.serve_workers) as srv:
-        t0 = time.perf_counter()
-        tickets = []
-        for t_arr, p, s, w in trace:
-            dt = t_arr - (time.perf_counter() - t0)
-            if dt > 0:
-                time.sleep(dt)
-            tickets.append((srv.submit(p, s, waves=w, precision=BS_PREC_MIXED), p.resolution))
-        gpu_ms = 0.0
-        for t, res in tickets:
-            srv.wait(t, 900.0)
-            _, info = srv.fetch(t)
-            gpu_ms += info.ms_gpu
-            by_res.setdefault(res, []).append(info.ms_total)
-        wall = time.perf_counter() - t0
-        st = srv.stats()
-    out = {"p50_ms": st.p50_ms, "p99_ms": st.p99_ms, "mean_ms": st.mean_ms, "max_ms": st.max_ms,
-           "p50_ms_by_resolution": {f"{r}^2": float(np.median(v)) for r, v in sorted(by_res.items())},
-           "requests": st.completed, "failed": st.failed, "lut_reuses": st.lut_reuses,
-           "workers": args.serve_workers, "arrival_rate_hz": args.serve_rate, "wall_s": wall,
-           "requests_per_s": st.completed / wall, "served_pixels_per_s": pixels / wall,
-           "served_lookups_per_s": lookups / wall, "lookups": lookups, "sum_gpu_ms": gpu_ms,
-           "peak_bytes": st.bytes_peak, "budget_bytes": st.hbm_budget,
-           "trace": f"{len(trace)} requests, Poisson arrivals at {args.serve_rate}/s; res in "
-                    "{128,256,512,1024,2048}^2, S ~ U{1..200}, lambda ~ U(2.5,12.5) um, nk in {200,1000,2000}, "
-                    "config-2 scene family, 25% repeat an earlier scene with new directions; mixed precision"}
+    out = serve_trace(trace, args.serve_workers, args.serve_rate)
+    if args.serve_light_requests > 0:
+        light = scenes.served_trace(args.serve_light_requests, seed=4, resolutions=(128, 256, 512, 1024, 2048),
+                                    rate_hz=args.serve_light_rate)
+        out["light_load"] = serve_trace(light, args.serve_workers, args.serve_light_rate)
     if args.no_fp64:
         return out
     # ---- the same requests: served mixed (closed loop) vs sequential plain FP64 ----
@@ -232,6 +208,43 @@ def run_served(args):
         "note": "measured: the requests of the trace of at most 1e11 lookups, in trace order up to 4e11 in all; "
                 "mixed through the server (all submitted at once), FP64 one fresh context per request in turn"}
     return out
+
+
+def serve_trace(trace, workers, rate):
+    """Submit `trace` (scenes.served_trace) at its arrival times to a server of `workers` contexts;
+    latencies are submit -> image ready."""
+    import numpy as np
+
+    from bimsim_gb300 import BS_PREC_MIXED, Server
+    lookups = sum(nf_pixels(p) * len(s) * len(w) for _, p, s, w in trace)
+    pixels = sum(nf_pixels(p) for _, p, _, _ in trace)
+    by_res = {}
+    with Server(workers=workers) as srv:
+        t0 = time.perf_counter()
+        tickets = []
+        for t_arr, p, s, w in trace:
+            dt = t_arr - (time.perf_counter() - t0)
+            if dt > 0:
+                time.sleep(dt)
+            tickets.append((srv.submit(p, s, waves=w, precision=BS_PREC_MIXED), p.resolution))
+        gpu_ms = 0.0
+        for t, res in tickets:
+            srv.wait(t, 900.0)
+            _, info = srv.fetch(t)
+            gpu_ms += info.ms_gpu
+            by_res.setdefault(res, []).append(info.ms_total)
+        wall = time.perf_counter() - t0
+        st = srv.stats()
+    return {"p50_ms": st.p50_ms, "p99_ms": st.p99_ms, "mean_ms": st.mean_ms, "max_ms": st.max_ms,
+            "p50_ms_by_resolution": {f"{r}^2": float(np.median(v)) for r, v in sorted(by_res.items())},
+            "requests": st.completed, "failed": st.failed, "lut_reuses": st.lut_reuses,
+            "workers": workers, "arrival_rate_hz": rate, "wall_s": wall,
+            "requests_per_s": st.completed / wall, "served_pixels_per_s": pixels / wall,
+            "served_lookups_per_s": lookups / wall, "lookups": lookups, "sum_gpu_ms": gpu_ms,
+            "peak_bytes": st.bytes_peak, "budget_bytes": st.hbm_budget,
+            "trace": f"{len(trace)} requests, Poisson arrivals at {rate}/s; res in "
+                     "{128,256,512,1024,2048}^2, S ~ U{1..200}, lambda ~ U(2.5,12.5) um, nk in {200,1000,2000}, "
+                     "config-2 scene family, 25% repeat an earlier scene with new directions; mixed precision"}
 
 
 def reference_host_timings():
@@ -678,7 +691,10 @@ def main():
                     help="profiling case: config-2 scene family at 256^2 over 25 um, 10 spheres, LUT 1024 x 1024")
     ap.add_argument("--serve-requests", type=int, default=32)
     ap.add_argument("--serve-rate", type=float, default=4.0)
-    ap.add_argument("--serve-workers", type=int, default=4)
+    ap.add_argument("--serve-workers", type=int, default=6)
+    ap.add_argument("--serve-light-requests", type=int, default=16,
+                    help="a second served run below saturation (0 skips it)")
+    ap.add_argument("--serve-light-rate", type=float, default=0.5)
     ap.add_argument("--workload", default="slice", choices=["slice", "sweep", "config1", "config5"])
     ap.add_argument("--c5-resolution", type=int, default=4096)
     ap.add_argument("--c5-samples", type=int, default=2000)

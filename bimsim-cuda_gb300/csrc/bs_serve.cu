@@ -11,12 +11,12 @@
 // first; a request passed by later ones 8 times starts next in any case.
 // Each context's stream gets a priority by the cost of its request, so that
 // the blocks of short requests are scheduled ahead of those of a long slice
-// already running, and with two or more workers the last one is a fast lane
-// that only takes short requests.  When the oldest request fits nowhere, idle workers give
-// their buffers back.  Contexts keep their tables between
-// requests (bs_set_lut_reuse) and a request goes preferably to the worker
-// that last ran the same scene.  Every kernel is deterministic, so a result
-// does not depend on what else runs.
+// already running, and with two or more workers the last third of them are
+// fast lanes that only take short requests.  When the oldest request fits
+// nowhere, idle workers give their buffers back.  Contexts keep their tables
+// between requests (bs_set_lut_reuse) and a request goes preferably to the
+// worker that last ran the same scene.  Every kernel is deterministic, so a
+// result does not depend on what else runs.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -48,9 +48,9 @@ double ms_between(Clock::time_point a, Clock::time_point b) {
 }
 
 constexpr int MAX_SKIPS = 8;  // a queued request is passed at most this often
-// With two or more workers the last one only takes requests of at most this
-// many (pixel, sphere, wave) interactions, so that a short request finds a
-// context even while long slices hold all the others.
+// With two or more workers the last third of them (at least one) only take
+// requests of at most this many (pixel, sphere, wave) interactions, so that
+// short requests find contexts even while long slices hold all the others.
 constexpr double FAST_LANE_COST = 1e11;
 
 bs_status set_error(bs_status st, const std::string& msg) {
@@ -175,7 +175,10 @@ struct bs_server {
     // Next request worker w may start (under mu), or nullptr: the cheapest
     // that it can start, so that short requests do not queue behind long
     // ones; a request passed MAX_SKIPS times by later ones is next in any case.
-    bool fast_lane(const Worker& w) const { return workers.size() >= 2 && w.index == (int)workers.size() - 1; }
+    bool fast_lane(const Worker& w) const {
+        const int n = (int)workers.size();
+        return n >= 2 && w.index >= n - std::max(1, n / 3);
+    }
 
     Request* pick(Worker& w) {
         const bool fast = fast_lane(w);
