@@ -51,21 +51,28 @@ bs_status fail(bs_status st, const char* fmt, ...) {
                         __LINE__);                                                                      \
     } while (0)
 
+// A context's device buffer.  Allocation and release are stream-ordered on
+// the owning context's stream (cudaMallocAsync / cudaFreeAsync): cudaFree
+// would wait for every stream of the device, so a context growing a buffer
+// would stall behind a long slice running on another context of the server.
 struct DevBuf {
     void* p = nullptr;
     size_t n = 0;
+    const cudaStream_t* st = nullptr;  // the owning context's stream (set by bs_create)
     cudaError_t ensure(size_t bytes) {
         if (bytes == 0) bytes = 256;
         if (bytes <= n) return cudaSuccess;
-        if (p) cudaFree(p);
-        p = nullptr;
-        n = 0;
-        cudaError_t e = cudaMalloc(&p, bytes);
+        release();
+        cudaError_t e = st ? cudaMallocAsync(&p, bytes, *st) : cudaMalloc(&p, bytes);
         if (e == cudaSuccess) n = bytes;
+        else p = nullptr;
         return e;
     }
     void release() {
-        if (p) cudaFree(p);
+        if (p) {
+            if (st) cudaFreeAsync(p, *st);
+            else cudaFree(p);
+        }
         p = nullptr;
         n = 0;
     }
@@ -124,6 +131,9 @@ struct TexSlot {
         tex[k] = surf[k] = 0;
         arr[k] = nullptr;
         cudaChannelFormatDesc fd = cudaCreateChannelDesc<float>();
+        // rows rounded up to a multiple of 256 (reads never pass the spare row): fewer
+        // reallocations, whose cudaFreeArray waits for the whole device
+        rows = (rows + 255) & ~255;
         cudaError_t e = cudaMallocArray(&arr[k], &fd, width, rows, cudaArraySurfaceLoadStore | cudaArrayTextureGather);
         if (e != cudaSuccess) return e;
         cudaResourceDesc rd = {};
@@ -240,6 +250,8 @@ bs_status bs_create(const bs_params* params, bs_ctx** out) {
     cudaError_t e = cudaGetDevice(&c->device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking);
     for (int i = 0; i < 6 && e == cudaSuccess; i++) e = cudaEventCreate(&c->ev[i]);
+    for (DevBuf* b : ctx_bufs(c)) b->st = &c->st;
+    c->d_texobj.st = &c->st;
     if (e != cudaSuccess) {
         delete c;
         return fail(BS_ERR_CUDA, "bs_create: %s", cudaGetErrorString(e));
@@ -252,6 +264,7 @@ bs_status bs_destroy(bs_ctx* c) {
     if (!c) return BS_OK;
     if (c->st) cudaStreamSynchronize(c->st);
     release_all(c);
+    if (c->st) cudaStreamSynchronize(c->st);  // the stream-ordered frees
     for (int i = 0; i < 6; i++)
         if (c->ev[i]) cudaEventDestroy(c->ev[i]);
     if (c->st) cudaStreamDestroy(c->st);
@@ -1028,7 +1041,6 @@ static bs_status run_nearfield(bs_ctx* c) {
                 // mixed path: the tables of every sphere of the batch in one launch
                 std::vector<LutBuildJob> jobs;
                 long long total_rb = 0;
-                int max_theta = 1;
                 for (int i = b.b0; i < b.b1 && !fp64; i++) {
                     const Sphere& S = c->hs[i];
                     const int L = S.Nl + 1;
@@ -1049,7 +1061,6 @@ static bs_status run_nearfield(bs_ctx* c) {
                         j.sre = sl.surf[2 * t];
                         j.sim = sl.surf[2 * t + 1];
                         total_rb += (j.rows + 7) / 8;
-                        max_theta = std::max(max_theta, S.thetaR);
                         jobs.push_back(j);
                     }
                 }
@@ -1057,7 +1068,7 @@ static bs_status run_nearfield(bs_ctx* c) {
                     CK(c->d_lbjobs.ensure(jobs.size() * sizeof(LutBuildJob)));
                     CK(cudaMemcpyAsync(c->d_lbjobs.p, jobs.data(), jobs.size() * sizeof(LutBuildJob),
                                        cudaMemcpyHostToDevice, c->st));
-                    launch_lut_build_tex_batch(c->d_lbjobs.as<LutBuildJob>(), (int)jobs.size(), total_rb, max_theta,
+                    launch_lut_build_tex_batch(c->d_lbjobs.as<LutBuildJob>(), (int)jobs.size(), total_rb,
                                                c->d_tab.as<zd>(), c->d_legP.as<double>(), c->legP_L,
                                                c->d_lut.as<float2>(), c->st);
                     LAUNCHED(c);
@@ -1164,7 +1175,8 @@ static size_t estimate_bytes(bs_ctx* c, bool fp64, size_t lut_budget) {
                         ha = std::max(ha, (size_t)hs[i].aR + 1);
                     }
                 }
-                b += 2 * thetaR * (hd + ha) * sizeof(float);
+                // the planes' rows are allocated in multiples of 256 (TexSlot::ensure)
+                b += 2 * thetaR * (((hd + 255) & ~(size_t)255) + ((ha + 255) & ~(size_t)255)) * sizeof(float);
             }
             b += B(4 * max_chunk * sizeof(unsigned long long)) + B((nk + 15) / 16 * sizeof(float4)) +
                  B(2 * sizeof(unsigned long long));

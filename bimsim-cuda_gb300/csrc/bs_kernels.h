@@ -77,8 +77,8 @@ struct LutBuildJob {
 // all) in one launch: the sums of launch_lut_build in double, stored as float in
 // the real and imaginary planes (CUDA arrays, through surfaces) and in the
 // linear rows used for staging
-void launch_lut_build_tex_batch(const LutBuildJob* jobs, int njobs, long long total_rb, int max_theta, const zd* tab,
-                                const double* P, int Pstride, float2* lin, cudaStream_t st);
+void launch_lut_build_tex_batch(const LutBuildJob* jobs, int njobs, long long total_rb, const zd* tab, const double* P,
+                                int Pstride, float2* lin, cudaStream_t st);
 
 // Direct scattered field through the addition theorem of spherical harmonics:
 // recurrence factors rec, per-wave tables tab (nk x L(L+1)/2), per-sphere
