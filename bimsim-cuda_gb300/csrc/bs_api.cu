@@ -178,7 +178,7 @@ struct bs_ctx {
     DevBuf d_cones, d_cnt;  // per-chunk wave cones; staged / total counters of the mixed LUT kernel
     DevBuf d_far;           // far fields Ud, Ufd on request (bs_get_far_field)
     DevBuf d_starts;        // row / coefficient offsets of a coefficient batch
-    DevBuf d_lbjobs;        // tables of a coefficient batch for the batched mixed LUT build
+    DevBuf d_lbjobs, d_lbjobs2;  // Usp and Uip tables of a coefficient batch for the mixed LUT build
     DevBuf d_fsave;         // U, Uf of a ring's first source (bs_simulate_ring_interp)
     DevBuf d_dacc;          // detector sum of bs_simulate_ring_detector
     DevBuf d_line, d_ringcs;  // radial lines and ring (cos, sin) of bs_simulate_ring_line
@@ -212,7 +212,7 @@ static std::vector<DevBuf*> ctx_bufs(bs_ctx* c) {
             &c->d_tabscr, &c->d_legP, &c->d_lut, &c->d_uft, &c->d_uftscr, &c->d_fields, &c->d_su,
             &c->d_sv, &c->d_mask, &c->d_wx, &c->d_wy, &c->d_wix, &c->d_wiy, &c->d_f1, &c->d_f2,
             &c->d_g1, &c->d_I, &c->d_D, &c->d_img, &c->d_cones, &c->d_cnt, &c->d_far,
-            &c->d_starts, &c->d_lbjobs, &c->d_fsave, &c->d_dacc, &c->d_line, &c->d_ringcs, &c->d_bp, &c->d_shrec, &c->d_shtab, &c->d_shcoef, &c->d_gscr, &c->d_ufw};
+            &c->d_starts, &c->d_lbjobs, &c->d_lbjobs2, &c->d_fsave, &c->d_dacc, &c->d_line, &c->d_ringcs, &c->d_bp, &c->d_shrec, &c->d_shtab, &c->d_shcoef, &c->d_gscr, &c->d_ufw};
 }
 
 static void release_all(bs_ctx* c) {
@@ -1038,40 +1038,45 @@ static bs_status run_nearfield(bs_ctx* c) {
                                        sc.kmag, c->d_A.as<zd>(), c->d_B.as<zd>(), c->d_tab.as<zd>(),
                                        c->d_tabscr.as<double>(), c->st);
                 LAUNCHED(c);
-                // mixed path: the tables of every sphere of the batch in one launch
-                std::vector<LutBuildJob> jobs;
-                long long total_rb = 0;
-                for (int i = b.b0; i < b.b1 && !fp64; i++) {
-                    const Sphere& S = c->hs[i];
-                    const int L = S.Nl + 1;
-                    const long long toff = b.starts[(size_t)(b.b1 - b.b0) + 1 + (i - b.b0)];
-                    TexSlot& sl = c->slots[i - s0];
-                    // one spare row repeats the last, so a gather at the last row clamps as the texture would
-                    const int rows[4] = {S.dR, S.dR, S.aR, S.aR};
-                    for (int k = 0; k < 4; k++) CK(sl.ensure(k, S.thetaR, rows[k] + 1));
-                    for (int t = 0; t < 2; t++) {
+                // mixed path: the tables of every sphere of the batch in two launches (the
+                // dR-row Usp tables, then the shorter Uip tables)
+                for (int t = 0; t < 2 && !fp64; t++) {
+                    std::vector<LutBuildJob> jobs;
+                    int max_rows = 0, max_theta = 1;
+                    for (int i = b.b0; i < b.b1; i++) {
+                        const Sphere& S = c->hs[i];
+                        const int L = S.Nl + 1;
+                        TexSlot& sl = c->slots[i - s0];
+                        if (t == 0) {
+                            // one spare row repeats the last, so a gather at the last row clamps as the texture would
+                            const int rows[4] = {S.dR, S.dR, S.aR, S.aR};
+                            for (int k = 0; k < 4; k++) CK(sl.ensure(k, S.thetaR, rows[k] + 1));
+                        }
                         LutBuildJob j{};
-                        j.tab_off = toff + (t ? (long long)S.dR * L : 0);
+                        j.tab_off = b.starts[(size_t)(b.b1 - b.b0) + 1 + (i - b.b0)] + (t ? (long long)S.dR * L : 0);
                         j.lin_off = t ? S.uip_off : S.usp_off;
-                        j.rb0 = total_rb;
                         j.rows = (t ? S.aR : S.dR) + 1;
                         j.L = L;
                         j.thetaR = S.thetaR;
                         j.lin_stride = S.lin_stride;
                         j.sre = sl.surf[2 * t];
                         j.sim = sl.surf[2 * t + 1];
-                        total_rb += (j.rows + 7) / 8;
+                        max_rows = std::max(max_rows, j.rows);
+                        max_theta = std::max(max_theta, S.thetaR);
                         jobs.push_back(j);
                     }
-                }
-                if (!jobs.empty()) {
-                    CK(c->d_lbjobs.ensure(jobs.size() * sizeof(LutBuildJob)));
-                    CK(cudaMemcpyAsync(c->d_lbjobs.p, jobs.data(), jobs.size() * sizeof(LutBuildJob),
-                                       cudaMemcpyHostToDevice, c->st));
-                    launch_lut_build_tex_batch(c->d_lbjobs.as<LutBuildJob>(), (int)jobs.size(), total_rb,
-                                               c->d_tab.as<zd>(), c->d_legP.as<double>(), c->legP_L,
-                                               c->d_lut.as<float2>(), c->st);
-                    LAUNCHED(c);
+                    if (jobs.empty()) continue;
+                    DevBuf& jb = t ? c->d_lbjobs2 : c->d_lbjobs;
+                    CK(jb.ensure(jobs.size() * sizeof(LutBuildJob)));
+                    CK(cudaMemcpyAsync(jb.p, jobs.data(), jobs.size() * sizeof(LutBuildJob), cudaMemcpyHostToDevice,
+                                       c->st));
+                    for (size_t j0 = 0; j0 < jobs.size(); j0 += 65535) {  // the grid's z extent
+                        launch_lut_build_tex_batch(jb.as<LutBuildJob>() + j0,
+                                                   (int)std::min<size_t>(65535, jobs.size() - j0), max_rows, max_theta,
+                                                   c->d_tab.as<zd>(), c->d_legP.as<double>(), c->legP_L,
+                                                   c->d_lut.as<float2>(), c->st);
+                        LAUNCHED(c);
+                    }
                 }
                 for (int i = b.b0; i < b.b1 && fp64; i++) {
                     const Sphere& S = c->hs[i];

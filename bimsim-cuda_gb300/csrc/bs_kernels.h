@@ -66,19 +66,18 @@ void launch_us_lut_tex(const Scene& sc, const Sphere* sph, int s0, int s1, int a
                        bool stage, int chunk, cudaStream_t st);
 // One table of the mixed path's table build: the rows (one spare) of one
 // sphere's Usp or Uip with their coefficient rows at tab + tab_off, written to
-// the planes sre/sim and the linear rows at lin + lin_off; rb0 is its first
-// block of 8 rows in the launch's flattened list.
+// the planes sre/sim and the linear rows at lin + lin_off.
 struct LutBuildJob {
-    long long tab_off, lin_off, rb0;
+    long long tab_off, lin_off;
     int rows, L, thetaR, lin_stride;
     cudaSurfaceObject_t sre, sim;
 };
-// every table of `jobs` (device array, njobs entries, total_rb blocks of 8 rows in
-// all) in one launch: the sums of launch_lut_build in double, stored as float in
-// the real and imaginary planes (CUDA arrays, through surfaces) and in the
-// linear rows used for staging
-void launch_lut_build_tex_batch(const LutBuildJob* jobs, int njobs, long long total_rb, const zd* tab, const double* P,
-                                int Pstride, float2* lin, cudaStream_t st);
+// the tables of `jobs` (device array of njobs <= 65535 entries, at most max_rows
+// rows and max_theta angles each) in one launch: the sums of launch_lut_build in
+// double, stored as float in the real and imaginary planes (CUDA arrays, through
+// surfaces) and in the linear rows used for staging
+void launch_lut_build_tex_batch(const LutBuildJob* jobs, int njobs, int max_rows, int max_theta, const zd* tab,
+                                const double* P, int Pstride, float2* lin, cudaStream_t st);
 
 // Direct scattered field through the addition theorem of spherical harmonics:
 // recurrence factors rec, per-wave tables tab (nk x L(L+1)/2), per-sphere

@@ -872,32 +872,18 @@ __device__ __forceinline__ void lut_build_tex_entry(const zd* __restrict__ tab, 
     }
 }
 
-// Every table of a sphere batch in one launch.  Block b computes the b-th
-// block of 8 rows in the flattened row blocks of all tables (the table found
-// once per block by binary search on rb0): warp w takes row 8 (b - rb0) + w
-// and its lanes step through the angles, so a row's coefficients are loaded
-// once per warp and the Legendre table rows stay in L1/L2.
-__global__ void __launch_bounds__(256) lut_build_tex_batch_kernel(const LutBuildJob* __restrict__ jobs, int njobs,
+// Tables of a sphere batch in one launch: blockIdx.z picks the table,
+// blockIdx.y its block of 8 rows (blocks past the table's rows return) and
+// blockIdx.x a block of 32 angles, as the one-table grid would.
+__global__ void __launch_bounds__(256) lut_build_tex_batch_kernel(const LutBuildJob* __restrict__ jobs,
                                                                     const zd* __restrict__ tab,
                                                                     const double* __restrict__ P, int Pstride,
                                                                     float2* __restrict__ lin) {
-    __shared__ int s_job;
-    const long long rb = blockIdx.x;
-    if (threadIdx.x == 0) {
-        int lo = 0, hi = njobs - 1;  // last job with rb0 <= rb
-        while (lo < hi) {
-            const int mid = (lo + hi + 1) >> 1;
-            if (jobs[mid].rb0 <= rb) lo = mid;
-            else hi = mid - 1;
-        }
-        s_job = lo;
-    }
-    __syncthreads();
-    const LutBuildJob& j = jobs[s_job];
-    const int r = (int)(rb - j.rb0) * 8 + (threadIdx.x >> 5);
-    for (int t = threadIdx.x & 31; t < j.thetaR; t += 32)
-        lut_build_tex_entry(tab + j.tab_off, j.rows, j.L, P, Pstride, j.thetaR, j.sre, j.sim, lin + j.lin_off,
-                            j.lin_stride, r, t);
+    const LutBuildJob& j = jobs[blockIdx.z];
+    const int r = blockIdx.y * 8 + (threadIdx.x >> 5);
+    if (r >= j.rows) return;
+    lut_build_tex_entry(tab + j.tab_off, j.rows, j.L, P, Pstride, j.thetaR, j.sre, j.sim, lin + j.lin_off,
+                        j.lin_stride, r, blockIdx.x * 32 + (threadIdx.x & 31));
 }
 
 // ---------------------------------------------------------------------------
@@ -1215,10 +1201,11 @@ void launch_us_lut_tex(const Scene& sc, const Sphere* sph, int s0, int s1, int a
                                                                                counters, chunk);
 }
 
-void launch_lut_build_tex_batch(const LutBuildJob* jobs, int njobs, long long total_rb, const zd* tab, const double* P,
-                                int Pstride, float2* lin, cudaStream_t st) {
-    if (njobs < 1 || total_rb < 1) return;
-    lut_build_tex_batch_kernel<<<(unsigned)total_rb, 256, 0, st>>>(jobs, njobs, tab, P, Pstride, lin);
+void launch_lut_build_tex_batch(const LutBuildJob* jobs, int njobs, int max_rows, int max_theta, const zd* tab,
+                                const double* P, int Pstride, float2* lin, cudaStream_t st) {
+    if (njobs < 1 || max_rows < 1) return;
+    dim3 grid(blocks_for(max_theta, 32), blocks_for(max_rows, 8), (unsigned)njobs);
+    lut_build_tex_batch_kernel<<<grid, 256, 0, st>>>(jobs, tab, P, Pstride, lin);
 }
 
 void launch_sh_tables(const Scene& sc, const Sphere* sph, int L, const double* waves, double2* rec, double2* tab,
