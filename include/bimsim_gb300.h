@@ -212,7 +212,8 @@ bs_status bs_get_lut(bs_ctx* ctx, int32_t sphere, int32_t which, double* host, s
 
 /* Measured FMA throughput (TFLOP/s, 2 flop per FMA) of the current GPU in
  * single and double precision, from bounded FMA-chain kernels timed with
- * CUDA events.  The denominator of the scattered-field kernels' roofline.
+ * CUDA events (single precision: the larger of scalar FMAs and packed
+ * fma.rn.f32x2 pairs).  The denominator of the scattered-field kernels' roofline.
  * No reference counterpart. */
 bs_status bs_measure_fma_peak(double* fp32_tflops, double* fp64_tflops);
 
