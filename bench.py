@@ -171,7 +171,7 @@ def run_served(args):
     on a fresh context as the reference runs one process per slice."""
     import numpy as np
 
-    from bimsim_gb300 import BS_IMG_INTENSITY, BS_PREC_FP64, BS_PREC_MIXED, Context, scenes
+    from bimsim_gb300 import BS_IMG_INTENSITY, BS_PREC_FP64, BS_PREC_MIXED, Context, Server, scenes
     trace = scenes.served_trace(args.serve_requests, seed=4, resolutions=(128, 256, 512, 1024, 2048),
                                 rate_hz=args.serve_rate)
     out = serve_trace(trace, args.serve_workers, args.serve_rate)
