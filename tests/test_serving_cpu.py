@@ -151,3 +151,45 @@ def test_wait_times_out_and_bad_tickets():
 def test_dry_run_needs_a_budget():
     with pytest.raises(BimsimError):
         Server(workers=1, hbm_budget=0, dry_run=True)
+
+
+def test_fast_lane_takes_only_short_requests():
+    """With 3 workers the last is a fast lane: requests above 1e11 (pixel, sphere, wave)
+    interactions never run on it (short ones may run on any worker)."""
+    big_p, big_s, _ = scene(res=256, ns=40)        # (768^2 px) x 40 spheres x 5000 waves = 1.2e11
+    big_w = scenes.mc_waves(5000, 0.0, 0.5, seed=5)
+    small_p, small_s, small_w = scene(res=32, ns=1, nk=16)
+    budget = 50 * estimate_bytes(big_p, big_s, len(big_w))
+    runs = []
+    with Server(workers=3, hbm_budget=budget, dry_run=True) as srv:
+        for i in range(12):
+            big = i % 2 == 0
+            p, s, w = (big_p, big_s, big_w) if big else (small_p, small_s, small_w)
+            runs.append((srv.submit(p, s, waves=w), big))
+        for t, _ in runs:
+            srv.wait(t, 20.0)
+        workers = {t: srv.fetch(t)[1].worker for t, _ in runs}
+    assert len(workers) == 12
+    assert all(workers[t] != 2 for t, big in runs if big)
+
+
+def test_cheapest_queued_request_starts_first():
+    """One worker, held by the first request; of the requests queued behind it the cheaper start
+    first, whatever their arrival order (each passes the older, dearer ones at most 8 times)."""
+    sizes = [(128, 8), (128, 8), (16, 1), (128, 8), (16, 1), (16, 1)]
+    reqs = [scene(res=r, ns=n, nk=32) for r, n in sizes]
+    budget = 10 * max(estimate_bytes(p, s, len(w)) for p, s, w in reqs)
+    with Server(workers=1, hbm_budget=budget, dry_run=True) as srv:
+        sub = []
+        for p, s, w in reqs:
+            sub.append((srv.submit(p, s, waves=w), time.perf_counter()))
+        start = {}
+        for t, t_sub in sub:
+            srv.wait(t, 20.0)
+            start[t] = t_sub + srv.fetch(t)[1].ms_queued * 1e-3
+    order = sorted(range(len(sub)), key=lambda i: start[sub[i][0]])
+    # after whichever request started first, the three small ones precede the remaining large ones
+    rest = [i for i in order if i != order[0]]
+    small = [i for i in rest if sizes[i][0] == 16]
+    large = [i for i in rest if sizes[i][0] == 128]
+    assert max(rest.index(i) for i in small) < min(rest.index(i) for i in large), order
