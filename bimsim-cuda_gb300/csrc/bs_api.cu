@@ -179,6 +179,7 @@ struct bs_ctx {
     DevBuf d_far;           // far fields Ud, Ufd on request (bs_get_far_field)
     DevBuf d_starts;        // row / coefficient offsets of a coefficient batch
     DevBuf d_lbjobs, d_lbjobs2;  // Usp and Uip tables of a coefficient batch for the mixed LUT build
+    DevBuf d_kcmp;               // Kahan compensation of the mixed LUT sums between sphere chunks
     DevBuf d_fsave;         // U, Uf of a ring's first source (bs_simulate_ring_interp)
     DevBuf d_dacc;          // detector sum of bs_simulate_ring_detector
     DevBuf d_line, d_ringcs;  // radial lines and ring (cos, sin) of bs_simulate_ring_line
@@ -212,7 +213,7 @@ static std::vector<DevBuf*> ctx_bufs(bs_ctx* c) {
             &c->d_tabscr, &c->d_legP, &c->d_lut, &c->d_uft, &c->d_uftscr, &c->d_fields, &c->d_su,
             &c->d_sv, &c->d_mask, &c->d_wx, &c->d_wy, &c->d_wix, &c->d_wiy, &c->d_f1, &c->d_f2,
             &c->d_g1, &c->d_I, &c->d_D, &c->d_img, &c->d_cones, &c->d_cnt, &c->d_far,
-            &c->d_starts, &c->d_lbjobs, &c->d_lbjobs2, &c->d_fsave, &c->d_dacc, &c->d_line, &c->d_ringcs, &c->d_bp, &c->d_shrec, &c->d_shtab, &c->d_shcoef, &c->d_gscr, &c->d_ufw};
+            &c->d_starts, &c->d_lbjobs, &c->d_lbjobs2, &c->d_kcmp, &c->d_fsave, &c->d_dacc, &c->d_line, &c->d_ringcs, &c->d_bp, &c->d_shrec, &c->d_shtab, &c->d_shcoef, &c->d_gscr, &c->d_ufw};
 }
 
 static void release_all(bs_ctx* c) {
@@ -983,6 +984,7 @@ static bs_status run_nearfield(bs_ctx* c) {
             }
         }
         const int nchunks = (int)chunk_start.size() - 1;
+        if (!fp64 && nchunks > 1) CK(c->d_kcmp.ensure((size_t)R * R * sizeof(float2)));
         bool use_stage = false;
         int max_chunk = 0;
         for (int ci = 0; ci < nchunks; ci++) max_chunk = std::max(max_chunk, chunk_start[ci + 1] - chunk_start[ci]);
@@ -1109,8 +1111,8 @@ static bs_status run_nearfield(bs_ctx* c) {
                 launch_us_lut_tex(sc, c->d_sph.as<Sphere>(), s0, s1, ci > 0, finalize, c->d_kw4.as<float4>(),
                                   c->d_cones.as<float4>(), c->d_ph.as<cpx<float>>(),
                                   c->d_texobj.as<unsigned long long>(), c->d_lut.as<float2>(), (const cpx<float>*)Uf,
-                                  (cpx<float>*)U, ns > 0 ? c->d_cnt.as<unsigned long long>() : nullptr, use_stage,
-                                  chunk, c->st);
+                                  (cpx<float>*)U, ns > 0 ? c->d_cnt.as<unsigned long long>() : nullptr,
+                                  nchunks > 1 ? c->d_kcmp.as<float2>() : nullptr, use_stage, chunk, c->st);
             }
             LAUNCHED(c);
             // the handle list and the table slots are reused by the next chunk
@@ -1168,6 +1170,7 @@ static size_t estimate_bytes(bs_ctx* c, bool fp64, size_t lut_budget) {
              B((size_t)maxstarts * sizeof(long long));
         b += B(thetaR * (size_t)c->Lmax * sizeof(double));    // Legendre table
         if (!fp64) {
+            if (cs.size() > 2) b += B(R * R * sizeof(float2));  // Kahan carry between chunks
             // slot k holds the k-th sphere of every chunk: the largest of those tables, plus a spare row each
             size_t max_chunk = 0;
             for (size_t ci = 0; ci + 1 < cs.size(); ci++) max_chunk = std::max(max_chunk, (size_t)(cs[ci + 1] - cs[ci]));

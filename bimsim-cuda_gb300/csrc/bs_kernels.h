@@ -59,11 +59,14 @@ void launch_us_lut_f64(const Scene& sc, const Sphere* sph, int s0, int s1, int a
 // of Sphere::lin_stride entries);
 // cones: one {axis, half-angle} per `chunk` waves; counters[0..1] receive
 // the staged and total (sphere, chunk) counts of every block (may be null);
+// kcmp (R x R, or null with a single sphere chunk) carries each pixel's Kahan
+// compensation from one sphere chunk's launch to the next, so that chunked
+// tables give the bits of one launch over all spheres;
 // stage = false runs the texture-only variant
 void launch_us_lut_tex(const Scene& sc, const Sphere* sph, int s0, int s1, int accumulate, int finalize,
                        const float4* kw4, const float4* cones, const cpx<float>* ph, const unsigned long long* tex,
                        const float2* lin, const cpx<float>* Uf, cpx<float>* U, unsigned long long* counters,
-                       bool stage, int chunk, cudaStream_t st);
+                       float2* kcmp, bool stage, int chunk, cudaStream_t st);
 // One table of the mixed path's table build: the rows (one spare) of one
 // sphere's Usp or Uip with their coefficient rows at tab + tab_off, written to
 // the planes sre/sim and the linear rows at lin + lin_off.

@@ -546,7 +546,7 @@ __global__ void __launch_bounds__(UST_TILE / PPT, STAGE ? 4 : 6) us_lut_tex_kern
                                                                     const cpx<float>* __restrict__ Uf,
                                                                     cpx<float>* __restrict__ U,
                                                                     unsigned long long* __restrict__ counters,
-                                                                    int chunk) {
+                                                                    float2* __restrict__ kcmp, int chunk) {
     constexpr int NT = UST_TILE / PPT, NWARP = NT / 32;
     static_assert(NT >= UST_CHUNK && NT % 32 == 0, "one thread per wave of a chunk");
     extern __shared__ float2 s_stage[];
@@ -591,6 +591,10 @@ __global__ void __launch_bounds__(UST_TILE / PPT, STAGE ? 4 : 6) us_lut_tex_kern
         if (accumulate && valid[j]) {
             tot_r[j] = U[iv[j] * sc.R + iu[j]].re;
             tot_i[j] = U[iv[j] * sc.R + iu[j]].im;
+            if (kcmp) {  // the Kahan compensation the previous sphere chunk left: the sum goes on as in one launch
+                cmp_r[j] = kcmp[iv[j] * sc.R + iu[j]].x;
+                cmp_i[j] = kcmp[iv[j] * sc.R + iu[j]].y;
+            }
         }
     }
     const int nchunks = (sc.nk + chunk - 1) / chunk;
@@ -845,6 +849,8 @@ __global__ void __launch_bounds__(UST_TILE / PPT, STAGE ? 4 : 6) us_lut_tex_kern
                 tot_r[j] += Uf[idx].re - cmp_r[j];
                 tot_i[j] += Uf[idx].im - cmp_i[j];
             }
+        } else if (kcmp) {
+            kcmp[idx] = make_float2(cmp_r[j], cmp_i[j]);
         }
         U[idx] = mk(tot_r[j], tot_i[j]);
     }
@@ -1183,12 +1189,12 @@ void launch_us_lut_f64(const Scene& sc, const Sphere* sph, int s0, int s1, int a
 void launch_us_lut_tex(const Scene& sc, const Sphere* sph, int s0, int s1, int accumulate, int finalize,
                        const float4* kw4, const float4* cones, const cpx<float>* ph, const unsigned long long* tex,
                        const float2* lin, const cpx<float>* Uf, cpx<float>* U, unsigned long long* counters,
-                       bool stage, int chunk, cudaStream_t st) {
+                       float2* kcmp, bool stage, int chunk, cudaStream_t st) {
     int tiles = (sc.R + 15) / 16;
     if (!stage) {
         us_lut_tex_kernel<false, 1><<<(unsigned)tiles * tiles, UST_TILE, 0, st>>>(sc, sph, s0, s1, accumulate, finalize,
                                                                                  kw4, cones, ph, tex, lin, Uf, U,
-                                                                                 counters, chunk);
+                                                                                 counters, kcmp, chunk);
         return;
     }
     const int smem = UST_STAGE * (int)sizeof(float2);
@@ -1198,7 +1204,7 @@ void launch_us_lut_tex(const Scene& sc, const Sphere* sph, int s0, int s1, int a
     cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     kernel<<<(unsigned)tiles * tiles, two ? UST_TILE / 2 : UST_TILE, smem, st>>>(sc, sph, s0, s1, accumulate, finalize,
                                                                                kw4, cones, ph, tex, lin, Uf, U,
-                                                                               counters, chunk);
+                                                                               counters, kcmp, chunk);
 }
 
 void launch_lut_build_tex_batch(const LutBuildJob* jobs, int njobs, int max_rows, int max_theta, const zd* tab,
