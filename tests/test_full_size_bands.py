@@ -14,6 +14,8 @@ thread, table budget), and the band of its near field U is compared.
 
 Tolerances (relative L2 over the band): FP64 1e-10, mixed 1e-4 (near field).
 """
+import os
+
 import numpy as np
 import pytest
 
@@ -105,3 +107,21 @@ def test_config5_reduced_band_matches_oracle():
     print("config 5 (512^2) band errors", {"fp64_250_waves": e64, "mixed": e_mixed, "max_order": nl})
     assert e64 <= TOL64
     assert e_mixed <= TOL_MIXED_FIELD
+
+
+@pytest.mark.skipif(os.environ.get("BIMSIM_LONG_TESTS") != "1",
+                    reason="about 13 minutes (a 7-minute slice and 5 minutes of oracle); set BIMSIM_LONG_TESTS=1")
+def test_config5_full_size_band_matches_oracle():
+    """Config 5 at its full size: 4096^2 over 400 um (near field 12288^2), 1000 spheres a ~ U(2, 20) um,
+    2000 waves, LUT 4096 x 1024, mixed: rows [R/2 - 2, R/2 + 2) against the oracle."""
+    if host_memory_available_gb() < 128:
+        pytest.skip("needs 128 GB of free host memory for the oracle's tables of 1000 spheres")
+    p, s, w = scenes.config5()
+    R = oracle_lib.geom(p).R
+    assert R == 12288
+    r0, r1 = R // 2 - 2, R // 2 + 2
+    mixed, st = gpu_band(p, s, w, BS_PREC_MIXED, r0, r1)
+    e = rel(mixed, oracle_band(p, s, w, r0, r1))
+    print("config 5 full-size band", {"mixed": e, "ms_us": st.ms_us, "wave_chunk": st.lut_wave_chunk,
+                                       "staged": st.lut_chunks_staged / max(1, st.lut_chunks_total)})
+    assert e <= TOL_MIXED_FIELD
