@@ -8,14 +8,18 @@
 // evaluated once; then blocks (z, y, x) and their threads (z, y, x) run one
 // after another on the calling host thread, each a plain call of the kernel
 // body with threadIdx/blockIdx set, so an early `return` ends that thread only.
-// Kernels that synchronise threads through shared memory are not run this way
-// (the checks call none of them; __syncthreads is a no-op here).
+// A launch with dynamic shared memory (the reference's only kernels that
+// synchronise threads: the ring reductions of microscope.cu) runs each block's
+// threads as coroutines instead (ref_runtime.cpp): __syncthreads() suspends the
+// calling thread until every thread of the block that has not returned reaches
+// it.  Elsewhere __syncthreads() does nothing.
 #ifndef BS_REF_PRELUDE_H
 #define BS_REF_PRELUDE_H
 
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <functional>
 #include <utility>
 
 #include "cuda_runtime.h"
@@ -29,7 +33,8 @@
 #define __launch_bounds__(...)
 #define HANDLE_ERROR(e) (e)
 
-inline void __syncthreads() {}
+void bs_ref_syncthreads();
+inline void __syncthreads() { bs_ref_syncthreads(); }
 
 // CUDA's max/min overloads of the device math library, as plain functions so
 // that mixed argument types promote as they do in device code.
@@ -47,14 +52,29 @@ inline double min(float a, double b) { return std::fmin((double)a, b); }
 inline double min(double a, float b) { return std::fmin(a, (double)b); }
 
 namespace bs_ref {
+// runs body() once per thread of a block of `block` threads, as coroutines that
+// __syncthreads() switches between (ref_runtime.cpp)
+void coop_block(const dim3& block, const std::function<void()>& body);
+
 template <class F>
 struct Launch {
     F f;
     dim3 grid, block;
+    size_t shmem;
     template <class... A>
     void operator()(A&&... a) {
         ::gridDim = grid;
         ::blockDim = block;
+        if (shmem > 0) {
+            const std::function<void()> body = [&]() { f(a...); };
+            for (unsigned bz = 0; bz < grid.z; bz++)
+                for (unsigned by = 0; by < grid.y; by++)
+                    for (unsigned bx = 0; bx < grid.x; bx++) {
+                        ::blockIdx = uint3{bx, by, bz};
+                        coop_block(block, body);
+                    }
+            return;
+        }
         for (unsigned bz = 0; bz < grid.z; bz++)
             for (unsigned by = 0; by < grid.y; by++)
                 for (unsigned bx = 0; bx < grid.x; bx++)
@@ -68,8 +88,8 @@ struct Launch {
     }
 };
 template <class F>
-Launch<F> launch_of(F f, dim3 g, dim3 b, size_t = 0, void* = nullptr) {
-    return Launch<F>{f, g, b};
+Launch<F> launch_of(F f, dim3 g, dim3 b, size_t shmem = 0, void* = nullptr) {
+    return Launch<F>{f, g, b, shmem};
 }
 }  // namespace bs_ref
 

@@ -1,10 +1,14 @@
 // ref_runtime.cpp -- TEST INFRASTRUCTURE: definitions behind cuda_runtime.h,
 // cufft.h and prelude.h of this directory (the host-run build of the
 // reference; see cuda_runtime.h).  Nothing here is product code.
+#include <ucontext.h>
+
 #include <chrono>
 #include <cmath>
 #include <complex>
+#include <functional>
 #include <map>
+#include <memory>
 #include <vector>
 
 #include "cufft.h"
@@ -16,8 +20,65 @@ thread_local dim3 blockDim;
 thread_local dim3 gridDim;
 
 // `extern __shared__ float shared[]` of the reference's ring kernels
-// (microscope.cu:142,200) resolves here; the checks never run those kernels.
+// (microscope.cu:142,200) resolves here; their blocks run one after another,
+// so one array serves as every block's shared memory.
 float shared[1 << 16];
+
+// ---- cooperative blocks ----------------------------------------------------
+// The threads of one block as coroutines on the calling host thread.  Each
+// round resumes, in thread order, every thread that has not returned; a thread
+// runs until it returns or calls __syncthreads().  Threads that returned no
+// longer take part in the barrier, as on the GPU.
+namespace {
+thread_local bool g_coop = false;
+thread_local ucontext_t g_sched;
+thread_local std::vector<ucontext_t>* g_ctx = nullptr;
+thread_local std::vector<char>* g_done = nullptr;
+thread_local const std::function<void()>* g_body = nullptr;
+thread_local int g_cur = 0;
+
+void coop_trampoline() {
+    (*g_body)();
+    (*g_done)[g_cur] = 1;  // returns to uc_link, the scheduler
+}
+}  // namespace
+
+void bs_ref_syncthreads() {
+    if (g_coop) swapcontext(&(*g_ctx)[g_cur], &g_sched);
+}
+
+namespace bs_ref {
+void coop_block(const dim3& block, const std::function<void()>& body) {
+    const int n = (int)(block.x * block.y * block.z);
+    const size_t stack = 1 << 16;
+    std::vector<ucontext_t> ctx(n);
+    std::unique_ptr<char[]> stacks(new char[(size_t)n * stack]);
+    std::vector<char> done(n, 0);
+    g_ctx = &ctx;
+    g_done = &done;
+    g_body = &body;
+    for (int i = 0; i < n; i++) {
+        getcontext(&ctx[i]);
+        ctx[i].uc_stack.ss_sp = stacks.get() + (size_t)i * stack;
+        ctx[i].uc_stack.ss_size = stack;
+        ctx[i].uc_link = &g_sched;
+        makecontext(&ctx[i], coop_trampoline, 0);
+    }
+    g_coop = true;
+    for (bool pending = true; pending;) {
+        pending = false;
+        for (int i = 0; i < n; i++) {
+            if (done[i]) continue;
+            g_cur = i;
+            ::threadIdx = uint3{(unsigned)i % block.x, ((unsigned)i / block.x) % block.y,
+                                (unsigned)i / (block.x * block.y)};
+            swapcontext(&g_sched, &ctx[i]);
+            if (!done[i]) pending = true;
+        }
+    }
+    g_coop = false;
+}
+}  // namespace bs_ref
 
 const char* cudaGetErrorString(cudaError_t e) { return e == cudaSuccess ? "no error" : "host-run CUDA stand-in error"; }
 cudaError_t cudaSetDevice(int) { return cudaSuccess; }

@@ -8,6 +8,11 @@
 //     nearfieldStruct::Simulate, step by step         (nearfield.cpp:194-218)
 //     microscopeStruct::SimulateImaging              (microscope.cu:840)
 //     getIntensity / getIncidentFieldImage / getAbsorbance (microscope.cu:722-814)
+// or, with stop = 2 and the reference's --interpolate 1, 2 or 3, the ring-source
+// driver that its Save dispatches to for that mode (fileout.cu:219-243):
+//     SimulateExtendedSourceInterpAtDetector         (microscope.cu:1004-1093)
+//     SimulateExtendedSourceInterpLineAtDetector     (microscope.cu:1097-1183)
+//     SimulateExtendedSourceWithInterpolation        (microscope.cu:1189-1253)
 // and keeps its Monte Carlo directions, Mie coefficients, per-sphere tables,
 // near fields and detector images for the accessors below.  Simulate is taken
 // step by step only so that the tables can be read after calcSpheres; the
@@ -54,12 +59,80 @@ void put_real(const std::string& key, const T* p, size_t n) {
     std::vector<double>& v = g_out[key];
     v.assign(p, p + n);
 }
+
+// the inputs as the reference holds them after parsing (single-precision flag values)
+void put_scene() {
+    const nearfieldStruct& nf = SCOPE->nf;
+    g_out["scene"] = {(double)nf.lambda, (double)nf.A, (double)nf.k[0], (double)nf.k[1], (double)nf.k[2],
+                      (double)nf.focus[0], (double)nf.focus[1], (double)nf.focus[2], (double)nf.condenser[0],
+                      (double)nf.condenser[1], (double)SCOPE->objective[0], (double)SCOPE->objective[1],
+                      (double)SCOPE->padding, (double)SCOPE->ss, (double)nf.m, (double)nf.lut_us,
+                      (double)nf.lut_uf, (double)nf.planeWave, (double)nf.nWaves};
+    g_out["nf_quad"] = {(double)nf.pos.A[0], (double)nf.pos.A[1], (double)nf.pos.A[2], (double)nf.pos.X[0],
+                        (double)nf.pos.X[1], (double)nf.pos.X[2], (double)nf.pos.Y[0], (double)nf.pos.Y[1],
+                        (double)nf.pos.Y[2]};
+}
+
+// Monte Carlo directions, sizes, per-sphere inputs and Mie coefficients after
+// calcWaves / calcSpheres
+void put_waves_and_spheres() {
+    const nearfieldStruct& nf = SCOPE->nf;
+    std::vector<double> w;
+    for (const bsVector& k : nf.inWaves)
+        for (int c = 0; c < 3; c++) w.push_back((double)k[c]);
+    g_out["waves"] = w;
+    g_out["dims"] = {(double)nf.U.R[0], (double)nf.U.R[1], (double)SCOPE->Ud.R[0] / SCOPE->ss,
+                     (double)SCOPE->ss, (double)nf.sVector.size(), (double)nf.inWaves.size()};
+    for (size_t s = 0; s < nf.sVector.size(); s++) {
+        const sphere& S = nf.sVector[s];
+        const std::string p = "sphere" + std::to_string(s) + ".";
+        // d_min and d_max are set only when the tables are built (the direct mode leaves them unset)
+        const double dmin = nf.lut_us ? (double)S.d_min : 0.0, dmax = nf.lut_us ? (double)S.d_max : 0.0;
+        g_out[p + "geom"] = {(double)S.Nl, dmin, dmax, (double)S.Usp.R[0], (double)S.Usp.R[1], (double)S.Uip.R[0],
+                             (double)S.Uip.R[1]};
+        g_out[p + "in"] = {(double)S.p[0], (double)S.p[1], (double)S.p[2], (double)S.a, (double)S.n.real(),
+                           (double)S.n.imag()};
+        put_complex(p + "A", S.A.data(), S.A.size());
+        put_complex(p + "B", S.B.data(), S.B.size());
+    }
+}
+
+void put_detector() {
+    scalarslice I = SCOPE->getIntensity();
+    scalarslice Ii = SCOPE->getIncidentFieldImage();
+    scalarslice Ab = SCOPE->getAbsorbance();
+    const size_t nd = (size_t)I.R[0] * I.R[1];
+    put_real("D", I.S, nd);
+    put_real("Di", Ii.S, nd);
+    put_real("Absorbance", Ab.S, nd);
+}
+
+// The ring-source driver for SCOPE->interpolate, called as fileout.cu:219-243
+// calls it, then the detector images it leaves.
+int run_rings() {
+    put_scene();  // before the drivers move the focus and amplitude
+    microscopeStruct* scope = SCOPE;
+    if (scope->interpolate == 1)
+        scope->SimulateExtendedSourceInterpAtDetector(scope->nf.extSource);
+    else if (scope->interpolate == 2)
+        scope->SimulateExtendedSourceInterpLineAtDetector(scope->nf.extSource);
+    else if (scope->interpolate == 3)
+        scope->SimulateExtendedSourceWithInterpolation(0, scope->nf.extSource);
+    else
+        return 2;
+    put_waves_and_spheres();
+    put_detector();
+    g_out["rings"] = {(double)scope->interpolate, (double)scope->nf.extSource[0], (double)scope->nf.extSource[1]};
+    return 0;
+}
 }  // namespace
 
 extern "C" {
 
 // Run the reference on `argv` (argv[0] is the program name).  stop = 1 ends
-// after calcSpheres (tables only); 0 runs the whole single-source path.
+// after calcSpheres (tables only); 0 runs the whole single-source path; 2 runs
+// the ring-source driver of the parsed --interpolate mode (1, 2 or 3) and keeps
+// the detector images.
 int ref_sim_run(int argc, const char** argv, int stop) {
     g_out.clear();
     std::vector<std::string> keep(argv, argv + argc);
@@ -72,6 +145,7 @@ int ref_sim_run(int argc, const char** argv, int stop) {
     LoadParameters(args);
     SCOPE->init();
     nearfieldStruct& nf = SCOPE->nf;
+    if (stop == 2) return run_rings();
 
     nf.t_Uf = 0;
     nf.t_Us = 0;
@@ -79,30 +153,11 @@ int ref_sim_run(int argc, const char** argv, int stop) {
     nf.calcUf();
     nf.calcSpheres();
 
-    std::vector<double> w;
-    for (const bsVector& k : nf.inWaves)
-        for (int c = 0; c < 3; c++) w.push_back((double)k[c]);
-    g_out["waves"] = w;
-    g_out["dims"] = {(double)nf.U.R[0], (double)nf.U.R[1], (double)SCOPE->Ud.R[0] / SCOPE->ss,
-                     (double)SCOPE->ss, (double)nf.sVector.size(), (double)nf.inWaves.size()};
-    // the inputs as the reference holds them after parsing (single-precision flag values)
-    g_out["scene"] = {(double)nf.lambda, (double)nf.A, (double)nf.k[0], (double)nf.k[1], (double)nf.k[2],
-                      (double)nf.focus[0], (double)nf.focus[1], (double)nf.focus[2], (double)nf.condenser[0],
-                      (double)nf.condenser[1], (double)SCOPE->objective[0], (double)SCOPE->objective[1],
-                      (double)SCOPE->padding, (double)SCOPE->ss, (double)nf.m, (double)nf.lut_us,
-                      (double)nf.lut_uf, (double)nf.planeWave, (double)nf.nWaves};
-    g_out["nf_quad"] = {(double)nf.pos.A[0], (double)nf.pos.A[1], (double)nf.pos.A[2], (double)nf.pos.X[0],
-                        (double)nf.pos.X[1], (double)nf.pos.X[2], (double)nf.pos.Y[0], (double)nf.pos.Y[1],
-                        (double)nf.pos.Y[2]};
+    put_scene();
+    put_waves_and_spheres();
     for (size_t s = 0; s < nf.sVector.size(); s++) {
         const sphere& S = nf.sVector[s];
         const std::string p = "sphere" + std::to_string(s) + ".";
-        g_out[p + "geom"] = {(double)S.Nl, (double)S.d_min, (double)S.d_max, (double)S.Usp.R[0],
-                             (double)S.Usp.R[1], (double)S.Uip.R[0], (double)S.Uip.R[1]};
-        g_out[p + "in"] = {(double)S.p[0], (double)S.p[1], (double)S.p[2], (double)S.a, (double)S.n.real(),
-                           (double)S.n.imag()};
-        put_complex(p + "A", S.A.data(), S.A.size());
-        put_complex(p + "B", S.B.data(), S.B.size());
         if (nf.lut_us) {
             put_complex(p + "Usp", S.Usp.x_hat, (size_t)S.Usp.R[0] * S.Usp.R[1]);
             put_complex(p + "Uip", S.Uip.x_hat, (size_t)S.Uip.R[0] * S.Uip.R[1]);
@@ -117,13 +172,7 @@ int ref_sim_run(int argc, const char** argv, int stop) {
     put_complex("Uf", nf.Uf.x_hat, nnf);
 
     SCOPE->SimulateImaging();
-    scalarslice I = SCOPE->getIntensity();
-    scalarslice Ii = SCOPE->getIncidentFieldImage();
-    scalarslice Ab = SCOPE->getAbsorbance();
-    const size_t nd = (size_t)I.R[0] * I.R[1];
-    put_real("D", I.S, nd);
-    put_real("Di", Ii.S, nd);
-    put_real("Absorbance", Ab.S, nd);
+    put_detector();
     put_complex("Ud", SCOPE->Ud.x_hat, (size_t)SCOPE->Ud.R[0] * SCOPE->Ud.R[1]);
     return 0;
 }

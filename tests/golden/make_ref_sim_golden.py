@@ -12,7 +12,9 @@ LUT apply and the incident-field LUT, whose texture copies are hard-coded for fl
 own flags, this writes into tests/golden/ref_sim.json the inputs as the reference holds them after
 parsing (wavelength, apertures, spheres, the near-field plane), its Monte Carlo directions, Mie
 coefficients, per-sphere tables (sampled rows), near fields U and Uf after sumUf, and the detector
-images D, Di and absorbance.  Arrays are little-endian float64, base64-encoded.
+images D, Di and absorbance; for the ring scenes (stop = 2: the driver of --interpolate 1, 2 or 3,
+as fileout.cu:219-243 calls it) the inputs, directions, coefficients and the detector images the
+driver leaves.  Arrays are little-endian float64, base64-encoded.
 """
 import base64
 import contextlib
@@ -28,7 +30,10 @@ REPO = os.path.dirname(os.path.dirname(HERE))
 
 TWO = ["--spheres", "0.3", "-0.2", "0", "2.2", "0", "5", "4", "1", "1", "1", "--materials", "1.5", "0.04", "1.3", "0"]
 
-# name: (build, stop after the tables?, flags)
+RING_OPTICS = ["--lambda", "3", "--condenser", "0", "0.6", "--objective", "0", "0.6", "--resolution", "12", "--xy",
+               "16", "0", "--samples", "20"]
+
+# name: (build, stop: 0 the whole path, 1 after the tables, 2 the ring-source driver; flags)
 SCENES = {
     # ptype double: direct (recursive) order sums, the whole path
     "rec_two_spheres": ("f64", 0, TWO + ["--lambda", "3", "--condenser", "0", "0.6", "--objective", "0", "0.6",
@@ -61,6 +66,16 @@ SCENES = {
     "rec_two_spheres_f32": ("f32", 0, TWO + ["--lambda", "3", "--condenser", "0", "0.6", "--objective", "0", "0.6",
                                             "--resolution", "12", "--xy", "16", "0", "--samples", "20",
                                             "--recursive"]),
+    # ptype float: the ring-source drivers of --interpolate 1, 2, 3 (stop = 2), their shared-memory
+    # ring sums run as cooperative blocks
+    "ring1_detector": ("f32", 2, TWO + RING_OPTICS + ["--focus", "0.5", "-0.25", "0", "--amplitude", "0.75",
+                                                     "--interpolate", "1", "--points-rings", "5", "4"]),
+    "ring2_line": ("f32", 2, TWO + RING_OPTICS + ["--interpolate", "2", "--points-rings", "7", "5"]),
+    "ring2_line_pow2": ("f32", 2, TWO + RING_OPTICS + ["--focus", "0.5", "-0.25", "0", "--amplitude", "0.75",
+                                                      "--interpolate", "2", "--points-rings", "8", "3"]),
+    "ring3_nearfield": ("f32", 2, TWO + RING_OPTICS + ["--focus", "0.5", "-0.25", "0", "--amplitude", "0.75",
+                                                      "--recursive", "--interpolate", "3", "--points-rings", "4",
+                                                      "3"]),
 }
 TABLE_THETA_ROWS = list(range(0, 1000, 37)) + [999]
 
@@ -71,18 +86,23 @@ def enc(a):
 
 @contextlib.contextmanager
 def quiet():
-    """The reference prints progress to stdout; keep it out of this script's output."""
+    """The reference prints progress to stdout and stderr; keep it out of this script's output."""
     sys.stdout.flush()
-    fd = os.dup(1)
+    sys.stderr.flush()
+    fds = [os.dup(1), os.dup(2)]
     null = os.open(os.devnull, os.O_WRONLY)
     os.dup2(null, 1)
+    os.dup2(null, 2)
     try:
         yield
     finally:
+        C.CDLL(None).fflush(None)  # the reference's buffered printf output
         sys.stdout.flush()
-        os.dup2(fd, 1)
-        os.close(fd)
-        os.close(null)
+        sys.stderr.flush()
+        os.dup2(fds[0], 1)
+        os.dup2(fds[1], 2)
+        for fd in fds + [null]:
+            os.close(fd)
 
 
 def main():
@@ -141,6 +161,10 @@ def main():
             rec["spheres"].append(sp)
         if stop == 0:
             for key in ("U", "Uf", "D", "Di", "Absorbance"):
+                rec[key] = enc(get(key))
+        if stop == 2:
+            rec["rings"] = get("rings").tolist()  # mode, points, rings
+            for key in ("D", "Di", "Absorbance"):
                 rec[key] = enc(get(key))
         out[name] = rec
         print(name, b, "R =", int(dims[0]), "res =", int(dims[2]), "ss =", int(dims[3]), "waves =", int(dims[5]))

@@ -79,5 +79,17 @@ def image(rec, key):
 
 
 def scenes(build=None, full=True):
+    """Single-source scenes: the whole path (full) or the tables only."""
     d = load()
-    return sorted(n for n, r in d.items() if (build is None or r["build"] == build) and (r["stop"] == 0) == full)
+    return sorted(n for n, r in d.items()
+                  if r["stop"] in (0, 1) and (build is None or r["build"] == build) and (r["stop"] == 0) == full)
+
+
+def ring_scenes():
+    """Scenes run through the reference's ring-source drivers (--interpolate 1, 2, 3)."""
+    return sorted(n for n, r in load().items() if r["stop"] == 2)
+
+
+def rings(rec):
+    """(mode, points, rings) of a ring scene."""
+    return tuple(int(v) for v in rec["rings"])

@@ -9,6 +9,8 @@ place for the host with CUDA stand-ins).
   * the reference as it ships (ptype float, LUT apply through emulated texture fetches with exact
     bilinear weights): within 1e-5 (2e-5 on absorbance), the single-precision rounding of its
     arithmetic
+  * the ring-source drivers (--interpolate 1, 2, 3) of the shipped reference: within 1e-5 (2e-5 on
+    absorbance)
   * the parsed plane, wavelength (--nu) and Monte Carlo directions as the reference derives them
 """
 import os
@@ -57,7 +59,27 @@ def test_oracle_within_single_precision_of_the_shipped_reference(name):
         assert rel(-np.log10(D / Di), rg.image(rec, "Absorbance")) <= 2e-5
 
 
-@pytest.mark.parametrize("name", rg.scenes())
+@pytest.mark.parametrize("name", rg.ring_scenes())
+def test_oracle_ring_drivers_within_single_precision_of_the_shipped_reference(name):
+    """The oracle's restatement of the ring-source drivers (--interpolate 1: rotated detector images,
+    2: the radial line of shared-memory ring sums, 3: rotated near fields) against the reference's own
+    drivers run on the CPU, their ring-sum blocks as cooperative threads."""
+    rec = rg.load()[name]
+    p = rg.params(rec)
+    arr, ns = abi.sphere_array(rg.spheres(rec))
+    mode, points, rings = rg.rings(rec)
+    D, Di = oracle_lib.simulate_rings(p, arr, ns, rg.waves(rec), mode, points, rings)
+    errs = {"D": rel(D, rg.image(rec, "D")), "Di": rel(Di, rg.image(rec, "Di"))}
+    assert max(errs.values()) <= TOL_F32, errs
+    # the line mode leaves D = Di = 0 beyond its last ring: absorbance NaN there, in both
+    with np.errstate(divide="ignore", invalid="ignore"):
+        A = -np.log10(D / Di)
+    ref = rg.image(rec, "Absorbance")
+    assert np.array_equal(np.isfinite(A), np.isfinite(ref))
+    assert rel(A[np.isfinite(A)], ref[np.isfinite(ref)]) <= 2e-5
+
+
+@pytest.mark.parametrize("name", rg.scenes() + rg.ring_scenes())
 def test_mie_coefficients_match_the_reference_run(name):
     rec = rg.load()[name]
     p = rg.params(rec)
@@ -96,7 +118,7 @@ def test_sphere_tables_match_the_reference_run(name):
         assert rel(mine_u, ref_u) <= TOL_F64 and rel(mine_i, ref_i) <= TOL_F64
 
 
-@pytest.mark.parametrize("name", rg.scenes() + rg.scenes(full=False))
+@pytest.mark.parametrize("name", rg.scenes() + rg.scenes(full=False) + rg.ring_scenes())
 def test_parsed_geometry_matches(name):
     """The near-field quad nf.pos and the derived sizes are the oracle's (arguments.h:340-438,
     microscope.cu:700-718); --nu gives lambda = 1e4/nu in single precision (arguments.h:118-123)."""
@@ -114,7 +136,7 @@ def test_parsed_geometry_matches(name):
         assert rec["scene"][0] == float(np.float32(10000) / nu)
 
 
-@pytest.mark.parametrize("name", rg.scenes("f32"))
+@pytest.mark.parametrize("name", rg.scenes("f32") + rg.ring_scenes())
 def test_reference_directions_are_the_compat_sampler(name):
     """The directions the shipped reference drew (srand(0) then mcSampleNA) are the oracle's
     restatement, which bs_sample_waves_compat reproduces on the GPU."""
