@@ -61,7 +61,8 @@ def build(verbose=False, force=False):
         obj = os.path.join(OBJ, os.path.basename(src) + ".o")
         objs.append(obj)
         if force or _stale(obj, [src] + hdrs):
-            jobs.append([nvcc] + ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
+            # host code: no contraction, so that single-precision restatements of the reference round as written
+            jobs.append([nvcc] + ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off",
                                          "-Xptxas", "-warn-spills", "-I", INCLUDE, "-I", CSRC,
                                          "-c", src, "-o", obj])
     for src in sorted(glob.glob(os.path.join(CSRC, "*.cpp"))):

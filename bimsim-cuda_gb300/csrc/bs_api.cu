@@ -410,6 +410,30 @@ static bs_status derive(bs_ctx* c) {
 // -(R-1-i) rather than -(R-i) on the negative side).
 static double bin_freq(int i, int R, double step) { return (i <= R / 2) ? i * step : -(double)(R - 1 - i) * step; }
 
+// applyBackpropagation's factor -exp(i kz d) at spectrum bin (iu, iv) of an R x R near field, in the
+// reference kernel's own arithmetic (microscope.cu:423-488): the momentum-space width Kx, its step
+// dkx, kx, k and kz are single-precision variables, du, dv and lambda double, and the phase kz d a
+// single-precision product; zero where kx^2 + ky^2 >= k^2, compared in single precision.
+static void backprop_factor(int iu, int iv, int R, double du, double dv, double lambda, float d, double* re,
+                            double* im) {
+    const float two_pi = 2.0f * (float)PI_REF;  // 2*PI, PI = 3.14159f
+    const float dkx = (float)((double)(two_pi * (float)R) * du) / (float)R;
+    const float dky = (float)((double)(two_pi * (float)R) * dv) / (float)R;
+    const float kx = (float)(iu <= R / 2 ? (double)iu * (double)dkx : -(double)(R - 1 - iu) * (double)dkx);
+    const float ky = (float)(iv <= R / 2 ? (double)iv * (double)dky : -(double)(R - 1 - iv) * (double)dky);
+    const float k = (float)((double)two_pi / lambda);
+    const float kx_sq = kx * kx, ky_sq = ky * ky, k_sq = k * k;
+    if (!(kx_sq + ky_sq < k_sq)) {
+        *re = *im = 0.0;
+        return;
+    }
+    const float kk = k * k, q = kk - kx_sq;
+    const float kz = std::sqrt(q - ky_sq);
+    const double ph = (double)(kz * d);
+    *re = -std::cos(ph);
+    *im = -std::sin(ph);
+}
+
 // Bins along u and v inside the objective's outer NA (the only ones the
 // band-pass keeps), with the frequency steps.
 static void passbands(const bs_ctx* c, std::vector<int>& su, std::vector<int>& sv, double& du, double& dv) {
@@ -495,16 +519,14 @@ static bs_status run_detector(bs_ctx* c, bool accumulate) {
                     c->d_mask.as<float>(), (T)1, nullptr, gs, scr, c->st);
     LAUNCHED(c);
     if (c->bp_on) {
-        // applyBackpropagation (microscope.cu:423-470, 592-605) on U only: -exp(i kz d) with
+        // applyBackpropagation (microscope.cu:423-488, 592-605) on U only: -exp(i kz d) with
         // kz = sqrt(k^2 - kx^2 - ky^2), k = 2 PI / lambda, kx = 2 PI u; zero where kx^2 + ky^2 >= k^2
         std::vector<cpx<T>> bp((size_t)Nv * Nu);
-        const double k = 2 * PI_REF / p.lambda;
         for (int j = 0; j < Nv; j++)
             for (int kk = 0; kk < Nu; kk++) {
-                const double kx = 2 * PI_REF * freq(su[kk], du), ky = 2 * PI_REF * freq(sv[j], dv);
-                const double q = k * k - kx * kx - ky * ky;
-                const double ph = q > 0 ? std::sqrt(q) * c->bp_d : 0;
-                bp[(size_t)j * Nu + kk] = q > 0 ? mk((T)(-std::cos(ph)), (T)(-std::sin(ph))) : mk((T)0, (T)0);
+                double re, im;
+                backprop_factor(su[kk], sv[j], R, du, dv, p.lambda, (float)c->bp_d, &re, &im);
+                bp[(size_t)j * Nu + kk] = mk((T)re, (T)im);
             }
         CK(c->d_bp.ensure(bp.size() * sizeof(cpx<T>)));
         CK(cudaMemcpyAsync(c->d_bp.p, bp.data(), bp.size() * sizeof(cpx<T>), cudaMemcpyHostToDevice, c->st));

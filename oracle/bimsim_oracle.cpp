@@ -1001,32 +1001,49 @@ void fft2(std::vector<cd>& f, int R, int sign) {
     }
 }
 
+// applyBackpropagation's factor -exp(i kz d) at spectrum bin (iu, iv) of an
+// R x R near field (microscope.cu:423-488), in that kernel's arithmetic:
+//     float Kx = 2*PI * uR * du;  float dkx = Kx / uR;  kx = (ptype)iu * dkx
+//     (or -(ptype)(uR - 1 - iu) * dkx above uR / 2, stored in a float);
+//     float k = 2*PI / lambda;  if (kx*kx + ky*ky < k*k) kz = sqrt(k*k - kx*kx - ky*ky)
+//     shift = -exp(i (kz * d)), d a float; else 0
+// with PI = 3.14159f and du, dv, lambda the double-precision build's ptype.
+cd backprop_factor(int iu, int iv, int R, double du, double dv, double lambda, float d) {
+    const float two_pi = 2 * (float)PI_REF;
+    const float Kx = (float)((double)(two_pi * (float)R) * du);
+    const float Ky = (float)((double)(two_pi * (float)R) * dv);
+    const float dkx = Kx / (float)R, dky = Ky / (float)R;
+    float kx, ky;
+    if (iu <= R / 2) kx = (float)((double)iu * dkx);
+    else kx = (float)(-(double)(R - 1 - iu) * dkx);
+    if (iv <= R / 2) ky = (float)((double)iv * dky);
+    else ky = (float)(-(double)(R - 1 - iv) * dky);
+    const float kx_sq = kx * kx, ky_sq = ky * ky;
+    const float k = (float)((double)two_pi / lambda);
+    const float k_sq = k * k;
+    if (!(kx_sq + ky_sq < k_sq)) return 0.0;
+    const float kz = std::sqrt(k * k - kx * kx - ky * ky);
+    const float ph = kz * d;
+    return cd(-std::cos((double)ph), -std::sin((double)ph));
+}
+
 // applyBandpass / bandpass / getFarField / integrateDetector
 // (microscope.cu:495-526, 608-662; fieldslice.cpp:25-94; fieldslice.cu:71-108,319-338)
-// bp: propagation distance of applyBackpropagation (microscope.cu:423-470,
-// 592-605), or null: the spectrum times -exp(i kz d), kz = sqrt(k^2 - kx^2 - ky^2)
-// with k = 2 PI / lambda and kx = 2 PI u on the band-pass frequency grid, zero
-// where kx^2 + ky^2 >= k^2.
+// bp: propagation distance of applyBackpropagation (microscope.cu:423-488,
+// 592-605), or null: the spectrum times backprop_factor (the reference
+// transforms back and forth between the two steps, fromAngularSpectrum
+// dividing by R^2, which is the identity here).
 std::vector<cd> bandpassed(const bs_params& p, const Geom& g, const cd* U, const double* bp = nullptr) {
     const int R = g.R;
     std::vector<cd> f(U, U + (size_t)R * R);
     fft2(f, R, -1);
     double du = 1.0 / len(g.nf.X), dv = 1.0 / len(g.nf.Y);
     double lo = p.objective[0] / p.lambda, hi = p.objective[1] / p.lambda;
-    const double k = 2 * PI_REF / p.lambda;
     for (int iv = 0; iv < R; iv++) {
         double v = (iv <= R / 2) ? iv * dv : -(double)(R - 1 - iv) * dv;
         for (int iu = 0; iu < R; iu++) {
             double u = (iu <= R / 2) ? iu * du : -(double)(R - 1 - iu) * du;
-            if (bp) {
-                const double kx = 2 * PI_REF * u, ky = 2 * PI_REF * v;
-                if (kx * kx + ky * ky < k * k) {
-                    const double kz = std::sqrt(k * k - kx * kx - ky * ky);
-                    f[(size_t)iv * R + iu] *= -std::exp(cd(0, kz * *bp));
-                } else {
-                    f[(size_t)iv * R + iu] = 0.0;
-                }
-            }
+            if (bp) f[(size_t)iv * R + iu] *= backprop_factor(iu, iv, R, du, dv, p.lambda, (float)*bp);
             double fm = std::sqrt(u * u + v * v);
             if (fm < lo || fm > hi) f[(size_t)iv * R + iu] = 0.0;
         }

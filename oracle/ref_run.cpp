@@ -8,6 +8,8 @@
 //     nearfieldStruct::Simulate, step by step         (nearfield.cpp:194-218)
 //     microscopeStruct::SimulateImaging              (microscope.cu:840)
 //     getIntensity / getIncidentFieldImage / getAbsorbance (microscope.cu:722-814)
+// (stop = 3: with microscopeStruct::applyBackpropagation, microscope.cu:592-605,
+// between them, where Simulate has it commented out, microscope.cu:853),
 // or, with stop = 2 and the reference's --interpolate 1, 2 or 3, the ring-source
 // driver that its Save dispatches to for that mode (fileout.cu:219-243):
 //     SimulateExtendedSourceInterpAtDetector         (microscope.cu:1004-1093)
@@ -132,7 +134,8 @@ extern "C" {
 // Run the reference on `argv` (argv[0] is the program name).  stop = 1 ends
 // after calcSpheres (tables only); 0 runs the whole single-source path; 2 runs
 // the ring-source driver of the parsed --interpolate mode (1, 2 or 3) and keeps
-// the detector images.
+// the detector images; 3 is 0 with the near field back-propagated over the
+// plane position before the band-pass (U and Uf are kept as sumUf left them).
 int ref_sim_run(int argc, const char** argv, int stop) {
     g_out.clear();
     std::vector<std::string> keep(argv, argv + argc);
@@ -171,6 +174,7 @@ int ref_sim_run(int argc, const char** argv, int stop) {
     put_complex("U", nf.U.x_hat, nnf);
     put_complex("Uf", nf.Uf.x_hat, nnf);
 
+    if (stop == 3) SCOPE->applyBackpropagation();
     SCOPE->SimulateImaging();
     put_detector();
     put_complex("Ud", SCOPE->Ud.x_hat, (size_t)SCOPE->Ud.R[0] * SCOPE->Ud.R[1]);

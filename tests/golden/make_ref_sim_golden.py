@@ -33,7 +33,8 @@ TWO = ["--spheres", "0.3", "-0.2", "0", "2.2", "0", "5", "4", "1", "1", "1", "--
 RING_OPTICS = ["--lambda", "3", "--condenser", "0", "0.6", "--objective", "0", "0.6", "--resolution", "12", "--xy",
                "16", "0", "--samples", "20"]
 
-# name: (build, stop: 0 the whole path, 1 after the tables, 2 the ring-source driver; flags)
+# name: (build, stop: 0 the whole path, 1 after the tables, 2 the ring-source driver, 3 the whole path with
+# the near field back-propagated; flags)
 SCENES = {
     # ptype double: direct (recursive) order sums, the whole path
     "rec_two_spheres": ("f64", 0, TWO + ["--lambda", "3", "--condenser", "0", "0.6", "--objective", "0", "0.6",
@@ -66,6 +67,11 @@ SCENES = {
     "rec_two_spheres_f32": ("f32", 0, TWO + ["--lambda", "3", "--condenser", "0", "0.6", "--objective", "0", "0.6",
                                             "--resolution", "12", "--xy", "16", "0", "--samples", "20",
                                             "--recursive"]),
+    # stop = 3: applyBackpropagation over the plane position (z = 1.5) before the band-pass
+    "rec_backprop": ("f64", 3, TWO + ["--lambda", "3", "--condenser", "0", "0.6", "--objective", "0", "0.6",
+                                     "--resolution", "12", "--xy", "16", "1.5", "--samples", "20", "--recursive"]),
+    "lut_backprop": ("f32", 3, TWO + ["--lambda", "3", "--condenser", "0", "0.6", "--objective", "0", "0.6",
+                                     "--resolution", "12", "--xy", "16", "-2.5", "--samples", "20"]),
     # ptype float: the ring-source drivers of --interpolate 1, 2, 3 (stop = 2), their shared-memory
     # ring sums run as cooperative blocks
     "ring1_detector": ("f32", 2, TWO + RING_OPTICS + ["--focus", "0.5", "-0.25", "0", "--amplitude", "0.75",
@@ -159,7 +165,7 @@ def main():
                 uip = get(f"sphere{s}.Uip").view(np.complex128).reshape(thetaR, aR)[TABLE_THETA_ROWS]
                 sp.update(theta_rows=TABLE_THETA_ROWS, Usp=enc(usp.view(np.float64)), Uip=enc(uip.view(np.float64)))
             rec["spheres"].append(sp)
-        if stop == 0:
+        if stop in (0, 3):
             for key in ("U", "Uf", "D", "Di", "Absorbance"):
                 rec[key] = enc(get(key))
         if stop == 2:

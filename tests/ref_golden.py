@@ -85,6 +85,19 @@ def scenes(build=None, full=True):
                   if r["stop"] in (0, 1) and (build is None or r["build"] == build) and (r["stop"] == 0) == full)
 
 
+def backprop_scenes(build=None):
+    """Whole-path scenes with applyBackpropagation before the band-pass."""
+    return sorted(n for n, r in load().items() if r["stop"] == 3 and (build is None or r["build"] == build))
+
+
+def plane_position(rec):
+    """z_d, the propagation distance: the plane position of --xy/--xz/--yz as a float (arguments.h:346-409)."""
+    for name in ("xy", "xz", "yz"):
+        if "--" + name in rec["flags"]:
+            return flag(rec["flags"], name, 2)[1]
+    raise ValueError("scene without an axis-aligned plane flag")
+
+
 def ring_scenes():
     """Scenes run through the reference's ring-source drivers (--interpolate 1, 2, 3)."""
     return sorted(n for n, r in load().items() if r["stop"] == 2)

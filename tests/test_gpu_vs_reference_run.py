@@ -9,6 +9,8 @@ the reference's own path run on the CPU (golden ref_sim.json; see tests/golden/m
     images, direct mode), hence the looser absorbance bound against it
   * the ring-source drivers (--interpolate 1, 2, 3), both precisions, within the same bounds of the
     shipped reference's drivers
+  * back-propagation before the band-pass (bs_set_backpropagation) against the reference's
+    applyBackpropagation in both builds, at each build's bounds
   * the CLI with the reference's flags (its Monte Carlo directions from the compat sampler): the
     ENVI images within the same bounds of the shipped reference's images, ring scenes included
 """
@@ -73,6 +75,28 @@ def test_gpu_matches_the_shipped_references_run(name):
     for prec in (BS_PREC_FP64, BS_PREC_MIXED):
         e = errors(gpu_run(rec, prec), rec)
         assert all(e[k] <= TOL_F32[k] for k in e), (prec, e)
+
+
+@pytest.mark.parametrize("name", rg.backprop_scenes())
+def test_gpu_backpropagation_matches_the_references_run(name):
+    """bs_set_backpropagation over the plane position against the reference's applyBackpropagation run
+    before its band-pass (double build: FP64 within 1e-10; shipped float build: the f32 bounds)."""
+    rec = rg.load()[name]
+    for prec in (BS_PREC_FP64, BS_PREC_MIXED):
+        with Context(rg.params(rec)) as ctx:
+            ctx.set_spheres(rg.spheres(rec))
+            ctx.set_waves(rg.waves(rec))
+            ctx.set_backpropagation(True, rg.plane_position(rec))
+            ctx.simulate(prec)
+            out = {"D": ctx.image(BS_IMG_INTENSITY, f64=True), "Di": ctx.image(BS_IMG_INCIDENT, f64=True),
+                   "Absorbance": ctx.image(BS_IMG_ABSORBANCE, f64=True)}
+        e = errors(out, rec)
+        if rec["build"] == "f64" and prec == BS_PREC_FP64:
+            assert max(e.values()) <= 1e-10, e
+        elif rec["build"] == "f64":
+            assert max(e.values()) <= 1e-5, e
+        else:
+            assert all(e[k] <= TOL_F32[k] for k in e), (prec, e)
 
 
 @pytest.mark.parametrize("name", rg.ring_scenes())

@@ -11,6 +11,7 @@ place for the host with CUDA stand-ins).
     arithmetic
   * the ring-source drivers (--interpolate 1, 2, 3) of the shipped reference: within 1e-5 (2e-5 on
     absorbance)
+  * applyBackpropagation before the band-pass, in both builds, at the bounds of each build
   * the parsed plane, wavelength (--nu) and Monte Carlo directions as the reference derives them
 """
 import os
@@ -59,6 +60,29 @@ def test_oracle_within_single_precision_of_the_shipped_reference(name):
         assert rel(-np.log10(D / Di), rg.image(rec, "Absorbance")) <= 2e-5
 
 
+@pytest.mark.parametrize("name", rg.backprop_scenes())
+def test_oracle_backpropagation_matches_the_reference_run(name):
+    """applyBackpropagation (microscope.cu:423-488, 592-605) run by the reference before its band-pass,
+    against the oracle's detector with the same propagator over the plane position."""
+    rec = rg.load()[name]
+    p, (U, Uf, _, _) = oracle_run(rec)
+    res = p.resolution
+    D, Di = np.zeros(res * res), np.zeros(res * res)
+    U = np.ascontiguousarray(U, dtype=np.complex128)
+    Uf = np.ascontiguousarray(Uf, dtype=np.complex128)
+    oracle_lib.load().bso_detector_bp(oracle_lib.C.byref(p), oracle_lib.P(U), oracle_lib.P(Uf),
+                                      rg.plane_position(rec), oracle_lib.P(D), oracle_lib.P(Di))
+    D, Di = D.reshape(res, res), Di.reshape(res, res)
+    tol = TOL_F64 if rec["build"] == "f64" else TOL_F32
+    errs = {"U": rel(U, rg.field(rec, "U")), "D": rel(D, rg.image(rec, "D")), "Di": rel(Di, rg.image(rec, "Di"))}
+    assert max(errs.values()) <= tol, errs
+    with np.errstate(divide="ignore", invalid="ignore"):
+        assert rel(-np.log10(D / Di), rg.image(rec, "Absorbance")) <= (TOL_F64 if rec["build"] == "f64" else 2e-5)
+    # the propagation changes the image: the single-source run of the same scene differs
+    _, _, D0, _ = oracle_lib.simulate(p, *abi.sphere_array(rg.spheres(rec)), rg.waves(rec))
+    assert rel(D0, D) > 1e-3
+
+
 @pytest.mark.parametrize("name", rg.ring_scenes())
 def test_oracle_ring_drivers_within_single_precision_of_the_shipped_reference(name):
     """The oracle's restatement of the ring-source drivers (--interpolate 1: rotated detector images,
@@ -79,7 +103,7 @@ def test_oracle_ring_drivers_within_single_precision_of_the_shipped_reference(na
     assert rel(A[np.isfinite(A)], ref[np.isfinite(ref)]) <= 2e-5
 
 
-@pytest.mark.parametrize("name", rg.scenes() + rg.ring_scenes())
+@pytest.mark.parametrize("name", rg.scenes() + rg.ring_scenes() + rg.backprop_scenes())
 def test_mie_coefficients_match_the_reference_run(name):
     rec = rg.load()[name]
     p = rg.params(rec)
@@ -118,7 +142,7 @@ def test_sphere_tables_match_the_reference_run(name):
         assert rel(mine_u, ref_u) <= TOL_F64 and rel(mine_i, ref_i) <= TOL_F64
 
 
-@pytest.mark.parametrize("name", rg.scenes() + rg.scenes(full=False) + rg.ring_scenes())
+@pytest.mark.parametrize("name", rg.scenes() + rg.scenes(full=False) + rg.ring_scenes() + rg.backprop_scenes())
 def test_parsed_geometry_matches(name):
     """The near-field quad nf.pos and the derived sizes are the oracle's (arguments.h:340-438,
     microscope.cu:700-718); --nu gives lambda = 1e4/nu in single precision (arguments.h:118-123)."""
