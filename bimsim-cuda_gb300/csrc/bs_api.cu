@@ -1458,7 +1458,8 @@ bs_status bs_material_kk(const char* path, double n0, int32_t n_samples, int32_t
     std::ifstream f(path);
     if (!f) return fail(BS_ERR_IO, "Material Error -- file not found: %s", path);
     std::string text((std::istreambuf_iterator<char>(f)), std::istreambuf_iterator<char>());
-    std::vector<float> lam, re, im;
+    // rts::material<double>: the instantiation whose arrays match FFTW's double transforms
+    std::vector<double> lam, re, im;
     std::string err;
     if (!material_load(text, lam, re, im, err)) return fail(BS_ERR_IO, "%s: %s", path, err.c_str());
     const int N = n_samples ? n_samples : (int)lam.size();
@@ -1467,16 +1468,16 @@ bs_status bs_material_kk(const char* path, double n0, int32_t n_samples, int32_t
     if (pf > 16) return fail(BS_ERR_ARG, "bs_material_kk: padding factor %d above 16", pf);
     const int M = N * pf;
     // resample kappa at evenly spaced wavenumbers, from the shortest wavelength up (material.h:294-316)
-    const double nu_min = 10000.0 / (double)lam.back(), nu_max = 10000.0 / (double)lam.front();
+    const double nu_min = 10000.0 / lam.back(), nu_max = 10000.0 / lam.front();
     const double dnu = (nu_max - nu_min) / (N - 1);
     std::vector<double> chi2(N), kap(N);
     for (int i = 0; i < N; i++) {
         const double l = 10000.0 / (nu_max - i * dnu);
-        float nr, ni;
-        material_eval(lam, re, im, (float)l, nr, ni);
+        double nr, ni;
+        material_eval(lam, re, im, l, nr, ni);
         kap[i] = ni;
         const float k = (float)(2 * (float)PI_REF / l);      // float k, alpha as in the reference
-        const float alpha = (float)((double)ni * (double)(2 * k));
+        const float alpha = (float)(ni * (double)(2 * k));
         chi2[i] = -(double)alpha * (n0 / (double)k);
         lambdas[i] = l;
     }

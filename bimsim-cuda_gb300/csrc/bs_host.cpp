@@ -388,10 +388,19 @@ namespace {
 
 enum MatField { MF_MICRONS, MF_WAVENUMBER, MF_N, MF_K, MF_A, MF_IGNORE };
 
+template <class T>
 struct MatPoint {
-    float lambda;
-    float n_re, n_im;
+    T lambda;
+    T n_re, n_im;
 };
+
+// one value as `stream >> T` reads it (strtof / strtod), the number of characters used in *used
+template <class T>
+T read_value(const std::string& s, size_t* used);
+template <>
+float read_value<float>(const std::string& s, size_t* used) { return std::stof(s, used); }
+template <>
+double read_value<double>(const std::string& s, size_t* used) { return std::stod(s, used); }
 
 // "microns,n,k"-style column list (entryType, material.h:62-95)
 std::vector<MatField> parse_format(std::string f) {
@@ -413,7 +422,8 @@ std::vector<MatField> parse_format(std::string f) {
 
 }  // namespace
 
-bool material_load(const std::string& text, std::vector<float>& lam, std::vector<float>& re, std::vector<float>& im,
+template <class T>
+bool material_load(const std::string& text, std::vector<T>& lam, std::vector<T>& re, std::vector<T>& im,
                    std::string& err) {
     std::stringstream ss(text);
     std::string line, format = "microns,n,k";
@@ -424,15 +434,15 @@ bool material_load(const std::string& text, std::vector<float>& lam, std::vector
         if (a != std::string::npos && b != std::string::npos) format = line.substr(a + 1, b - a - 1);
     }
     const std::vector<MatField> cols = parse_format(format);
-    std::vector<MatPoint> pts;
+    std::vector<MatPoint<T>> pts;
     int lineno = 0;
     while (std::getline(ss, line)) {
         lineno++;
         if (!line.empty() && line[0] == '#') continue;
         if (line.find_first_not_of(" \t\r") == std::string::npos) continue;  // the reference loops forever here
         // inputEntry (material.h:105-160): before each value skip every character
-        // that is not a digit (so signs are dropped: "-0.5" reads 0.5), then read a float
-        MatPoint p{0.f, 0.f, 0.f};
+        // that is not a digit (so signs are dropped: "-0.5" reads 0.5), then read a T
+        MatPoint<T> p{0, 0, 0};
         size_t pos = 0;
         for (MatField c : cols) {
             while (pos < line.size() && (line[pos] < '0' || line[pos] > '9')) pos++;
@@ -442,11 +452,11 @@ bool material_load(const std::string& text, std::vector<float>& lam, std::vector
                 return false;
             }
             size_t used = 0;
-            float v = std::stof(line.substr(pos), &used);
+            const T v = read_value<T>(line.substr(pos), &used);
             pos += used;
             switch (c) {
                 case MF_MICRONS: p.lambda = v; break;
-                case MF_WAVENUMBER: p.lambda = 10000.0f / v; break;
+                case MF_WAVENUMBER: p.lambda = (T)10000.0 / v; break;
                 case MF_N: p.n_re = v; break;
                 case MF_K: p.n_im = v; break;
                 case MF_A: p.n_im = (v * p.lambda) / (4 * (float)PI_REF); break;  // _A(), material.h:37-40
@@ -455,7 +465,7 @@ bool material_load(const std::string& text, std::vector<float>& lam, std::vector
         }
         // function::insert: before the first point with a larger wavelength (function.h:80-98)
         auto it = std::upper_bound(pts.begin(), pts.end(), p,
-                                   [](const MatPoint& a, const MatPoint& b) { return a.lambda < b.lambda; });
+                                   [](const MatPoint<T>& a, const MatPoint<T>& b) { return a.lambda < b.lambda; });
         pts.insert(it, p);
     }
     if (pts.empty()) {
@@ -477,8 +487,9 @@ bool material_load(const std::string& text, std::vector<float>& lam, std::vector
 // (material.h:617-621, function.h:44-75): the first point with a larger
 // wavelength bounds the interval, ends clamp, and the weights are swapped as in
 // the reference: value = y_lo * a + y_hi * (1 - a), a = (l - l_lo) / (l_hi - l_lo).
-void material_eval(const std::vector<float>& lam, const std::vector<float>& re, const std::vector<float>& im,
-                   float l, float& n_re, float& n_im) {
+template <class T>
+void material_eval(const std::vector<T>& lam, const std::vector<T>& re, const std::vector<T>& im, T l, T& n_re,
+                   T& n_im) {
     size_t i = std::upper_bound(lam.begin(), lam.end(), l) - lam.begin();
     if (i == lam.size()) {
         n_re = re.back();
@@ -487,10 +498,19 @@ void material_eval(const std::vector<float>& lam, const std::vector<float>& re, 
         n_re = re.front();
         n_im = im.front();
     } else {
-        const float a = (l - lam[i - 1]) / (lam[i] - lam[i - 1]);
-        n_re = re[i - 1] * a + re[i] * (1.0f - a);
-        n_im = im[i - 1] * a + im[i] * (1.0f - a);
+        const T a = (l - lam[i - 1]) / (lam[i] - lam[i - 1]);
+        n_re = re[i - 1] * a + re[i] * ((T)1 - a);
+        n_im = im[i - 1] * a + im[i] * ((T)1 - a);
     }
 }
+
+template bool material_load<float>(const std::string&, std::vector<float>&, std::vector<float>&,
+                                   std::vector<float>&, std::string&);
+template bool material_load<double>(const std::string&, std::vector<double>&, std::vector<double>&,
+                                    std::vector<double>&, std::string&);
+template void material_eval<float>(const std::vector<float>&, const std::vector<float>&, const std::vector<float>&,
+                                   float, float&, float&);
+template void material_eval<double>(const std::vector<double>&, const std::vector<double>&,
+                                    const std::vector<double>&, double, double&, double&);
 
 }  // namespace bs

@@ -60,11 +60,15 @@ struct Sphere {
 };
 
 // Host helpers (bs_host.cpp).
-// Material files: parse (sorted by wavelength) and evaluate n + ik at lambda (um).
-bool material_load(const std::string& text, std::vector<float>& lam, std::vector<float>& re, std::vector<float>& im,
+// Material files: parse (sorted by wavelength) and evaluate n + ik at lambda (um), in the
+// precision T of the reference's rts::material<T> (float: the CLI's materials; double: the
+// instantiation its Kramers-Kronig routine works in).  Instantiated for float and double.
+template <class T>
+bool material_load(const std::string& text, std::vector<T>& lam, std::vector<T>& re, std::vector<T>& im,
                    std::string& err);
-void material_eval(const std::vector<float>& lam, const std::vector<float>& re, const std::vector<float>& im,
-                   float l, float& n_re, float& n_im);
+template <class T>
+void material_eval(const std::vector<T>& lam, const std::vector<T>& re, const std::vector<T>& im, T l, T& n_re,
+                   T& n_im);
 
 struct V3 {
     double x, y, z;

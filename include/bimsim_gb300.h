@@ -239,7 +239,9 @@ bs_status bs_material_eval(const char* path, const double* lambdas, int32_t n, d
 
 /* Kramers-Kronig real index of a material file (material::computeN,
  * rts/optics/material.h:257-432, which the reference never calls and which
- * needs FFTW).  kappa is resampled at n_samples (0: the file's entry count,
+ * needs FFTW).  The file is read and kappa interpolated in double precision,
+ * as rts::material<double> does (the instantiation whose arrays match FFTW's
+ * double transforms).  kappa is resampled at n_samples (0: the file's entry count,
  * at most BS_KK_MAX_SAMPLES) wavenumbers evenly spaced from 1e4 / lambda_min
  * down to 1e4 / lambda_max; chi2 = -alpha n0 / k with k = 2 pi / lambda and
  * alpha = 2 k kappa in single precision (the reference's float k and alpha);
@@ -248,8 +250,8 @@ bs_status bs_material_eval(const char* path, const double* lambdas, int32_t n, d
  * inverse / M), here as the equivalent circular convolution on the GPU in
  * double precision; n = Re(chi1) / (2 n0) + n0.  Outputs: the sample
  * wavelengths (increasing, um) and (n, kappa) pairs.  The reference's routine
- * hands complex<float> arrays to FFTW's double transforms; this restates the
- * double-precision transform it describes. */
+ * hands complex<float> arrays to FFTW's double transforms in the float
+ * instantiation; this is its double instantiation. */
 #define BS_KK_MAX_SAMPLES 16384
 bs_status bs_material_kk(const char* path, double n0, int32_t n_samples, int32_t pf, double* lambdas,
                          double* n_out);

@@ -9,6 +9,12 @@
 #include <cstring>
 #include <complex>
 
+// material::computeN (the Kramers-Kronig routine) is compiled only with FFTW;
+// its calls resolve to the stand-in ref_stub/fftw3.h.  Only this translation
+// unit instantiates it.
+#define FFTW_AVAILABLE
+#include <fftw3.h>
+
 #include "sphere.h"
 #include "nearfield.h"
 #include "montecarlo.h"
@@ -158,6 +164,23 @@ int ref_material_eval(const char* path, int n, const double* lambdas, double* ou
         out[2 * i + 1] = c.imag();
     }
     return 0;
+}
+
+// rts::material<double>(filename).computeN(n0, n_samples, pf) (material.h:257-432):
+// the returned material's samples (wavelength, n, kappa), increasing in
+// wavelength, n_samples of them (0: the file's count).  The double
+// instantiation is the one whose arrays match FFTW's double transforms.
+int ref_material_kk(const char* path, double n0, int n_samples, double pf, double* lambdas, double* n_out) {
+    rts::material<double> m{std::string(path)};
+    rts::material<double> kk = m.computeN(n0, (unsigned)n_samples, pf);
+    kk.setN0(0.0);  // getF adds n0 to every stored value
+    rts::function<double, rts::complex<double>> f = kk.getF();
+    for (unsigned i = 0; i < f.getN(); i++) {
+        lambdas[i] = f.getX(i);
+        n_out[2 * i] = f.getY(i).real();
+        n_out[2 * i + 1] = f.getY(i).imag();
+    }
+    return (int)f.getN();
 }
 
 // scalarslice::toEnvi's file handling (scalarslice.cu:146-166)

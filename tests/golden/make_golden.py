@@ -6,8 +6,9 @@ Run where the reference checkout exists (it is not available on the GPU host):
     python tests/golden/make_golden.py
 
 It loads oracle/_ref/libref_bimsim.so, i.e. the reference's bessjy.cpp,
-cbessjy.cpp, gamma.cpp, sphere.cpp, montecarlo.cpp, nearfield.cpp and
-rts/envi/envi.h compiled in place (oracle/Makefile), and records what those
+cbessjy.cpp, gamma.cpp, sphere.cpp, montecarlo.cpp, nearfield.cpp,
+rts/envi/envi.h and rts/optics/material.h (its Kramers-Kronig routine over the
+FFTW stand-in oracle/ref_stub/fftw3.h) compiled in place (oracle/Makefile), and records what those
 functions return on a fixed grid of inputs.  The CPU tests then check the
 oracle against these files on any machine.
 """
@@ -168,6 +169,31 @@ def main():
             r.ref_material_eval(path.encode(), lams.size, P(lams), P(res))
             mats[name] = {"text": text, "lambda": lams.tolist(), "n": res.tolist()}
     out["material"] = mats
+
+    # Kramers-Kronig (material<double>::computeN, material.h:257-432, with the FFTW stand-in
+    # oracle/ref_stub/fftw3.h): resampling grid, float k and alpha, zero padding, the FFT Hilbert
+    # multiplier and n = Re(chi1) / (2 n0) + n0
+    lam = np.linspace(2.5, 12.5, 120)
+    kap = 0.08 * 0.3 ** 2 / ((lam - 6.0) ** 2 + 0.3 ** 2)
+    band = "".join(f"{l:.6f} 1.5 {k:.8f}\n" for l, k in zip(lam, kap))
+    nu = np.linspace(3800.0, 900.0, 150)
+    absb = 0.6 * 30.0 ** 2 / ((nu - 1650.0) ** 2 + 30.0 ** 2) + 0.2 * 25.0 ** 2 / ((nu - 1240.0) ** 2 + 25.0 ** 2)
+    wn = "# FTIR [wavenumber,n,A]\n" + "".join(f"{v:.3f} 1.45 {a:.7f}\n" for v, a in zip(nu, absb))
+    kk_cases = {"band_default": (band, 1.5, 0, 2), "band_64_pf1": (band, 1.5, 64, 1),
+                "band_200_pf3": (band, 1.5, 200, 3), "wavenumber_absorbance": (wn, 1.45, 0, 4)}
+    r.ref_material_kk.argtypes = [C.c_char_p, C.c_double, C.c_int, C.c_double, C.c_void_p, C.c_void_p]
+    kks = {}
+    with tempfile.TemporaryDirectory() as td:
+        for name, (text, n0, ns, pf) in kk_cases.items():
+            path = os.path.join(td, name + ".txt")
+            open(path, "w").write(text)
+            N = ns or (len(text.strip().splitlines()) - text.startswith("#"))
+            lams, nk = np.zeros(N), np.zeros(2 * N)
+            got = r.ref_material_kk(path.encode(), n0, ns, float(pf), P(lams), P(nk))
+            assert got == N, (name, got, N)
+            kks[name] = {"text": text, "n0": n0, "n_samples": ns, "pf": pf, "lambda": lams.tolist(),
+                         "n": nk[0::2].tolist(), "k": nk[1::2].tolist()}
+    out["material_kk"] = kks
 
     for key, val in out.items():
         with open(os.path.join(HERE, key + ".json"), "w") as fh:

@@ -1,7 +1,12 @@
 """Kramers-Kronig real index of a material file (bs_material_kk, the
 reference's material::computeN, rts/optics/material.h:257-432): the oracle's
-FFT restatement against numpy on the CPU, the GPU routine against the oracle."""
+FFT restatement against numpy and against the reference's own routine
+(golden material_kk.json, recorded from material<double>::computeN compiled in
+place over an FFTW stand-in) on the CPU; the GPU routine against the oracle and
+against the same goldens."""
 import ctypes as C
+import json
+import os
 
 import numpy as np
 import pytest
@@ -53,6 +58,19 @@ def test_oracle_transform_matches_numpy(pf):
     assert np.max(np.abs(a - b)) <= 1e-12 * np.max(np.abs(b - 1.45))
 
 
+KK_GOLDEN = json.load(open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "material_kk.json")))
+
+
+@pytest.mark.parametrize("name", sorted(KK_GOLDEN))
+def test_oracle_transform_matches_the_references_computeN(name):
+    """Given the reference's own resampled kappa, the oracle's transform gives its n (to rounding)."""
+    g = KK_GOLDEN[name]
+    lam, kap, n = np.array(g["lambda"]), np.array(g["k"]), np.array(g["n"])
+    assert np.all(np.diff(lam) > 0) and np.max(np.abs(n - g["n0"])) > 1e-3
+    o = oracle_kk(lam, kap, g["n0"], g["pf"])
+    assert np.max(np.abs(o - n)) <= 1e-13 * np.max(np.abs(n - g["n0"])), np.max(np.abs(o - n))
+
+
 def _sin_pi_ratio(a, M):
     """sin(pi a / M) with a reduced in integers to a ratio in [0, 1/2], as kk_kernel_g does."""
     r = a % (2 * M)
@@ -98,10 +116,25 @@ def test_gpu_kk_matches_oracle(tmp_path, n_samples, pf):
     assert len(lam) == N and np.all(np.diff(lam) > 0)
     nu = 1e4 / lam
     assert np.allclose(np.diff(nu), (nu[-1] - nu[0]) / (N - 1), rtol=1e-9)  # even in wavenumber
-    # kappa is the file's, interpolated like bs_material_eval
-    assert np.array_equal(n.imag, lib.material_eval(path, lam).imag)
+    # kappa is the file's, interpolated like bs_material_eval but in double precision (material<double>)
+    assert np.allclose(n.imag, lib.material_eval(path, lam).imag, rtol=1e-6, atol=0)
     ref = oracle_kk(lam, n.imag, 1.5, pf)
     assert np.max(np.abs(n.real - ref)) <= 1e-10 * np.max(np.abs(ref - 1.5)), np.max(np.abs(n.real - ref))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", sorted(KK_GOLDEN))
+def test_gpu_kk_matches_the_references_computeN(tmp_path, name):
+    """bs_material_kk against the reference's own material<double>::computeN: the same wavelength grid and
+    kappa (bit-identical), n to the transform's rounding."""
+    g = KK_GOLDEN[name]
+    path = tmp_path / "m.txt"
+    path.write_text(g["text"])
+    lam, n = lib.material_kk(path, g["n0"], g["n_samples"], g["pf"])
+    ref_n = np.array(g["n"])
+    np.testing.assert_allclose(lam, g["lambda"], rtol=1e-15, atol=0)
+    assert np.array_equal(n.imag, np.array(g["k"]))
+    assert np.max(np.abs(n.real - ref_n)) <= 1e-10 * np.max(np.abs(ref_n - g["n0"]))
 
 
 @pytest.mark.gpu
