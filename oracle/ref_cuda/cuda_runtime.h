@@ -30,8 +30,10 @@ struct dim3 {
     dim3(unsigned int a = 1, unsigned int b = 1, unsigned int c = 1) : x(a), y(b), z(c) {}
 };
 struct float2 { float x, y; };
+struct float4 { float x, y, z, w; };
 struct double2 { double x, y; };
 inline float2 make_float2(float x, float y) { return float2{x, y}; }
+inline float4 make_float4(float x, float y, float z, float w) { return float4{x, y, z, w}; }
 
 // launch geometry of the emulated kernel being run (one host thread runs a launch)
 extern thread_local uint3 threadIdx;
@@ -127,6 +129,12 @@ inline float tex1D(const texture<float, dim, mode>& t, float x) {
     float v;
     bs_ref_tex_fetch(t.array, 1, t.addressMode, t.filterMode, t.normalized, x, 0.5f, &v);
     return v;
+}
+template <int dim, int mode>
+inline float4 tex1D(const texture<float4, dim, mode>& t, float x) {
+    float v[4];
+    bs_ref_tex_fetch(t.array, 4, t.addressMode, t.filterMode, t.normalized, x, 0.5f, v);
+    return float4{v[0], v[1], v[2], v[3]};
 }
 
 #endif
