@@ -167,8 +167,9 @@ std::vector<unsigned char> colormap(const std::vector<double>& v, double vmin, d
     for (int i = 0; i < 11; i++)
         for (int c = 0; c < 3; c++) brewer[i][c] = (float)(std::round(brewer8[i][c] / 255.0 * 1e6) / 1e6);
     std::vector<unsigned char> rgb(v.size() * 3);
+    const float lo = (float)vmin, span = (float)vmax - lo;  // the reference maps single-precision images
     for (size_t i = 0; i < v.size(); i++) {
-        const float a = (float)((v[i] - vmin) / (vmax - vmin));
+        const float a = ((float)v[i] - lo) / span;
         unsigned char* px = &rgb[3 * i];
         if (!(a == a)) {  // NaN (also vmin == vmax): black
             px[0] = px[1] = px[2] = 0;
@@ -178,16 +179,19 @@ std::vector<unsigned char> colormap(const std::vector<double>& v, double vmin, d
             const float g = a > 1.f ? 1.f : (a < 0.f ? 0.f : a);
             px[0] = px[1] = px[2] = (unsigned char)(255.f * g);
         } else {
-            // tex1D with normalised coordinate a + 1/22, linear filtering, clamp:
-            // texel coordinate 11 a, between control points floor(11 a) and +1
-            const float x = 11.f * a;
-            const float fl = std::floor(x);
-            const float fr = x - fl;
+            // applyBrewer (rts/visualization/colormap.h:92-110): tex1D at the normalised
+            // coordinate a + 1/22 (a float sum), linear filtering, clamp: texel coordinate
+            // 11 t - 0.5 between control points floor of it and the next, with exact weights
+            // (the texture unit's are 8-bit)
+            const float t = a + (float)(1.0 / 22);
+            const double xb = (double)t * 11 - 0.5;
+            const double fl = std::floor(xb);
+            const double fr = xb - fl;
             int i0 = (int)fl, i1 = i0 + 1;
             i0 = i0 < 0 ? 0 : (i0 > 10 ? 10 : i0);
             i1 = i1 < 0 ? 0 : (i1 > 10 ? 10 : i1);
             for (int c = 0; c < 3; c++)
-                px[c] = (unsigned char)(255.f * ((1.f - fr) * brewer[i0][c] + fr * brewer[i1][c]));
+                px[c] = (unsigned char)(255.f * (float)((1 - fr) * brewer[i0][c] + fr * brewer[i1][c]));
         }
     }
     return rgb;

@@ -14,7 +14,9 @@ parsing (wavelength, apertures, spheres, the near-field plane), its Monte Carlo 
 coefficients, per-sphere tables (sampled rows), near fields U and Uf after sumUf, and the detector
 images D, Di and absorbance; for the ring scenes (stop = 2: the driver of --interpolate 1, 2 or 3,
 as fileout.cu:219-243 calls it) the inputs, directions, coefficients and the detector images the
-driver leaves.  Arrays are little-endian float64, base64-encoded.
+driver leaves.  Arrays are little-endian float64, base64-encoded.  tests/golden/ref_colormap.json
+holds the reference's colour map (rts::gpu2cpu of rts/visualization/colormap.h, Brewer and gray) of a
+set of values, from oracle/ref_colormap.cpp in the same library.
 """
 import base64
 import contextlib
@@ -177,6 +179,22 @@ def main():
     with open(os.path.join(HERE, "ref_sim.json"), "w") as fh:
         json.dump(out, fh, separators=(",", ":"))
     print("wrote ref_sim.json", os.path.getsize(os.path.join(HERE, "ref_sim.json")), "bytes")
+
+    # the colour map of image outputs: rts::gpu2cpu (rts/visualization/colormap.h), Brewer and gray,
+    # on [0, max] as scalarslice::toImage maps a positive image (scalarslice.cu:93-138)
+    lib = libs["f32"]
+    lib.ref_colormap.argtypes = [C.c_void_p, C.c_int, C.c_float, C.c_float, C.c_int, C.c_void_p]
+    rng = np.random.default_rng(11)
+    vals = np.concatenate([rng.uniform(0, 3.5, 1500), np.linspace(0, 3.5, 701), [3.5, 0.0, 1.75]])
+    vals = vals.astype(np.float32)
+    cmap = {"values": vals.astype(np.float64).tolist(), "vmin": 0.0, "vmax": 3.5}
+    for cm, name in ((0, "brewer"), (1, "gray")):
+        rgb = np.zeros(3 * vals.size, np.uint8)
+        lib.ref_colormap(vals.ctypes.data_as(C.c_void_p), vals.size, 0.0, 3.5, cm, rgb.ctypes.data_as(C.c_void_p))
+        cmap[name] = rgb.tobytes().hex()
+    with open(os.path.join(HERE, "ref_colormap.json"), "w") as fh:
+        json.dump(cmap, fh, separators=(",", ":"))
+    print("wrote ref_colormap.json")
 
 
 if __name__ == "__main__":

@@ -189,19 +189,23 @@ def test_extended_source_images_give_one_source_per_nonzero_pixel(tmp_path):
 
 
 def brewer_rgb(values, vmin, vmax):
-    """Restatement of the Brewer map (rts/visualization/colormap.h) in float32 arithmetic."""
+    """Restatement of the Brewer map (rts/visualization/colormap.h:92-110): a = (v - vmin) / (vmax - vmin)
+    in float32, the normalised texture coordinate a + 1/22 (float32), linear filtering with exact
+    weights and clamping between the 11 control points, 255 * colour truncated to 8 bits."""
     ctrl = np.array([[49, 54, 149], [69, 117, 180], [116, 173, 209], [171, 217, 233], [224, 243, 248],
                      [255, 255, 191], [254, 224, 144], [253, 174, 97], [244, 109, 67], [215, 48, 39],
                      [165, 0, 38]], dtype=np.float64)
-    ctrl = (np.round(ctrl / 255.0 * 1e6) / 1e6).astype(np.float32)
-    a = ((np.asarray(values, np.float64) - vmin) / (vmax - vmin)).astype(np.float32)
-    x = np.float32(11) * a
-    fl = np.floor(x)
-    fr = (x - fl).astype(np.float32)
+    ctrl = (np.round(ctrl / 255.0 * 1e6) / 1e6).astype(np.float32).astype(np.float64)
+    v = np.asarray(values, np.float64).astype(np.float32)
+    a = (v - np.float32(vmin)) / (np.float32(vmax) - np.float32(vmin))
+    t = (a + np.float32(1.0 / 22)).astype(np.float32)
+    xb = t.astype(np.float64) * 11 - 0.5
+    fl = np.floor(xb)
+    fr = xb - fl
     i0 = np.clip(fl.astype(int), 0, 10)
     i1 = np.clip(fl.astype(int) + 1, 0, 10)
-    c = (np.float32(1) - fr)[:, None] * ctrl[i0] + fr[:, None] * ctrl[i1]
-    return (np.float32(255) * c.astype(np.float32)).astype(np.uint8)
+    c = ((1 - fr)[:, None] * ctrl[i0] + fr[:, None] * ctrl[i1]).astype(np.float32)
+    return (np.float32(255) * c).astype(np.uint8)
 
 
 def read_bmp24(path):
@@ -280,6 +284,24 @@ def test_brewer_bmp_and_png_match_the_reference_colormap(image_writer, tmp_path)
     # the six-decimal control points: (69, 117, 180) of the second point render as (68, 117, 179)
     ctrl = (np.round(np.array([69, 117, 180]) / 255.0 * 1e6) / 1e6).astype(np.float32)
     assert (np.float32(255) * ctrl).astype(np.uint8).tolist() == [68, 117, 179]
+
+
+def test_colour_maps_are_the_references(image_writer, tmp_path):
+    """The image writer's Brewer and gray maps give the bytes of the reference's own rts::gpu2cpu
+    (rts/visualization/colormap.h; golden ref_colormap.json from its kernels run on the CPU with exact
+    texture weights) for 2204 values on [0, 3.5]; and the numpy restatement agrees."""
+    import json
+    g = json.load(open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ref_colormap.json")))
+    vals = np.array(g["values"])
+    n = vals.size
+    grid = vals.reshape(19, n // 19) if n % 19 == 0 else np.concatenate([vals, np.full(-n % 29, 0.0)]).reshape(-1, 29)
+    for cm, name in ((0, "brewer"), (1, "gray")):
+        ref = np.frombuffer(bytes.fromhex(g[name]), np.uint8).reshape(-1, 3)
+        path = tmp_path / f"{name}.bmp"
+        assert image_writer(path, grid, cm=cm).returncode == 0
+        img = read_bmp24(path).reshape(-1, 3)[:n]
+        assert np.array_equal(img, ref), np.argwhere(np.any(img != ref, axis=1))[:5].ravel()
+    assert np.array_equal(brewer_rgb(vals, 0.0, 3.5), np.frombuffer(bytes.fromhex(g["brewer"]), np.uint8).reshape(-1, 3))
 
 
 def test_gray_and_signed_range(image_writer, tmp_path):
