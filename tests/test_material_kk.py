@@ -116,8 +116,10 @@ def test_gpu_kk_matches_oracle(tmp_path, n_samples, pf):
     assert len(lam) == N and np.all(np.diff(lam) > 0)
     nu = 1e4 / lam
     assert np.allclose(np.diff(nu), (nu[-1] - nu[0]) / (N - 1), rtol=1e-9)  # even in wavenumber
-    # kappa is the file's, interpolated like bs_material_eval but in double precision (material<double>)
-    assert np.allclose(n.imag, lib.material_eval(path, lam).imag, rtol=1e-6, atol=0)
+    # kappa is the file's, interpolated like bs_material_eval but in double precision (material<double>),
+    # where bs_material_eval interpolates in single precision at the wavelength rounded to float
+    k32 = lib.material_eval(path, lam).imag
+    assert np.max(np.abs(n.imag - k32)) <= 1e-5 * np.max(np.abs(k32))
     ref = oracle_kk(lam, n.imag, 1.5, pf)
     assert np.max(np.abs(n.real - ref)) <= 1e-10 * np.max(np.abs(ref - 1.5)), np.max(np.abs(n.real - ref))
 
