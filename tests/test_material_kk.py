@@ -116,10 +116,16 @@ def test_gpu_kk_matches_oracle(tmp_path, n_samples, pf):
     assert len(lam) == N and np.all(np.diff(lam) > 0)
     nu = 1e4 / lam
     assert np.allclose(np.diff(nu), (nu[-1] - nu[0]) / (N - 1), rtol=1e-9)  # even in wavenumber
-    # kappa is the file's, interpolated like bs_material_eval but in double precision (material<double>),
-    # where bs_material_eval interpolates in single precision at the wavelength rounded to float
-    k32 = lib.material_eval(path, lam).imag
-    assert np.max(np.abs(n.imag - k32)) <= 1e-5 * np.max(np.abs(k32))
+    # kappa is the file's, interpolated in double precision as material<double>::getN does (function.h:44-75:
+    # the first row with a larger wavelength bounds the interval, the weights are swapped, the ends clamp)
+    rows = np.array([[float(x) for x in line.split()] for line in path.read_text().splitlines()])
+    fl, fk = rows[:, 0], rows[:, 2]
+    i = np.searchsorted(fl, lam, side="right")
+    inner = (i > 0) & (i < len(fl))
+    ii = np.clip(i, 1, len(fl) - 1)
+    a = (lam - fl[ii - 1]) / (fl[ii] - fl[ii - 1])
+    k64 = np.where(inner, fk[ii - 1] * a + fk[ii] * (1.0 - a), np.where(i == 0, fk[0], fk[-1]))
+    assert np.max(np.abs(n.imag - k64)) <= 1e-15 * np.max(np.abs(k64))
     ref = oracle_kk(lam, n.imag, 1.5, pf)
     assert np.max(np.abs(n.real - ref)) <= 1e-10 * np.max(np.abs(ref - 1.5)), np.max(np.abs(n.real - ref))
 
