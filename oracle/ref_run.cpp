@@ -15,6 +15,10 @@
 //     SimulateExtendedSourceInterpAtDetector         (microscope.cu:1004-1093)
 //     SimulateExtendedSourceInterpLineAtDetector     (microscope.cu:1097-1183)
 //     SimulateExtendedSourceWithInterpolation        (microscope.cu:1189-1253)
+// or, with stop = 4 and --extended-source, the point-source driver Save runs
+// for the sources LoadParameters loaded from the image (fileout.cu:197-207):
+//     LoadExtendedSource                             (microscope.cu:1258-1296)
+//     SimulateExtendedSource                         (microscope.cu:873-913)
 // and keeps its Monte Carlo directions, Mie coefficients, per-sphere tables,
 // near fields and detector images for the accessors below.  Simulate is taken
 // step by step only so that the tables can be read after calcSpheres; the
@@ -127,6 +131,21 @@ int run_rings() {
     g_out["rings"] = {(double)scope->interpolate, (double)scope->nf.extSource[0], (double)scope->nf.extSource[1]};
     return 0;
 }
+
+// The extended source LoadParameters loaded, and SimulateExtendedSource over it.
+int run_sources() {
+    put_scene();
+    microscopeStruct* scope = SCOPE;
+    if (scope->focalPoints.empty()) return 3;
+    std::vector<double> pts;
+    for (const sourcePoint& p : scope->focalPoints)
+        for (double v : {(double)p.f[0], (double)p.f[1], (double)p.f[2], (double)p.A}) pts.push_back(v);
+    g_out["sources"] = pts;
+    scope->SimulateExtendedSource();
+    put_waves_and_spheres();
+    put_detector();
+    return 0;
+}
 }  // namespace
 
 extern "C" {
@@ -135,7 +154,9 @@ extern "C" {
 // after calcSpheres (tables only); 0 runs the whole single-source path; 2 runs
 // the ring-source driver of the parsed --interpolate mode (1, 2 or 3) and keeps
 // the detector images; 3 is 0 with the near field back-propagated over the
-// plane position before the band-pass (U and Uf are kept as sumUf left them).
+// plane position before the band-pass (U and Uf are kept as sumUf left them);
+// 4 runs SimulateExtendedSource over the sources of --extended-source and keeps
+// them (x, y, z, amplitude) and the detector images.
 int ref_sim_run(int argc, const char** argv, int stop) {
     g_out.clear();
     std::vector<std::string> keep(argv, argv + argc);
@@ -149,6 +170,7 @@ int ref_sim_run(int argc, const char** argv, int stop) {
     SCOPE->init();
     nearfieldStruct& nf = SCOPE->nf;
     if (stop == 2) return run_rings();
+    if (stop == 4) return run_sources();
 
     nf.t_Uf = 0;
     nf.t_Us = 0;

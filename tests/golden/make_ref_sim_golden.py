@@ -24,6 +24,7 @@ import ctypes as C
 import json
 import os
 import sys
+import tempfile
 
 import numpy as np
 
@@ -32,11 +33,14 @@ REPO = os.path.dirname(os.path.dirname(HERE))
 
 TWO = ["--spheres", "0.3", "-0.2", "0", "2.2", "0", "5", "4", "1", "1", "1", "--materials", "1.5", "0.04", "1.3", "0"]
 
+# a 4 x 3 source image: four nonzero pixels of different brightness
+EXT_PGM = b"P5\n4 3\n255\n" + bytes([0, 255, 0, 128, 64, 0, 0, 0, 0, 0, 200, 0])
+
 RING_OPTICS = ["--lambda", "3", "--condenser", "0", "0.6", "--objective", "0", "0.6", "--resolution", "12", "--xy",
                "16", "0", "--samples", "20"]
 
 # name: (build, stop: 0 the whole path, 1 after the tables, 2 the ring-source driver, 3 the whole path with
-# the near field back-propagated; flags)
+# the near field back-propagated, 4 the extended-source driver; flags)
 SCENES = {
     # ptype double: direct (recursive) order sums, the whole path
     "rec_two_spheres": ("f64", 0, TWO + ["--lambda", "3", "--condenser", "0", "0.6", "--objective", "0", "0.6",
@@ -74,6 +78,11 @@ SCENES = {
                                      "--resolution", "12", "--xy", "16", "1.5", "--samples", "20", "--recursive"]),
     "lut_backprop": ("f32", 3, TWO + ["--lambda", "3", "--condenser", "0", "0.6", "--objective", "0", "0.6",
                                      "--resolution", "12", "--xy", "16", "-2.5", "--samples", "20"]),
+    # stop = 4: --extended-source, the reference's point-source driver over the nonzero pixels of an
+    # 8-bit image (EXT_PGM, written to a temporary file that replaces "{image}")
+    "ext_source": ("f32", 4, TWO + ["--lambda", "3", "--condenser", "0", "0.6", "--objective", "0", "0.6",
+                                   "--resolution", "12", "--xy", "16", "0", "--samples", "20",
+                                   "--extended-source", "{image}"]),
     # ptype float: the ring-source drivers of --interpolate 1, 2, 3 (stop = 2), their shared-memory
     # ring sums run as cooperative blocks
     "ring1_detector": ("f32", 2, TWO + RING_OPTICS + ["--focus", "0.5", "-0.25", "0", "--amplitude", "0.75",
@@ -126,9 +135,13 @@ def main():
         lib.ref_sim_get.argtypes = [C.c_char_p, C.c_void_p]
         libs[b] = lib
     out = {}
+    tmp = tempfile.mkdtemp()
+    image = os.path.join(tmp, "source.pgm")
+    with open(image, "wb") as fh:
+        fh.write(EXT_PGM)
     for name, (b, stop, flags) in SCENES.items():
         lib = libs[b]
-        argv = ["bimsim"] + flags
+        argv = ["bimsim"] + [image if f == "{image}" else f for f in flags]
         arr = (C.c_char_p * len(argv))(*[a.encode() for a in argv])
         with quiet():
             rc = lib.ref_sim_run(len(argv), arr, stop)
@@ -172,6 +185,11 @@ def main():
                 rec[key] = enc(get(key))
         if stop == 2:
             rec["rings"] = get("rings").tolist()  # mode, points, rings
+            for key in ("D", "Di", "Absorbance"):
+                rec[key] = enc(get(key))
+        if stop == 4:
+            rec["image_pgm"] = EXT_PGM.hex()
+            rec["sources"] = get("sources").tolist()  # x, y, z, amplitude per source, in load order
             for key in ("D", "Di", "Absorbance"):
                 rec[key] = enc(get(key))
         out[name] = rec

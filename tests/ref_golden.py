@@ -98,6 +98,16 @@ def plane_position(rec):
     raise ValueError("scene without an axis-aligned plane flag")
 
 
+def source_scenes():
+    """Scenes run through the reference's extended-source driver (--extended-source)."""
+    return sorted(n for n, r in load().items() if r["stop"] == 4)
+
+
+def sources(rec):
+    """The point sources (x, y, z, amplitude) the reference loaded from the scene's image."""
+    return np.array(rec["sources"]).reshape(-1, 4)
+
+
 def ring_scenes():
     """Scenes run through the reference's ring-source drivers (--interpolate 1, 2, 3)."""
     return sorted(n for n, r in load().items() if r["stop"] == 2)

@@ -11,6 +11,8 @@ the reference's own path run on the CPU (golden ref_sim.json; see tests/golden/m
     shipped reference's drivers
   * back-propagation before the band-pass (bs_set_backpropagation) against the reference's
     applyBackpropagation in both builds, at each build's bounds
+  * bs_simulate_sources over the sources of an --extended-source image against the reference's
+    SimulateExtendedSource (and the CLI with that flag), at the f32 bounds
   * the CLI with the reference's flags (its Monte Carlo directions from the compat sampler): the
     ENVI images within the same bounds of the shipped reference's images, ring scenes included
 """
@@ -99,6 +101,22 @@ def test_gpu_backpropagation_matches_the_references_run(name):
             assert all(e[k] <= TOL_F32[k] for k in e), (prec, e)
 
 
+@pytest.mark.parametrize("name", rg.source_scenes())
+def test_gpu_extended_source_matches_the_references_driver(name):
+    """bs_simulate_sources over the point sources the reference loaded from the scene's image, against
+    its SimulateExtendedSource (shipped single-precision build run on the CPU)."""
+    rec = rg.load()[name]
+    for prec in (BS_PREC_FP64, BS_PREC_MIXED):
+        with Context(rg.params(rec)) as ctx:
+            ctx.set_spheres(rg.spheres(rec))
+            ctx.set_waves(rg.waves(rec))
+            ctx.simulate_sources(rg.sources(rec), prec)
+            out = {"D": ctx.image(BS_IMG_INTENSITY, f64=True), "Di": ctx.image(BS_IMG_INCIDENT, f64=True),
+                   "Absorbance": ctx.image(BS_IMG_ABSORBANCE, f64=True)}
+        e = errors(out, rec)
+        assert all(e[k] <= TOL_F32[k] for k in e), (prec, e)
+
+
 @pytest.mark.parametrize("name", rg.ring_scenes())
 def test_gpu_ring_drivers_match_the_shipped_references_run(name):
     """bs_simulate_ring_detector / _line / _interp against the reference's own --interpolate 1, 2, 3
@@ -117,12 +135,16 @@ def test_gpu_ring_drivers_match_the_shipped_references_run(name):
         assert all(e[k] <= TOL_F32[k] for k in e), (prec, e)
 
 
-@pytest.mark.parametrize("name", rg.scenes("f32") + rg.ring_scenes())
+@pytest.mark.parametrize("name", rg.scenes("f32") + rg.ring_scenes() + rg.source_scenes())
 def test_cli_with_the_references_flags_matches_its_run(name, tmp_path):
     rec = rg.load()[name]
     outs = {k: str(tmp_path / k) for k in ("D", "Di", "Absorbance")}
-    cmd = [EXE] + rec["flags"] + ["--intensity", outs["D"], "--incident", outs["Di"], "--absorbance",
-                                  outs["Absorbance"], "--absorbance-spec", ""]
+    flags = list(rec["flags"])
+    if "{image}" in flags:  # the extended-source image the reference read
+        (tmp_path / "source.pgm").write_bytes(bytes.fromhex(rec["image_pgm"]))
+        flags = [str(tmp_path / "source.pgm") if f == "{image}" else f for f in flags]
+    cmd = [EXE] + flags + ["--intensity", outs["D"], "--incident", outs["Di"], "--absorbance",
+                           outs["Absorbance"], "--absorbance-spec", ""]
     r = subprocess.run(cmd, capture_output=True, text=True, cwd=str(tmp_path))
     assert r.returncode == 0, r.stdout + r.stderr
     res = int(rec["dims"][2])

@@ -12,6 +12,8 @@ place for the host with CUDA stand-ins).
   * the ring-source drivers (--interpolate 1, 2, 3) of the shipped reference: within 1e-5 (2e-5 on
     absorbance)
   * applyBackpropagation before the band-pass, in both builds, at the bounds of each build
+  * the extended-source driver (--extended-source): the points it loads from the image and its summed
+    detector images, within 1e-5
   * the parsed plane, wavelength (--nu) and Monte Carlo directions as the reference derives them
 """
 import os
@@ -83,6 +85,38 @@ def test_oracle_backpropagation_matches_the_reference_run(name):
     assert rel(D0, D) > 1e-3
 
 
+@pytest.mark.parametrize("name", rg.source_scenes())
+def test_oracle_extended_source_matches_the_references_driver(name):
+    """--extended-source: the reference's LoadExtendedSource (microscope.cu:1258-1296) placed a point source
+    at pos(x / width, y / height) of the detector plane with amplitude pixel / 255 for every nonzero pixel,
+    x outer, y inner; its SimulateExtendedSource (:873-913) summed their detector images.  The library's
+    plane mapping gives the same points, and the oracle's per-source slices sum to its images."""
+    from bimsim_gb300 import lib
+    rec = rg.load()[name]
+    p = rg.params(rec)
+    pgm = bytes.fromhex(rec["image_pgm"])
+    hdr = pgm.split(b"\n", 3)
+    w, h = (int(v) for v in hdr[1].split())
+    px = np.frombuffer(hdr[3], np.uint8).reshape(h, w)
+    expect = [(x, y) for x in range(w) for y in range(h) if px[y, x] != 0]
+    src = rg.sources(rec)
+    assert len(src) == len(expect)
+    for (x, y), (sx, sy, sz, a) in zip(expect, src):
+        u, v = float(np.float32(x) / np.float32(w)), float(np.float32(y) / np.float32(h))
+        np.testing.assert_allclose(lib.plane_point(p, u, v), (sx, sy, sz), rtol=0, atol=2e-6)
+        assert a == float(np.float32(px[y, x]) / np.float32(255))
+    arr, ns = abi.sphere_array(rg.spheres(rec))
+    D = Di = 0
+    for sx, sy, sz, a in src:
+        q = rg.params(rec)
+        q.focus[0], q.focus[1], q.focus[2] = sx, sy, sz
+        q.amplitude = a
+        _, _, d, di = oracle_lib.simulate(q, arr, ns, rg.waves(rec))
+        D, Di = D + d, Di + di
+    errs = {"D": rel(D, rg.image(rec, "D")), "Di": rel(Di, rg.image(rec, "Di"))}
+    assert max(errs.values()) <= TOL_F32, errs
+
+
 @pytest.mark.parametrize("name", rg.ring_scenes())
 def test_oracle_ring_drivers_within_single_precision_of_the_shipped_reference(name):
     """The oracle's restatement of the ring-source drivers (--interpolate 1: rotated detector images,
@@ -103,7 +137,7 @@ def test_oracle_ring_drivers_within_single_precision_of_the_shipped_reference(na
     assert rel(A[np.isfinite(A)], ref[np.isfinite(ref)]) <= 2e-5
 
 
-@pytest.mark.parametrize("name", rg.scenes() + rg.ring_scenes() + rg.backprop_scenes())
+@pytest.mark.parametrize("name", rg.scenes() + rg.ring_scenes() + rg.backprop_scenes() + rg.source_scenes())
 def test_mie_coefficients_match_the_reference_run(name):
     rec = rg.load()[name]
     p = rg.params(rec)
