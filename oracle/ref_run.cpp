@@ -10,7 +10,8 @@
 //     getIntensity / getIncidentFieldImage / getAbsorbance (microscope.cu:722-814)
 // (stop = 3: with microscopeStruct::applyBackpropagation, microscope.cu:592-605,
 // between them, where Simulate has it commented out, microscope.cu:853),
-// or, with stop = 2 and the reference's --interpolate 1, 2 or 3, the ring-source
+// or, with stop = 2 and the reference's --interpolate 1, 2 or 3 (or 0 with no
+// rings), the ring-source
 // driver that its Save dispatches to for that mode (fileout.cu:219-243):
 //     SimulateExtendedSourceInterpAtDetector         (microscope.cu:1004-1093)
 //     SimulateExtendedSourceInterpLineAtDetector     (microscope.cu:1097-1183)
@@ -124,6 +125,11 @@ int run_rings() {
         scope->SimulateExtendedSourceInterpLineAtDetector(scope->nf.extSource);
     else if (scope->interpolate == 3)
         scope->SimulateExtendedSourceWithInterpolation(0, scope->nf.extSource);
+    else if (scope->interpolate == 0 && scope->nf.extSource[1] == 0)
+        // SimulateExtendedGausssianSourceNoInterp (microscope.cu:1327-1409) with no rings: the central
+        // source only.  With one ring or more its loop `for (int j = spacing; ...; j += spacing)`,
+        // spacing = 0.5, never advances, so it is not run.
+        scope->SimulateExtendedGausssianSourceNoInterp(scope->nf.extSource);
     else
         return 2;
     put_waves_and_spheres();

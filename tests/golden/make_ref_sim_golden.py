@@ -90,6 +90,8 @@ SCENES = {
     "ring2_line": ("f32", 2, TWO + RING_OPTICS + ["--interpolate", "2", "--points-rings", "7", "5"]),
     "ring2_line_pow2": ("f32", 2, TWO + RING_OPTICS + ["--focus", "0.5", "-0.25", "0", "--amplitude", "0.75",
                                                       "--interpolate", "2", "--points-rings", "8", "3"]),
+    "ring0_no_rings": ("f32", 2, TWO + RING_OPTICS + ["--focus", "0.5", "-0.25", "0", "--amplitude", "0.75",
+                                                     "--interpolate", "0", "--points-rings", "3", "0"]),
     "ring3_nearfield": ("f32", 2, TWO + RING_OPTICS + ["--focus", "0.5", "-0.25", "0", "--amplitude", "0.75",
                                                       "--recursive", "--interpolate", "3", "--points-rings", "4",
                                                       "3"]),

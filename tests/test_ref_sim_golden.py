@@ -120,13 +120,17 @@ def test_oracle_extended_source_matches_the_references_driver(name):
 @pytest.mark.parametrize("name", rg.ring_scenes())
 def test_oracle_ring_drivers_within_single_precision_of_the_shipped_reference(name):
     """The oracle's restatement of the ring-source drivers (--interpolate 1: rotated detector images,
-    2: the radial line of shared-memory ring sums, 3: rotated near fields) against the reference's own
-    drivers run on the CPU, their ring-sum blocks as cooperative threads."""
+    2: the radial line of shared-memory ring sums, 3: rotated near fields; 0 with no rings: the central
+    source) against the reference's own drivers run on the CPU, their ring-sum blocks as cooperative
+    threads."""
     rec = rg.load()[name]
     p = rg.params(rec)
     arr, ns = abi.sphere_array(rg.spheres(rec))
     mode, points, rings = rg.rings(rec)
-    D, Di = oracle_lib.simulate_rings(p, arr, ns, rg.waves(rec), mode, points, rings)
+    if mode == 0:  # no rings: the central source alone
+        _, _, D, Di = oracle_lib.simulate(p, arr, ns, rg.waves(rec))
+    else:
+        D, Di = oracle_lib.simulate_rings(p, arr, ns, rg.waves(rec), mode, points, rings)
     errs = {"D": rel(D, rg.image(rec, "D")), "Di": rel(Di, rg.image(rec, "Di"))}
     assert max(errs.values()) <= TOL_F32, errs
     # the line mode leaves D = Di = 0 beyond its last ring: absorbance NaN there, in both
