@@ -162,7 +162,9 @@ extern "C" {
 // the detector images; 3 is 0 with the near field back-propagated over the
 // plane position before the band-pass (U and Uf are kept as sumUf left them);
 // 4 runs SimulateExtendedSource over the sources of --extended-source and keeps
-// them (x, y, z, amplitude) and the detector images.
+// them (x, y, z, amplitude) and the detector images; 5 ends after sumUf (the
+// near fields only: with --vector the reference's getFarField copies the y and z
+// components into a crop slice allocated without them, fieldslice.cu:340-361).
 int ref_sim_run(int argc, const char** argv, int stop) {
     g_out.clear();
     std::vector<std::string> keep(argv, argv + argc);
@@ -201,6 +203,7 @@ int ref_sim_run(int argc, const char** argv, int stop) {
     const size_t nnf = (size_t)nf.U.R[0] * nf.U.R[1];
     put_complex("U", nf.U.x_hat, nnf);
     put_complex("Uf", nf.Uf.x_hat, nnf);
+    if (stop == 5) return 0;
 
     if (stop == 3) SCOPE->applyBackpropagation();
     SCOPE->SimulateImaging();

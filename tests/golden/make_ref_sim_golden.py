@@ -40,7 +40,7 @@ RING_OPTICS = ["--lambda", "3", "--condenser", "0", "0.6", "--objective", "0", "
                "16", "0", "--samples", "20"]
 
 # name: (build, stop: 0 the whole path, 1 after the tables, 2 the ring-source driver, 3 the whole path with
-# the near field back-propagated, 4 the extended-source driver; flags)
+# the near field back-propagated, 4 the extended-source driver, 5 the near fields only; flags)
 SCENES = {
     # ptype double: direct (recursive) order sums, the whole path
     "rec_two_spheres": ("f64", 0, TWO + ["--lambda", "3", "--condenser", "0", "0.6", "--objective", "0", "0.6",
@@ -57,6 +57,12 @@ SCENES = {
     "rec_supersample": ("f64", 0, ["--spheres", "0.23", "0.11", "0", "1.03", "0", "--materials", "1.4", "0.05",
                                    "--lambda", "1.5", "--condenser", "0", "0.5", "--objective", "0", "0.5",
                                    "--resolution", "6", "--xy", "6", "0", "--samples", "16", "--recursive"]),
+    # --vector: the reference's vector stub (nfVectorUf.cu's incident field, no scattered field); stop = 5,
+    # the near fields only: past sumUf the reference writes the crop's y and z components through null
+    # pointers (fieldslice.cu:340-361)
+    "vec_direct": ("f64", 5, TWO + ["--lambda", "3", "--condenser", "0.1", "0.6", "--objective", "0", "0.6",
+                                   "--resolution", "12", "--xy", "16", "0", "--samples", "20", "--focus", "0.5",
+                                   "-0.25", "0", "--vector"]),
     # ptype double: the per-sphere tables of the LUT mode (sphere::calcUp and sphere.cu's sums)
     "tables_two_spheres": ("f64", 1, TWO + ["--lambda", "3", "--resolution", "12", "--xy", "16", "0",
                                            "--samples", "8"]),
@@ -70,6 +76,9 @@ SCENES = {
     "lut_supersample_nu": ("f32", 0, ["--spheres", "0.23", "0.11", "0", "1.03", "0", "--materials", "1.4", "0.05",
                                       "--nu", "6666.667", "--condenser", "0", "0.5", "--objective", "0", "0.5",
                                       "--resolution", "6", "--xy", "6", "0", "--samples", "16"]),
+    "vec_direct_f32": ("f32", 5, TWO + ["--lambda", "3", "--condenser", "0.1", "0.6", "--objective", "0", "0.6",
+                                       "--resolution", "12", "--xy", "16", "0", "--samples", "20", "--focus", "0.5",
+                                       "-0.25", "0", "--vector"]),
     "rec_two_spheres_f32": ("f32", 0, TWO + ["--lambda", "3", "--condenser", "0", "0.6", "--objective", "0", "0.6",
                                             "--resolution", "12", "--xy", "16", "0", "--samples", "20",
                                             "--recursive"]),
@@ -184,6 +193,9 @@ def main():
             rec["spheres"].append(sp)
         if stop in (0, 3):
             for key in ("U", "Uf", "D", "Di", "Absorbance"):
+                rec[key] = enc(get(key))
+        if stop == 5:
+            for key in ("U", "Uf"):
                 rec[key] = enc(get(key))
         if stop == 2:
             rec["rings"] = get("rings").tolist()  # mode, points, rings

@@ -85,6 +85,11 @@ def scenes(build=None, full=True):
                   if r["stop"] in (0, 1) and (build is None or r["build"] == build) and (r["stop"] == 0) == full)
 
 
+def nearfield_scenes(build=None):
+    """Scenes recorded up to sumUf (the near fields U and Uf only)."""
+    return sorted(n for n, r in load().items() if r["stop"] == 5 and (build is None or r["build"] == build))
+
+
 def backprop_scenes(build=None):
     """Whole-path scenes with applyBackpropagation before the band-pass."""
     return sorted(n for n, r in load().items() if r["stop"] == 3 and (build is None or r["build"] == build))

@@ -13,6 +13,7 @@ the reference's own path run on the CPU (golden ref_sim.json; see tests/golden/m
     applyBackpropagation in both builds, at each build's bounds
   * bs_simulate_sources over the sources of an --extended-source image against the reference's
     SimulateExtendedSource (and the CLI with that flag), at the f32 bounds
+  * the vector stub's near fields (--vector), FP64 within 1e-10 of the double build, otherwise 1e-4
   * the CLI with the reference's flags (its Monte Carlo directions from the compat sampler): the
     ENVI images within the same bounds of the shipped reference's images, ring scenes included
 """
@@ -77,6 +78,24 @@ def test_gpu_matches_the_shipped_references_run(name):
     for prec in (BS_PREC_FP64, BS_PREC_MIXED):
         e = errors(gpu_run(rec, prec), rec)
         assert all(e[k] <= TOL_F32[k] for k in e), (prec, e)
+
+
+@pytest.mark.parametrize("name", rg.nearfield_scenes())
+def test_gpu_vector_stub_near_fields_match_the_references_run(name):
+    """--vector (the reference's vector stub: its incident field, no scattered field): U and Uf of both
+    precisions against the reference's near fields after sumUf."""
+    rec = rg.load()[name]
+    for prec in (BS_PREC_FP64, BS_PREC_MIXED):
+        with Context(rg.params(rec)) as ctx:
+            ctx.set_spheres(rg.spheres(rec))
+            ctx.set_waves(rg.waves(rec))
+            ctx.simulate(prec)
+            out = {"U": ctx.field(BS_FIELD_TOTAL), "Uf": ctx.field(BS_FIELD_INCIDENT)}
+        e = errors(out, rec)
+        if rec["build"] == "f64" and prec == BS_PREC_FP64:
+            assert max(e.values()) <= 1e-10, e
+        else:
+            assert max(e.values()) <= 1e-4, (prec, e)
 
 
 @pytest.mark.parametrize("name", rg.backprop_scenes())

@@ -14,6 +14,7 @@ place for the host with CUDA stand-ins).
   * applyBackpropagation before the band-pass, in both builds, at the bounds of each build
   * the extended-source driver (--extended-source): the points it loads from the image and its summed
     detector images, within 1e-5
+  * the vector stub (--vector): U and Uf after sumUf, at the bounds of each build
   * the parsed plane, wavelength (--nu) and Monte Carlo directions as the reference derives them
 """
 import os
@@ -60,6 +61,19 @@ def test_oracle_within_single_precision_of_the_shipped_reference(name):
     # absorbance, a log of a ratio of nearly equal images, carries more of the float build's rounding
     with np.errstate(divide="ignore", invalid="ignore"):
         assert rel(-np.log10(D / Di), rg.image(rec, "Absorbance")) <= 2e-5
+
+
+@pytest.mark.parametrize("name", rg.nearfield_scenes())
+def test_oracle_vector_stub_near_fields_match_the_reference_run(name):
+    """--vector: the reference's vector stub computes the incident field of nfVectorUf.cu and no scattered
+    field; U and Uf after its sumUf against the oracle's (its run stops there: getFarField then writes the
+    crop's y and z components through null pointers, fieldslice.cu:340-361)."""
+    rec = rg.load()[name]
+    assert "--vector" in rec["flags"]
+    p, (U, Uf, _, _) = oracle_run(rec)
+    tol = TOL_F64 if rec["build"] == "f64" else TOL_F32
+    errs = {"U": rel(U, rg.field(rec, "U")), "Uf": rel(Uf, rg.field(rec, "Uf"))}
+    assert max(errs.values()) <= tol, errs
 
 
 @pytest.mark.parametrize("name", rg.backprop_scenes())
@@ -141,7 +155,8 @@ def test_oracle_ring_drivers_within_single_precision_of_the_shipped_reference(na
     assert rel(A[np.isfinite(A)], ref[np.isfinite(ref)]) <= 2e-5
 
 
-@pytest.mark.parametrize("name", rg.scenes() + rg.ring_scenes() + rg.backprop_scenes() + rg.source_scenes())
+@pytest.mark.parametrize("name", rg.scenes() + rg.ring_scenes() + rg.backprop_scenes() + rg.source_scenes() +
+                         rg.nearfield_scenes())
 def test_mie_coefficients_match_the_reference_run(name):
     rec = rg.load()[name]
     p = rg.params(rec)
