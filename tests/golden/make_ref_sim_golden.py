@@ -63,6 +63,10 @@ SCENES = {
     "vec_direct": ("f64", 5, TWO + ["--lambda", "3", "--condenser", "0.1", "0.6", "--objective", "0", "0.6",
                                    "--resolution", "12", "--xy", "16", "0", "--samples", "20", "--focus", "0.5",
                                    "-0.25", "0", "--vector"]),
+    # --plane-wave: one incident plane wave along k instead of the focused field (nfScalarUf.cu:187,
+    # nfScalarUs.cu:541, nfScalarUpLut.cu:365)
+    "rec_plane_wave": ("f64", 0, TWO + ["--lambda", "3", "--objective", "0", "0.6", "--resolution", "12", "--xy",
+                                       "16", "0", "--amplitude", "1.5", "--plane-wave", "--recursive"]),
     # ptype double: the per-sphere tables of the LUT mode (sphere::calcUp and sphere.cu's sums)
     "tables_two_spheres": ("f64", 1, TWO + ["--lambda", "3", "--resolution", "12", "--xy", "16", "0",
                                            "--samples", "8"]),
@@ -76,6 +80,8 @@ SCENES = {
     "lut_supersample_nu": ("f32", 0, ["--spheres", "0.23", "0.11", "0", "1.03", "0", "--materials", "1.4", "0.05",
                                       "--nu", "6666.667", "--condenser", "0", "0.5", "--objective", "0", "0.5",
                                       "--resolution", "6", "--xy", "6", "0", "--samples", "16"]),
+    "lut_plane_wave": ("f32", 0, TWO + ["--lambda", "3", "--objective", "0", "0.6", "--resolution", "12", "--xy",
+                                       "16", "0", "--amplitude", "1.5", "--plane-wave"]),
     "vec_direct_f32": ("f32", 5, TWO + ["--lambda", "3", "--condenser", "0.1", "0.6", "--objective", "0", "0.6",
                                        "--resolution", "12", "--xy", "16", "0", "--samples", "20", "--focus", "0.5",
                                        "-0.25", "0", "--vector"]),
