@@ -67,6 +67,12 @@ SCENES = {
     # nfScalarUs.cu:541, nfScalarUpLut.cu:365)
     "rec_plane_wave": ("f64", 0, TWO + ["--lambda", "3", "--objective", "0", "0.6", "--resolution", "12", "--xy",
                                        "16", "0", "--amplitude", "1.5", "--plane-wave", "--recursive"]),
+    # a yz plane (it contains the beam axis, so the objective passes little of the incident field and the
+    # float build's rounding of Di grows: double build only)
+    "rec_yz_plane": ("f64", 0, ["--spheres", "0.3", "0.2", "-0.4", "1.8", "0", "-0.5", "3", "3", "1.2", "1",
+                                "--materials", "1.42", "0.03", "1.33", "0.01", "--lambda", "2.8", "--condenser", "0",
+                                "0.5", "--objective", "0", "0.55", "--yz", "14", "1.9", "--resolution", "10",
+                                "--samples", "24", "--field-order", "16", "--recursive"]),
     # ptype double: the per-sphere tables of the LUT mode (sphere::calcUp and sphere.cu's sums)
     "tables_two_spheres": ("f64", 1, TWO + ["--lambda", "3", "--resolution", "12", "--xy", "16", "0",
                                            "--samples", "8"]),
@@ -82,6 +88,8 @@ SCENES = {
                                       "--resolution", "6", "--xy", "6", "0", "--samples", "16"]),
     "lut_plane_wave": ("f32", 0, TWO + ["--lambda", "3", "--objective", "0", "0.6", "--resolution", "12", "--xy",
                                        "16", "0", "--amplitude", "1.5", "--plane-wave"]),
+    "lut_padding0": ("f32", 0, TWO + ["--lambda", "3", "--condenser", "0", "0.6", "--objective", "0", "0.6",
+                                     "--resolution", "20", "--xy", "16", "0", "--samples", "20", "--padding", "0"]),
     "vec_direct_f32": ("f32", 5, TWO + ["--lambda", "3", "--condenser", "0.1", "0.6", "--objective", "0", "0.6",
                                        "--resolution", "12", "--xy", "16", "0", "--samples", "20", "--focus", "0.5",
                                        "-0.25", "0", "--vector"]),
