@@ -212,6 +212,28 @@ int ref_sim_run(int argc, const char** argv, int stop) {
     return 0;
 }
 
+// The reference's executable on `argv` as its main() runs it (main.cpp:42-78):
+// SetArguments, parse, LoadParameters, microscopeStruct::init, then
+// fileoutStruct::Save (fileout.cu:189-265), which simulates and writes the
+// output files the flags name (ENVI through rts/envi; colour images go to the
+// STIM stand-in, which writes nothing).  The output settings are reset first,
+// as a fresh process would have them.
+int ref_sim_save(int argc, const char** argv) {
+    g_out.clear();
+    std::vector<std::string> keep(argv, argv + argc);
+    std::vector<char*> av;
+    for (std::string& s : keep) av.push_back(&s[0]);
+    rts::arglist args;
+    SetArguments(args);
+    args.parse(argc, av.data());
+    gFileOut = fileoutStruct();
+    SCOPE = new microscopeStruct();
+    LoadParameters(args);
+    SCOPE->init();
+    gFileOut.Save(SCOPE);
+    return 0;
+}
+
 // Number of values stored under `key` (-1 if none).
 long ref_sim_size(const char* key) {
     auto it = g_out.find(key);

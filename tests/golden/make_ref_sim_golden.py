@@ -16,7 +16,9 @@ images D, Di and absorbance; for the ring scenes (stop = 2: the driver of --inte
 as fileout.cu:219-243 calls it) the inputs, directions, coefficients and the detector images the
 driver leaves.  Arrays are little-endian float64, base64-encoded.  tests/golden/ref_colormap.json
 holds the reference's colour map (rts::gpu2cpu of rts/visualization/colormap.h, Brewer and gray) of a
-set of values, from oracle/ref_colormap.cpp in the same library.
+set of values, from oracle/ref_colormap.cpp in the same library; tests/golden/ref_cli_files.json the
+files its executable writes (ENVI intensity, incident, absorbance and transmittance with their headers,
+the absorbance-spectrum text) for runs with --append and --nu and runs that overwrite.
 """
 import base64
 import contextlib
@@ -225,6 +227,34 @@ def main():
     with open(os.path.join(HERE, "ref_sim.json"), "w") as fh:
         json.dump(out, fh, separators=(",", ":"))
     print("wrote ref_sim.json", os.path.getsize(os.path.join(HERE, "ref_sim.json")), "bytes")
+
+    # the reference's executable end to end (ref_sim_save: main.cpp's steps, then fileoutStruct::Save): the
+    # ENVI files and the absorbance-spectrum text it writes, one run per entry of "runs" in the same
+    # directory ("{dir}" in the flags)
+    lib.ref_sim_save.argtypes = [C.c_int, C.c_void_p]
+    optics = ["--condenser", "0", "0.6", "--objective", "0", "0.6", "--resolution", "12", "--xy", "16", "0",
+              "--samples", "20"]
+    outs = ["--intensity", "{dir}/i", "--incident", "{dir}/inc", "--absorbance", "{dir}/a", "--transmittance",
+            "{dir}/t", "--absorbance-spec", "{dir}/as.txt"]
+    cli_cases = {"nu_append": [TWO + ["--nu", nu] + optics + outs + ["--append"] for nu in ("3333.3333", "3500")],
+                 "lambda_overwrite": [TWO + ["--lambda", lam] + optics + outs for lam in ("3", "3.25")]}
+    files = {}
+    for name, runs in cli_cases.items():
+        d = tempfile.mkdtemp()
+        for flags in runs:
+            argv = ["bimsim"] + [f.replace("{dir}", d) for f in flags]
+            arr = (C.c_char_p * len(argv))(*[a.encode() for a in argv])
+            with quiet():
+                assert lib.ref_sim_save(len(argv), arr) == 0, name
+        rec = {"runs": runs, "files": {}}
+        for f in ("i", "inc", "a", "t"):
+            rec["files"][f] = {"hdr": open(os.path.join(d, f + ".hdr")).read(),
+                               "data": base64.b64encode(open(os.path.join(d, f), "rb").read()).decode()}
+        rec["as.txt"] = open(os.path.join(d, "as.txt")).read()
+        files[name] = rec
+    with open(os.path.join(HERE, "ref_cli_files.json"), "w") as fh:
+        json.dump(files, fh, separators=(",", ":"))
+    print("wrote ref_cli_files.json")
 
     # the colour map of image outputs: rts::gpu2cpu (rts/visualization/colormap.h), Brewer and gray,
     # on [0, max] as scalarslice::toImage maps a positive image (scalarslice.cu:93-138)

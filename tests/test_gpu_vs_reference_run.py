@@ -15,7 +15,9 @@ the reference's own path run on the CPU (golden ref_sim.json; see tests/golden/m
     SimulateExtendedSource (and the CLI with that flag), at the f32 bounds
   * the vector stub's near fields (--vector), FP64 within 1e-10 of the double build, otherwise 1e-4
   * the CLI with the reference's flags (its Monte Carlo directions from the compat sampler): the
-    ENVI images within the same bounds of the shipped reference's images, ring scenes included
+    ENVI images within the same bounds of the shipped reference's images, ring scenes included; and
+    the files the reference's executable itself writes (ENVI headers and absorbance-spectrum text
+    identical, band data within the bounds)
 """
 import os
 import subprocess
@@ -155,6 +157,35 @@ def test_gpu_ring_drivers_match_the_shipped_references_run(name):
                    "Absorbance": ctx.image(BS_IMG_ABSORBANCE, f64=True)}
         e = errors(out, rec)
         assert all(e[k] <= TOL_F32[k] for k in e), (prec, e)
+
+
+CLI_FILES = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ref_cli_files.json")
+
+
+@pytest.mark.parametrize("name", ["nu_append", "lambda_overwrite"])
+def test_cli_writes_the_references_output_files(name, tmp_path):
+    """The files the reference's executable writes (its main() and fileoutStruct::Save run on the CPU,
+    golden ref_cli_files.json): this CLI run with the same flags in the same order gives the same ENVI
+    headers (band values of --nu or --lambda, --append or overwrite) and absorbance-spectrum text, and
+    each band's data within the single-precision bounds."""
+    import base64
+    import json
+    g = json.load(open(CLI_FILES))[name]
+    for flags in g["runs"]:
+        r = subprocess.run([EXE] + [f.replace("{dir}", str(tmp_path)) for f in flags], capture_output=True,
+                           text=True, cwd=str(tmp_path))
+        assert r.returncode == 0, r.stdout + r.stderr
+    tol = {"i": TOL_F32["D"], "inc": TOL_F32["Di"], "a": TOL_F32["Absorbance"], "t": TOL_F32["Absorbance"]}
+    for f, ref in g["files"].items():
+        assert (tmp_path / (f + ".hdr")).read_text() == ref["hdr"], f
+        mine = np.fromfile(tmp_path / f, dtype="<f4")
+        theirs = np.frombuffer(base64.b64decode(ref["data"]), dtype="<f4")
+        assert mine.shape == theirs.shape, f
+        bands = mine.size // 144
+        for b in range(bands):
+            e = rel_finite(mine[b * 144:(b + 1) * 144].astype(np.float64), theirs[b * 144:(b + 1) * 144].astype(np.float64))
+            assert e <= tol[f], (f, b, e)
+    assert (tmp_path / "as.txt").read_text() == g["as.txt"]
 
 
 @pytest.mark.parametrize("name", rg.scenes("f32") + rg.ring_scenes() + rg.source_scenes())
