@@ -515,7 +515,7 @@ int main(int argc, char** argv) {
         return 0;
     }
 
-    // ---- simulate (microscopeStruct::init + fileoutStruct::Save, fileout.cu:300-318) ----
+    // ---- simulate (microscopeStruct::init + fileoutStruct::Save, fileout.cu:189-265) ----
     bs_ctx* ctx = nullptr;
     if (check(bs_create(&p, &ctx))) return 1;
     if (check(bs_set_spheres(ctx, spheres.data(), (int)spheres.size()))) return 1;

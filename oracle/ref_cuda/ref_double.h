@@ -1,7 +1,7 @@
 // ref_double.h -- TEST INFRASTRUCTURE, force-included after prelude.h for the
 // double-precision host-run build of the reference (libref_sim_f64.so).  The
 // reference's dataTypes.h hard-codes PRECISION_SINGLE (dataTypes.h:6); this
-// header stands in for it with the same definitions (dataTypes.h:4-46) except
+// header stands in for it with the same definitions (dataTypes.h:4-38) except
 // that ptype is double and PRECISION_DOUBLE is set, which selects the
 // reference's own Z2Z branches (fieldslice.cpp:34,46,68,80).  Its include
 // guard makes the reference's copy a no-op.
