@@ -138,6 +138,25 @@ int run_rings() {
     return 0;
 }
 
+// The state after LoadParameters and init, nothing simulated: the scene, the
+// near-field plane, the sizes and each sphere with the index its material gives
+// at the wavelength (mVector[iMaterial](lambda), as calcSpheres takes it,
+// nearfield.cpp:126-129).
+int run_parse() {
+    put_scene();
+    const nearfieldStruct& nf = SCOPE->nf;
+    g_out["dims"] = {(double)nf.U.R[0], (double)nf.U.R[1], (double)SCOPE->Ud.R[0] / SCOPE->ss, (double)SCOPE->ss,
+                     (double)nf.sVector.size(), (double)nf.nWaves};
+    for (size_t s = 0; s < nf.sVector.size(); s++) {
+        const sphere& S = nf.sVector[s];
+        rts::material<ptype> m = SCOPE->nf.mVector[S.iMaterial];
+        const rts::complex<ptype> n = m(nf.lambda);
+        g_out["sphere" + std::to_string(s) + ".in"] = {(double)S.p[0], (double)S.p[1], (double)S.p[2], (double)S.a,
+                                                        (double)n.real(), (double)n.imag()};
+    }
+    return 0;
+}
+
 // The extended source LoadParameters loaded, and SimulateExtendedSource over it.
 int run_sources() {
     put_scene();
@@ -162,7 +181,8 @@ extern "C" {
 // the detector images; 3 is 0 with the near field back-propagated over the
 // plane position before the band-pass (U and Uf are kept as sumUf left them);
 // 4 runs SimulateExtendedSource over the sources of --extended-source and keeps
-// them (x, y, z, amplitude) and the detector images; 5 ends after sumUf (the
+// them (x, y, z, amplitude) and the detector images; 6 keeps the parsed state
+// only (run_parse); 5 ends after sumUf (the
 // near fields only: with --vector the reference's getFarField copies the y and z
 // components into a crop slice allocated without them, fieldslice.cu:340-361).
 int ref_sim_run(int argc, const char** argv, int stop) {
@@ -179,6 +199,7 @@ int ref_sim_run(int argc, const char** argv, int stop) {
     nearfieldStruct& nf = SCOPE->nf;
     if (stop == 2) return run_rings();
     if (stop == 4) return run_sources();
+    if (stop == 6) return run_parse();
 
     nf.t_Uf = 0;
     nf.t_Us = 0;

@@ -42,7 +42,8 @@ RING_OPTICS = ["--lambda", "3", "--condenser", "0", "0.6", "--objective", "0", "
                "16", "0", "--samples", "20"]
 
 # name: (build, stop: 0 the whole path, 1 after the tables, 2 the ring-source driver, 3 the whole path with
-# the near field back-propagated, 4 the extended-source driver, 5 the near fields only; flags)
+# the near field back-propagated, 4 the extended-source driver, 5 the near fields only; flags; 6, the parse
+# only, is the PARSE table below)
 SCENES = {
     # ptype double: direct (recursive) order sums, the whole path
     "rec_two_spheres": ("f64", 0, TWO + ["--lambda", "3", "--condenser", "0", "0.6", "--objective", "0", "0.6",
@@ -120,6 +121,27 @@ SCENES = {
     "ring3_nearfield": ("f32", 2, TWO + RING_OPTICS + ["--focus", "0.5", "-0.25", "0", "--amplitude", "0.75",
                                                       "--recursive", "--interpolate", "3", "--points-rings", "4",
                                                       "3"]),
+}
+# stop = 6: the reference's parse of its own flags only (LoadParameters and init; nothing simulated), for
+# the CLI grammar: "{dir}/name" is a file of PARSE_FILES written to a temporary directory
+PARSE_FILES = {"s.txt": "1 2 0 1.5 1\n-3 0.5 0.2 2\n0 -4 -1 1.2 0\n",
+               "m1.txt": "3.0 1.40 0.01\n4.0 1.45 0.03\n5.0 1.50 0.02\n",
+               "m2.txt": "# [wavenumber,n,k]\n3000 1.30 0.00\n2000 1.35 0.05\n1500 1.32 0.01\n"}
+PARSE = {
+    "p_defaults": [],
+    "p_k_direction": ["--k", "0.3", "0.5", "--xy", "20", "0", "--resolution", "16"],
+    "p_explicit_plane": ["--plane-lower-left", "-4", "-3", "1", "--plane-upper-right", "4", "5", "1",
+                         "--plane-normal", "0", "0", "1", "--resolution", "16"],
+    "p_single_na": ["--condenser", "0.45", "--objective", "0.7", "--lambda", "2", "--resolution", "16", "--xy", "10"],
+    "p_supersample_rule": ["--xy", "10", "0", "--resolution", "20", "--lambda", "0.3"],
+    "p_sphere_file": ["--sphere-file", "{dir}/s.txt", "--materials", "1.4", "0.05", "1.5", "0.01", "--resolution",
+                      "16", "--xy", "20", "0"],
+    "p_material_files": ["--material-file", "{dir}/m1.txt", "{dir}/m2.txt", "--lambda", "4.2", "--spheres", "0", "0",
+                         "0", "2", "1", "3", "3", "0", "1", "0", "--resolution", "16", "--xy", "20", "0"],
+    "p_nu_xz": ["--nu", "2500", "--xz", "30", "2", "--resolution", "32"],
+    "p_single_n": ["--materials", "1.33", "--spheres", "0", "0", "0", "2", "--resolution", "16"],
+    "p_flags": ["--recursive-us", "--lut-uf", "--plane-wave", "--samples", "123", "--field-order", "17", "--padding",
+                "2", "--amplitude", "0.5", "--focus", "1", "2", "3", "--resolution", "16", "--xy", "12", "1"],
 }
 TABLE_THETA_ROWS = list(range(0, 1000, 37)) + [999]
 
@@ -224,6 +246,28 @@ def main():
                 rec[key] = enc(get(key))
         out[name] = rec
         print(name, b, "R =", int(dims[0]), "res =", int(dims[2]), "ss =", int(dims[3]), "waves =", int(dims[5]))
+    for f, text in PARSE_FILES.items():
+        with open(os.path.join(tmp, f), "w") as fh:
+            fh.write(text)
+    for name, flags in PARSE.items():
+        lib = libs["f32"]
+        argv = ["bimsim"] + [f.replace("{dir}", tmp) for f in flags]
+        arr = (C.c_char_p * len(argv))(*[a.encode() for a in argv])
+        with quiet():
+            assert lib.ref_sim_run(len(argv), arr, 6) == 0, name
+
+        def get(key):
+            n = lib.ref_sim_size(key.encode())
+            v = np.zeros(n)
+            lib.ref_sim_get(key.encode(), v.ctypes.data_as(C.c_void_p))
+            return v
+
+        dims = get("dims")
+        out[name] = {"build": "f32", "flags": flags, "stop": 6, "dims": dims.tolist(), "scene": get("scene").tolist(),
+                     "nf_quad": get("nf_quad").tolist(), "files": {f: PARSE_FILES[f] for f in PARSE_FILES
+                                                                   if "{dir}/" + f in flags},
+                     "spheres": [{"in": get(f"sphere{s}.in").tolist()} for s in range(int(dims[4]))]}
+        print(name, "parsed: R =", int(dims[0]), "spheres =", int(dims[4]))
     with open(os.path.join(HERE, "ref_sim.json"), "w") as fh:
         json.dump(out, fh, separators=(",", ":"))
     print("wrote ref_sim.json", os.path.getsize(os.path.join(HERE, "ref_sim.json")), "bytes")

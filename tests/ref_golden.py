@@ -26,27 +26,48 @@ def arr(b64):
     return np.frombuffer(base64.b64decode(b64), dtype="<f8").copy()
 
 
+def values(flags, name):
+    """The single-precision values that follow --name, up to the next flag."""
+    i = flags.index("--" + name) + 1
+    out = []
+    while i < len(flags) and not flags[i].startswith("--"):
+        out.append(float(np.float32(flags[i])))
+        i += 1
+    return out
+
+
 def flag(flags, name, n):
-    i = flags.index("--" + name)
-    return [float(np.float32(v)) for v in flags[i + 1:i + 1 + n]]
+    return values(flags, name)[:n]
 
 
 def plane(flags):
-    """(pmin, pmax, normal) as lImagePlane builds them in single precision (arguments.h:340-407)."""
+    """(pmin, pmax, normal) as lImagePlane builds them in single precision (arguments.h:340-407): an
+    axis-aligned plane of size s (default 40) at a position (default 0), else the explicit corners and
+    normal (defaults (-5, 0, -5), (5, 0, 5), (0, 1, 0))."""
     f = np.float32
+    for name in ("xy", "xz", "yz"):
+        if "--" + name in flags:
+            v = values(flags, name)
+            s = v[0] if v else 40.0
+            pos = v[1] if len(v) > 1 else 0.0
+            h = float(f(s) / f(2))
+            if name == "xy":
+                return (-h, -h, pos), (h, h, pos), (0.0, 0.0, 1.0)
+            if name == "xz":
+                return (-h, pos, -h), (h, pos, h), (0.0, -1.0, 0.0)
+            return (pos, -h, -h), (pos, h, h), (1.0, 0.0, 0.0)
+
+    def vec(name, default):
+        return tuple(values(flags, name)) if "--" + name in flags else tuple(float(f(v)) for v in default)
+    return vec("plane-lower-left", (-5, 0, -5)), vec("plane-upper-right", (5, 0, 5)), vec("plane-normal", (0, 1, 0))
+
+
+def plane_size(flags):
+    """s of the supersampling rule: the --xy size, else 40 (arguments.h:346-418)."""
     if "--xy" in flags:
-        s, z = flag(flags, "xy", 2)
-        h = float(f(s) / f(2))
-        return (-h, -h, z), (h, h, z), (0.0, 0.0, 1.0)
-    if "--xz" in flags:
-        s, y = flag(flags, "xz", 2)
-        h = float(f(s) / f(2))
-        return (-h, y, -h), (h, y, h), (0.0, -1.0, 0.0)
-    if "--yz" in flags:
-        s, x = flag(flags, "yz", 2)
-        h = float(f(s) / f(2))
-        return (x, -h, -h), (x, h, h), (1.0, 0.0, 0.0)
-    raise ValueError("scene without an axis-aligned plane flag")
+        v = values(flags, "xy")
+        return v[0] if v else 40.0
+    return 40.0
 
 
 def params(rec):
@@ -99,8 +120,22 @@ def plane_position(rec):
     """z_d, the propagation distance: the plane position of --xy/--xz/--yz as a float (arguments.h:346-409)."""
     for name in ("xy", "xz", "yz"):
         if "--" + name in rec["flags"]:
-            return flag(rec["flags"], name, 2)[1]
-    raise ValueError("scene without an axis-aligned plane flag")
+            v = values(rec["flags"], name)
+            return v[1] if len(v) > 1 else 0.0
+    return 0.0
+
+
+def parse_scenes():
+    """The reference's parse of its own flags, nothing simulated (CLI grammar cases)."""
+    return sorted(n for n, r in load().items() if r["stop"] == 6)
+
+
+def flags_with_files(rec, directory):
+    """The record's flags with its files written into `directory` ("{dir}" replaced)."""
+    for name, text in rec.get("files", {}).items():
+        with open(os.path.join(str(directory), name), "w") as fh:
+            fh.write(text)
+    return [f.replace("{dir}", str(directory)) for f in rec["flags"]]
 
 
 def source_scenes():

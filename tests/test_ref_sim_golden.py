@@ -195,7 +195,8 @@ def test_sphere_tables_match_the_reference_run(name):
         assert rel(mine_u, ref_u) <= TOL_F64 and rel(mine_i, ref_i) <= TOL_F64
 
 
-@pytest.mark.parametrize("name", rg.scenes() + rg.scenes(full=False) + rg.ring_scenes() + rg.backprop_scenes())
+@pytest.mark.parametrize("name", rg.scenes() + rg.scenes(full=False) + rg.ring_scenes() + rg.backprop_scenes() +
+                         rg.parse_scenes())
 def test_parsed_geometry_matches(name):
     """The near-field quad nf.pos and the derived sizes are the oracle's (arguments.h:340-438,
     microscope.cu:700-718); --nu gives lambda = 1e4/nu in single precision (arguments.h:118-123)."""
@@ -206,7 +207,7 @@ def test_parsed_geometry_matches(name):
     assert (g.R, g.det_res) == (int(rec["dims"][0]), int(rec["dims"][2]))
     # ss from the plane size, which only --xy sets (40 otherwise; arguments.h:346-418)
     fl = rec["flags"]
-    kw = {"xy": tuple(rg.flag(fl, "xy", 2))} if "--xy" in fl else {"plane": rg.plane(fl)}
+    kw = {"xy": (rg.plane_size(fl), rg.plane_position(rec))} if "--xy" in fl else {"plane": rg.plane(fl)}
     assert int(rec["scene"][13]) == abi.make_params(lam=p.lambda_, resolution=p.resolution, **kw).supersample
     if "--nu" in rec["flags"]:
         nu = np.float32(rec["flags"][rec["flags"].index("--nu") + 1])
@@ -226,8 +227,8 @@ def test_reference_directions_are_the_compat_sampler(name):
     np.testing.assert_allclose(out, rg.waves(rec).ravel(), rtol=0, atol=2e-7)
 
 
-@pytest.mark.parametrize("name", rg.scenes("f32"))
-def test_cli_parses_the_references_flags_into_its_state(name):
+@pytest.mark.parametrize("name", rg.scenes("f32") + rg.parse_scenes())
+def test_cli_parses_the_references_flags_into_its_state(name, tmp_path):
     """The `bimsim` CLI of this project, given the reference's flags, derives the state the
     shipped reference held after LoadParameters (single-precision values)."""
     import json
@@ -239,7 +240,7 @@ def test_cli_parses_the_references_flags_into_its_state(name):
         from bimsim_gb300 import build
         build.build()
     rec = rg.load()[name]
-    r = subprocess.run([exe, "--dry-run"] + rec["flags"], capture_output=True, text=True)
+    r = subprocess.run([exe, "--dry-run"] + rg.flags_with_files(rec, tmp_path), capture_output=True, text=True)
     assert r.returncode == 0, r.stdout + r.stderr
     d = json.loads(r.stdout.strip().splitlines()[-1])
     sc = rec["scene"]
@@ -250,5 +251,9 @@ def test_cli_parses_the_references_flags_into_its_state(name):
     assert (d["padding"], d["supersample"], d["field_order"]) == (int(sc[12]), int(sc[13]), int(sc[14]))
     assert (d["lut_us"], d["lut_uf"], d["plane_wave"], d["samples"]) == tuple(int(v) for v in sc[15:19])
     assert d["resolution"] == int(rec["dims"][2])
+    assert len(d["spheres"]) == len(rec["spheres"])
     for mine, theirs in zip(d["spheres"], rec["spheres"]):
         assert [f(v) for v in mine] == [f(v) for v in theirs["in"]]
+    pmin, pmax, nrm = rg.plane(rec["flags"])
+    assert [f(v) for v in d["plane_min"]] == list(pmin) and [f(v) for v in d["plane_max"]] == list(pmax)
+    assert [f(v) for v in d["normal"]] == list(nrm)
