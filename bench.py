@@ -192,21 +192,27 @@ def run_served(args):
             srv.wait(t, 900.0)
             srv.fetch(t)
         wall_mixed = time.perf_counter() - t0
-    t0 = time.perf_counter()
-    for _, p, s, w in sub:
-        with Context(p) as c:
-            c.set_spheres(s)
-            c.set_waves(w)
-            c.simulate(BS_PREC_FP64)
-            c.image(BS_IMG_INTENSITY)
-    wall_fp64 = time.perf_counter() - t0
+    def sequential(prec):
+        t0 = time.perf_counter()
+        for _, p, s, w in sub:
+            with Context(p) as c:
+                c.set_spheres(s)
+                c.set_waves(w)
+                c.simulate(prec)
+                c.image(BS_IMG_INTENSITY)
+        return time.perf_counter() - t0
+    wall_mixed_seq = sequential(BS_PREC_MIXED)
+    wall_fp64 = sequential(BS_PREC_FP64)
     out["same_requests_vs_fp64"] = {
         "requests": idx, "resolutions": sorted({p.resolution for _, p, _, _ in sub}),
         "nf_pixels": sub_pixels, "served_mixed_wall_s": wall_mixed, "fp64_sequential_wall_s": wall_fp64,
         "served_mixed_pixels_per_s": sub_pixels / wall_mixed, "fp64_sequential_pixels_per_s": sub_pixels / wall_fp64,
         "speedup": wall_fp64 / wall_mixed, "target": 10.0,
+        "mixed_sequential_wall_s": wall_mixed_seq, "served_vs_sequential_mixed": wall_mixed_seq / wall_mixed,
         "note": "measured: the requests of the trace of at most 1e11 lookups, in trace order up to 4e11 in all; "
-                "mixed through the server (all submitted at once), FP64 one fresh context per request in turn"}
+                "mixed through the server (all submitted at once), FP64 one fresh context per request in turn; "
+                "mixed_sequential_wall_s: the same mixed requests one fresh context at a time, so "
+                "served_vs_sequential_mixed is what running them side by side on the workers' streams gains"}
     return out
 
 
