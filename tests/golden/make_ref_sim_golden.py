@@ -89,6 +89,9 @@ SCENES = {
     "lut_supersample_nu": ("f32", 0, ["--spheres", "0.23", "0.11", "0", "1.03", "0", "--materials", "1.4", "0.05",
                                       "--nu", "6666.667", "--condenser", "0", "0.5", "--objective", "0", "0.5",
                                       "--resolution", "6", "--xy", "6", "0", "--samples", "16"]),
+    "vec_lut_uf_f32": ("f32", 5, TWO + ["--lambda", "3", "--condenser", "0", "0.6", "--objective", "0", "0.6",
+                                       "--resolution", "12", "--xy", "16", "0", "--samples", "20", "--vector",
+                                       "--lut-uf"]),
     "lut_plane_wave": ("f32", 0, TWO + ["--lambda", "3", "--objective", "0", "0.6", "--resolution", "12", "--xy",
                                        "16", "0", "--amplitude", "1.5", "--plane-wave"]),
     "lut_padding0": ("f32", 0, TWO + ["--lambda", "3", "--condenser", "0", "0.6", "--objective", "0", "0.6",

@@ -93,6 +93,9 @@ def test_gpu_vector_stub_near_fields_match_the_references_run(name):
             ctx.set_waves(rg.waves(rec))
             ctx.simulate(prec)
             out = {"U": ctx.field(BS_FIELD_TOTAL), "Uf": ctx.field(BS_FIELD_INCIDENT)}
+        if not any(np.any(rg.field(rec, k)) for k in out):  # --lut-uf: the stub's fields are empty
+            assert not any(np.any(v) for v in out.values())
+            continue
         e = errors(out, rec)
         if rec["build"] == "f64" and prec == BS_PREC_FP64:
             assert max(e.values()) <= 1e-10, e

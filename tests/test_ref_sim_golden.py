@@ -72,8 +72,12 @@ def test_oracle_vector_stub_near_fields_match_the_reference_run(name):
     assert "--vector" in rec["flags"]
     p, (U, Uf, _, _) = oracle_run(rec)
     tol = TOL_F64 if rec["build"] == "f64" else TOL_F32
-    errs = {"U": rel(U, rg.field(rec, "U")), "Uf": rel(Uf, rg.field(rec, "Uf"))}
-    assert max(errs.values()) <= tol, errs
+    for mine, key in ((U, "U"), (Uf, "Uf")):
+        ref = rg.field(rec, key)
+        if not np.any(ref):  # with --lut-uf the stub's incident field is empty (nfVectorUfLut.cu:7-10)
+            assert not np.any(mine), key
+        else:
+            assert rel(mine, ref) <= tol, (key, rel(mine, ref))
 
 
 @pytest.mark.parametrize("name", rg.backprop_scenes())
