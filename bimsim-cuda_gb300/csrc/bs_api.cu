@@ -748,7 +748,8 @@ static std::vector<float4> wave_cones(const std::vector<double>& w, int chunk) {
 // kernel 383 ms): staged kernel with 23 % of windows staged 395 ms, 41 %
 // 360 ms, 85 % 329 ms; at 3072^2, 98 % staged 772 ms against 1510 ms.
 constexpr double STAGED_KERNEL_MIN_FRACTION = 0.3;
-static double predict_staged_fraction(const bs_ctx* c, const std::vector<float4>& cones, int s0, int s1) {
+static double predict_staged_fraction(const bs_ctx* c, const std::vector<float4>& cones, int s0, int s1, int chunk) {
+    const int cap = lut_stage_entries(chunk);
     const Scene& sc = c->sc;
     const int R = sc.R, tiles = (R + LUT_TILE - 1) / LUT_TILE;
     const int ts = std::max(1, tiles / 16), ss = std::max(1, (s1 - s0) / 32);
@@ -808,7 +809,7 @@ static double predict_staged_fraction(const bs_ctx* c, const std::vector<float4>
                     const int t_lo = std::max(0, (int)std::floor((thc - k.w - gam) * tsc) - 1);
                     const int t_hi = std::min(S.thetaR, (int)std::floor((thc + k.w + gam) * tsc) + 2);
                     const int W = t_hi - t_lo + 1;
-                    if (W >= 2 && (long long)nrows * lut_stage_stride(W) <= LUT_STAGE_ENTRIES) staged++;
+                    if (W >= 2 && (long long)nrows * lut_stage_stride(W) <= cap) staged++;
                 }
             }
         }
@@ -836,7 +837,7 @@ static ChunkPlan choose_chunk(const bs_ctx* c, const std::vector<double>& waves,
         best.w = waves;
         sort_waves(best.w, best.chunk);
         best.cones = wave_cones(best.w, best.chunk);
-        best.predicted = predict_staged_fraction(c, best.cones, 0, ns);
+        best.predicted = predict_staged_fraction(c, best.cones, 0, ns, best.chunk);
         return best;
     }
     for (int cand : {WAVE_CHUNK_MAX, WAVE_CHUNK_MAX / 2, WAVE_CHUNK_MAX / 4}) {
@@ -845,7 +846,7 @@ static ChunkPlan choose_chunk(const bs_ctx* c, const std::vector<double>& waves,
         cp.w = waves;
         sort_waves(cp.w, cand);
         cp.cones = wave_cones(cp.w, cand);
-        cp.predicted = predict_staged_fraction(c, cp.cones, 0, ns);
+        cp.predicted = predict_staged_fraction(c, cp.cones, 0, ns, cand);
         if (cand == WAVE_CHUNK_MAX) {
             first = cp;
             if (c->lut_staging == 2) return first;
@@ -1039,7 +1040,7 @@ static bs_status run_nearfield(bs_ctx* c) {
             CK(c->d_texobj.ensure((size_t)4 * max_chunk * sizeof(unsigned long long)));
             if (cones.empty()) {
                 cones = wave_cones(w, chunk);
-                predicted = predict_staged_fraction(c, cones, 0, ns);
+                predicted = predict_staged_fraction(c, cones, 0, ns, chunk);
             }
             c->stats.lut_staged_predicted = predicted;
             use_stage = c->lut_staging == 1 ||

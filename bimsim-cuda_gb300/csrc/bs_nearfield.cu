@@ -416,7 +416,7 @@ __global__ void __launch_bounds__(128) us_lut_f64_kernel(Scene sc, const Sphere*
 // gamma of the tile-centre direction r_c, every lookup angle of a chunk lies
 // in angle(c_k, r_c) +- (beta_k + gamma) (triangle inequality on the sphere of
 // directions).  The table values of the tile's rows times that angular window
-// (float2, at most UST_STAGE of them) are copied to shared memory once per
+// (float2, at most lut_stage_entries(chunk) of them) are copied to shared memory once per
 // chunk and the bilinear cells are read from there.  Chunks whose window does
 // not fit, and tiles touching or containing the sphere, read the cells through
 // the texture path instead: the tables also live in CUDA arrays (block-linear
@@ -500,7 +500,6 @@ __device__ __forceinline__ float2 f2_unpack(f32x2 v) {
 
 __device__ __forceinline__ void copy_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 constexpr int UST_CHUNK = WAVE_CHUNK_MAX;  // shared arrays; the run's chunk may be smaller
-constexpr int UST_STAGE = LUT_STAGE_ENTRIES;
 constexpr float UST_MARGIN = LUT_STAGE_MARGIN;
 
 // Block-uniform values of one (tile, sphere) pair, kept in shared memory so
@@ -519,14 +518,14 @@ struct TileSphere {
 // first column and width, width 0 when the block does not stage this sphere or
 // the window does not fit.  Columns go up to thetaR: the linear rows carry a
 // copy of the last column there.
-__device__ __forceinline__ int2 chunk_plan(const float4 cone, const TileSphere& ts) {
+__device__ __forceinline__ int2 chunk_plan(const float4 cone, const TileSphere& ts, int stage_cap) {
     if (ts.nrows == 0) return make_int2(0, 0);
     const float tsc = ts.tsc, gam = ts.gam;
     const float thc = acosf(fminf(fmaxf(cone.x * ts.cx + cone.y * ts.cy + cone.z * ts.cz, -1.f), 1.f));
     const int t_lo = max(0, (int)floorf((thc - cone.w - gam) * tsc) - 1);
     const int t_hi = min(ts.thetaR, (int)floorf((thc + cone.w + gam) * tsc) + 2);
     int W = t_hi - t_lo + 1;
-    if (W < 2 || ts.nrows * lut_stage_stride(W) > UST_STAGE) W = 0;
+    if (W < 2 || ts.nrows * lut_stage_stride(W) > stage_cap) W = 0;
     return make_int2(t_lo, W);
 }
 
@@ -535,6 +534,7 @@ __device__ __forceinline__ int2 chunk_plan(const float4 cone, const TileSphere& 
 // thread: the tile's eight 4 x 8 warp blocks are spread over 8 / PPT warps, and
 // each wave's direction and phase (shared-memory broadcasts) are read once for
 // the thread's PPT pixels.  Every pixel's arithmetic is the same for any PPT.
+// stage_cap: float2 entries of the dynamic shared memory (lut_stage_entries).
 template <bool STAGE, int PPT>
 __global__ void __launch_bounds__(UST_TILE / PPT, STAGE ? 4 : 6) us_lut_tex_kernel(Scene sc, const Sphere* __restrict__ sph, int s0, int s1,
                                                                     int accumulate, int finalize,
@@ -546,7 +546,8 @@ __global__ void __launch_bounds__(UST_TILE / PPT, STAGE ? 4 : 6) us_lut_tex_kern
                                                                     const cpx<float>* __restrict__ Uf,
                                                                     cpx<float>* __restrict__ U,
                                                                     unsigned long long* __restrict__ counters,
-                                                                    float2* __restrict__ kcmp, int chunk) {
+                                                                    float2* __restrict__ kcmp, int chunk,
+                                                                    int stage_cap) {
     constexpr int NT = UST_TILE / PPT, NWARP = NT / 32;
     static_assert(NT >= UST_CHUNK && NT % 32 == 0, "one thread per wave of a chunk");
     extern __shared__ float2 s_stage[];
@@ -694,7 +695,7 @@ __global__ void __launch_bounds__(UST_TILE / PPT, STAGE ? 4 : 6) us_lut_tex_kern
                 s_ts.thetaR = S.thetaR;
                 s_ts.lin_stride = S.lin_stride;
                 s_ts.off = S.usp_off;
-                s_plan = chunk_plan(cones[0], s_ts);
+                s_plan = chunk_plan(cones[0], s_ts, stage_cap);
             }
         }
         // local rows of each pixel in the staged block (clamped, so always in bounds)
@@ -731,7 +732,7 @@ __global__ void __launch_bounds__(UST_TILE / PPT, STAGE ? 4 : 6) us_lut_tex_kern
             }
             copy_async_wait_all();
             __syncthreads();
-            if (STAGE && threadIdx.x == 0 && ch + 1 < nchunks) s_plan = chunk_plan(cones[ch + 1], s_ts);
+            if (STAGE && threadIdx.x == 0 && ch + 1 < nchunks) s_plan = chunk_plan(cones[ch + 1], s_ts, stage_cap);
             // t < thetaR - 1 + 1e-3 (PI_REF < pi): the last column is repeated in the staged rows and
             // clamped in the texture planes, so t past thetaR - 1 reads the last column, as a clamp would
             const float tsc = s_ts.tsc, tscpi = s_ts.tscpi;
@@ -1194,17 +1195,17 @@ void launch_us_lut_tex(const Scene& sc, const Sphere* sph, int s0, int s1, int a
     if (!stage) {
         us_lut_tex_kernel<false, 1><<<(unsigned)tiles * tiles, UST_TILE, 0, st>>>(sc, sph, s0, s1, accumulate, finalize,
                                                                                  kw4, cones, ph, tex, lin, Uf, U,
-                                                                                 counters, kcmp, chunk);
+                                                                                 counters, kcmp, chunk, 0);
         return;
     }
-    const int smem = UST_STAGE * (int)sizeof(float2);
-    // per device and cheap; a failure shows up as the launch error
     const bool two = chunk >= UST_TWO_PIXEL_MIN_CHUNK;
+    const int cap = lut_stage_entries(chunk), smem = cap * (int)sizeof(float2);
+    // per device and cheap; a failure shows up as the launch error
     auto kernel = two ? us_lut_tex_kernel<true, 2> : us_lut_tex_kernel<true, 1>;
     cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     kernel<<<(unsigned)tiles * tiles, two ? UST_TILE / 2 : UST_TILE, smem, st>>>(sc, sph, s0, s1, accumulate, finalize,
                                                                                kw4, cones, ph, tex, lin, Uf, U,
-                                                                               counters, kcmp, chunk);
+                                                                               counters, kcmp, chunk, cap);
 }
 
 void launch_lut_build_tex_batch(const LutBuildJob* jobs, int njobs, int max_rows, int max_theta, const zd* tab,
