@@ -536,7 +536,7 @@ __device__ __forceinline__ int2 chunk_plan(const float4 cone, const TileSphere& 
 // the thread's PPT pixels.  Every pixel's arithmetic is the same for any PPT.
 // stage_cap: float2 entries of the dynamic shared memory (lut_stage_entries).
 template <bool STAGE, int PPT>
-__global__ void __launch_bounds__(UST_TILE / PPT, STAGE ? 4 : 6) us_lut_tex_kernel(Scene sc, const Sphere* __restrict__ sph, int s0, int s1,
+__global__ void __launch_bounds__(UST_TILE / PPT, STAGE ? (PPT == 1 ? 3 : 4) : 5) us_lut_tex_kernel(Scene sc, const Sphere* __restrict__ sph, int s0, int s1,
                                                                     int accumulate, int finalize,
                                                                     const float4* __restrict__ kw4,
                                                                     const float4* __restrict__ cones,
