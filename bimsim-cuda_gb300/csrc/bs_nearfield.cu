@@ -535,8 +535,12 @@ __device__ __forceinline__ int2 chunk_plan(const float4 cone, const TileSphere& 
 // each wave's direction and phase (shared-memory broadcasts) are read once for
 // the thread's PPT pixels.  Every pixel's arithmetic is the same for any PPT.
 // stage_cap: float2 entries of the dynamic shared memory (lut_stage_entries).
+// Blocks per SM: the one-pixel staged kernel runs 3 (its 72 KB stage) and may
+// take 80 registers (config 3 262 against 266 ms per band at 64); the two-pixel
+// one 4; the texture-only one 6 (5, at 48 registers without spills, measured
+// no faster).
 template <bool STAGE, int PPT>
-__global__ void __launch_bounds__(UST_TILE / PPT, STAGE ? (PPT == 1 ? 3 : 4) : 5) us_lut_tex_kernel(Scene sc, const Sphere* __restrict__ sph, int s0, int s1,
+__global__ void __launch_bounds__(UST_TILE / PPT, STAGE ? (PPT == 1 ? 3 : 4) : 6) us_lut_tex_kernel(Scene sc, const Sphere* __restrict__ sph, int s0, int s1,
                                                                     int accumulate, int finalize,
                                                                     const float4* __restrict__ kw4,
                                                                     const float4* __restrict__ cones,
