@@ -16,13 +16,14 @@ constexpr int WAVE_CHUNK_MAX = 64;
 
 // Mixed LUT kernel staging: float2 table values a 16 x 16 pixel tile stages
 // per wave chunk, and the angle margin (radians) added to its window bounds.
-// 64-wave chunks (two pixels per thread, 128 registers): 43 KB, 4 blocks per
-// SM; 32- and 16-wave chunks (one pixel per thread, coarser pixel pitches):
-// 72 KB, 3 blocks per SM, so that wider windows fit -- config 3 266 against
-// 305 ms per band, config 5 at 512^2 9.9 against 11.7 s, both with 32-wave
-// chunks where 43 KB windows needed 16.
+// 64-wave chunks (two pixels per thread, 128 registers): 51 KB, 4 blocks per
+// SM (config 2: 99.6 % of windows staged; 43 KB: 98 %, 730 against 721 ms);
+// 32- and 16-wave chunks (one pixel per thread, coarser pixel pitches): 72 KB,
+// 3 blocks per SM, so that wider windows fit -- config 3 266 against 305 ms
+// per band, config 5 at 512^2 9.9 against 11.7 s, both with 32-wave chunks
+// where 43 KB windows needed 16.
 constexpr int LUT_TILE = 16;
-__host__ __device__ constexpr int lut_stage_entries(int chunk) { return chunk >= 64 ? 5400 : 9000; }
+__host__ __device__ constexpr int lut_stage_entries(int chunk) { return chunk >= 64 ? 6400 : 9000; }
 constexpr float LUT_STAGE_MARGIN = 2e-3f;
 // Shared-memory row stride of a staged window W entries wide: odd, so that
 // lanes reading the same column of different rows fall in different banks.
