@@ -756,7 +756,9 @@ __global__ void __launch_bounds__(UST_TILE / PPT, STAGE ? (PPT == 1 ? 3 : 4) : 6
                     alp[j] = f2_splat(al[j]);
                     ax[j] = ay[j] = 0ull;
                 }
-#pragma unroll(8 / PPT)
+                // 32 lookups per thread per unrolled step (config 2: 697 ms; 8: 721 ms, 16: 700 ms,
+                // 64: 792 ms)
+#pragma unroll(32 / PPT)
                 for (int w = 0; w < nw; w++) {
                     const float4 kk = s_k[w];
                     const float2 pw = s_p[w];
