@@ -747,7 +747,13 @@ static std::vector<float4> wave_cones(const std::vector<double>& w, int chunk) {
 // Measured on the config-2 scene at 1536^2 near-field pixels (texture-only
 // kernel 383 ms): staged kernel with 23 % of windows staged 395 ms, 41 %
 // 360 ms, 85 % 329 ms; at 3072^2, 98 % staged 772 ms against 1510 ms.
-constexpr double STAGED_KERNEL_MIN_FRACTION = 0.3;
+// The fraction of windows the staged kernel must fit to beat the texture-only
+// one: its texture fallback runs with the L1 that its shared-memory stage
+// leaves -- 64-wave chunks (51 KB x 4 blocks per SM): 0.3; smaller chunks
+// (72 KB x 3 blocks): 0.7 (served 256^2 - 512^2 requests with 48-62 % of
+// windows staged took 169-320 ms staged against 123-273 ms texture-only;
+// config 3 at 71 % 326 against 383 ms).
+static double staged_min_fraction(int chunk) { return chunk >= WAVE_CHUNK_MAX ? 0.3 : 0.7; }
 static double predict_staged_fraction(const bs_ctx* c, const std::vector<float4>& cones, int s0, int s1, int chunk) {
     const int cap = lut_stage_entries(chunk);
     const Scene& sc = c->sc;
@@ -818,10 +824,11 @@ static double predict_staged_fraction(const bs_ctx* c, const std::vector<float4>
 
 // Waves per chunk for the mixed LUT kernel, with the matching wave order and
 // cones: the largest of 64, 32 and 16 whose predicted staged fraction reaches
-// 0.8, else the one with the largest fraction.  Smaller chunks have narrower
-// cones, so more windows fit, but each chunk pays a window copy, two barriers
-// and a Kahan step.  64 whenever the texture-only kernel will run;
-// bs_set_lut_wave_chunk fixes the chunk instead.
+// 0.8, else the one with the largest fraction if that reaches its
+// staged_min_fraction, else the largest fraction among those that reach
+// theirs.  Smaller chunks have narrower cones, so more windows fit, but each
+// chunk pays a window copy, two barriers and a Kahan step.  64 whenever the
+// texture-only kernel will run; bs_set_lut_wave_chunk fixes the chunk instead.
 struct ChunkPlan {
     int chunk = WAVE_CHUNK_MAX;
     std::vector<double> w;
@@ -830,8 +837,8 @@ struct ChunkPlan {
 };
 
 static ChunkPlan choose_chunk(const bs_ctx* c, const std::vector<double>& waves, int ns) {
-    ChunkPlan first, best;
-    best.predicted = -1;
+    ChunkPlan first, best, viable;  // viable: the best that the staged kernel would run to advantage
+    best.predicted = viable.predicted = -1;
     if (c->lut_chunk) {
         best.chunk = c->lut_chunk;
         best.w = waves;
@@ -852,12 +859,13 @@ static ChunkPlan choose_chunk(const bs_ctx* c, const std::vector<double>& waves,
             if (c->lut_staging == 2) return first;
         }
         const bool enough = cp.predicted >= 0.8;
+        if (cp.predicted >= staged_min_fraction(cand) && cp.predicted > viable.predicted) viable = cp;
         if (cp.predicted > best.predicted || enough) best = std::move(cp);
         if (enough) break;
     }
-    if (c->lut_staging == 0 && best.predicted < STAGED_KERNEL_MIN_FRACTION) {
-        first.predicted = best.predicted;  // the texture-only kernel runs; report the best staging model
-        return first;
+    if (c->lut_staging == 0 && best.predicted < staged_min_fraction(best.chunk)) {
+        if (viable.predicted >= 0) return viable;
+        return first;  // 64-wave chunks below their threshold too: the texture-only kernel runs
     }
     return best;
 }
@@ -1044,7 +1052,7 @@ static bs_status run_nearfield(bs_ctx* c) {
             }
             c->stats.lut_staged_predicted = predicted;
             use_stage = c->lut_staging == 1 ||
-                        (c->lut_staging == 0 && c->stats.lut_staged_predicted >= STAGED_KERNEL_MIN_FRACTION);
+                        (c->lut_staging == 0 && c->stats.lut_staged_predicted >= staged_min_fraction(chunk));
             CK(c->d_cones.ensure(cones.size() * sizeof(float4)));
             CK(cudaMemcpyAsync(c->d_cones.p, cones.data(), cones.size() * sizeof(float4), cudaMemcpyHostToDevice,
                                c->st));

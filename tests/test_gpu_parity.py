@@ -217,7 +217,8 @@ def test_kernel_choice_model_tracks_the_staged_fraction():
     measured = st.lut_chunks_staged / st.lut_chunks_total
     assert abs(st.lut_staged_predicted - measured) < 0.2, (st.lut_staged_predicted, measured)
     auto = run_gpu("lut_staged", BS_PREC_MIXED)["stats"]
-    assert (auto.lut_chunks_staged > 0) == (auto.lut_staged_predicted >= 0.3)
+    threshold = 0.3 if auto.lut_wave_chunk >= 64 else 0.7  # the staged kernel's break-even fraction per chunk
+    assert (auto.lut_chunks_staged > 0) == (auto.lut_staged_predicted >= threshold)
 
 
 def test_mixed_rejects_tables_beyond_the_texture_limit():
