@@ -428,9 +428,10 @@ __global__ void __launch_bounds__(128) us_lut_f64_kernel(Scene sc, const Sphere*
 constexpr int UST_TILE = 256;           // 16 x 16 pixel tile
 // Pixels per thread of the staged kernel.  With 64-wave chunks two pixels per thread (128 threads
 // at 128 registers, 4 blocks per SM) are fastest: 730 ms on the 1024^2, 50-sphere slice against
-// 755 ms for one pixel (four: 19 % slower; two at 96 registers and 5 blocks per SM: 11 %).  With
-// 16-wave chunks the per-chunk barriers and window copies weigh more and one pixel per thread on
-// 8 warps is faster (512^2 slice at 3x the table rows per tile: 307 against 366 ms).
+// 755 ms for one pixel (four: 19 % slower; two at 96 registers and 5 blocks per SM: 11 %), 697 ms
+// with 51 KB windows and the wave loop unrolled 16 deep.  With 16- and 32-wave chunks the
+// per-chunk barriers and window copies weigh more and one pixel per thread on 8 warps is faster
+// (512^2 slice at 3x the table rows per tile: 307 against 366 ms with 16-wave chunks).
 constexpr int UST_TWO_PIXEL_MIN_CHUNK = 64;
 
 // Fractional LUT angle index t = acos(c) tsc for c in [-1, 1] (c is clamped),
