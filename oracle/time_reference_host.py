@@ -1,4 +1,5 @@
-"""Time the reference's own host special-function work, single-threaded, as its executable runs it.
+"""TEST INFRASTRUCTURE (a measurement of the reference, not product code): time the reference's own
+host special-function work, single-threaded, as its executable runs it.
 
     make -C oracle ref REF_DIR=<reference checkout>
     python oracle/time_reference_host.py
