@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <mutex>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -242,6 +243,19 @@ void set_last_error(const char* msg) { g_err = msg; }
 
 extern "C" {
 
+// Every kernel loaded on the context's device before its first run (once per
+// device and process; see preload_nearfield_kernels).
+static void preload_kernels(int device) {
+    static std::mutex mu;
+    static std::vector<int> done;
+    std::lock_guard<std::mutex> lock(mu);
+    if (std::find(done.begin(), done.end(), device) != done.end()) return;
+    preload_nearfield_kernels();
+    preload_detector_kernels();
+    cudaGetLastError();  // a kernel this device cannot load reports at its launch instead
+    done.push_back(device);
+}
+
 bs_status bs_create(const bs_params* params, bs_ctx** out) {
     if (!params || !out) return fail(BS_ERR_ARG, "bs_create: null argument");
     std::string why;
@@ -249,6 +263,7 @@ bs_status bs_create(const bs_params* params, bs_ctx** out) {
     bs_ctx* c = new bs_ctx();
     c->prm = *params;
     cudaError_t e = cudaGetDevice(&c->device);
+    if (e == cudaSuccess) preload_kernels(c->device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking);
     for (int i = 0; i < 6 && e == cudaSuccess; i++) e = cudaEventCreate(&c->ev[i]);
     for (DevBuf* b : ctx_bufs(c)) b->st = &c->st;

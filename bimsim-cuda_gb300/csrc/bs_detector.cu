@@ -400,6 +400,28 @@ void launch_cmul(int n, const cpx<T>* a, cpx<T>* x, cudaStream_t st) {
     if (n > 0) cmul_kernel<T><<<(n + 255) / 256, 256, 0, st>>>(n, a, x);
 }
 
+// Loads every kernel of this file (cudaFuncGetAttributes), see preload_kernels.
+template <class T>
+static void preload_detector_t() {
+    cudaFuncAttributes a;
+    cudaFuncGetAttributes(&a, twiddle_kernel<T>);
+    cudaFuncGetAttributes(&a, cgemm_kernel<T>);
+    cudaFuncGetAttributes(&a, cgemm_reduce_kernel<T>);
+    cudaFuncGetAttributes(&a, bin_kernel<T>);
+    cudaFuncGetAttributes(&a, image_kernel<T>);
+    cudaFuncGetAttributes(&a, rotate_add_images_kernel<T>);
+    cudaFuncGetAttributes(&a, ring_line_kernel<T>);
+    cudaFuncGetAttributes(&a, line_image_kernel<T>);
+    cudaFuncGetAttributes(&a, cmul_kernel<T>);
+}
+void preload_detector_kernels() {
+    preload_detector_t<float>();
+    preload_detector_t<double>();
+    cudaFuncAttributes a;
+    cudaFuncGetAttributes(&a, kk_kernel_g);
+    cudaFuncGetAttributes(&a, kk_kernel_conv);
+}
+
 #define BS_DET_INST(T)                                                                                          \
     template void launch_twiddle<T>(int, int, const int*, int, int, int, int, int, cpx<T>*, cudaStream_t);      \
     template void launch_cgemm<T>(int, int, int, int, const cpx<T>*, int, long long, const cpx<T>*, int,       \

@@ -33,6 +33,14 @@ template <class T>
 struct cpx;
 using zd = cpx<double>;
 
+// Load every kernel of the library into the current device's context now: with
+// CUDA's default lazy loading a kernel is loaded at its first launch, and a load
+// while other streams' kernels run waits for them (a served request that was the
+// first to use a kernel waited for the long slices on the other workers' streams:
+// p50 8.3 s against 1.9 s with every kernel loaded up front).
+void preload_nearfield_kernels();
+void preload_detector_kernels();
+
 // One bilinear LUT cell at (r, t): {T00, T10 - T00, T01 - T00, T11 - T10 - T01 + T00}
 // as (re, im) pairs, so that T(r + a, t + b) = (v0 + a v1) + b (v2 + a v3).
 template <class T>

@@ -1287,6 +1287,35 @@ void launch_rotate_fields(int R, float c, float s, const cpx<T>* src, cpx<T>* ds
     rotate_fields_kernel<T><<<grid, 128, 0, st>>>(R, c, s, src, dst);
 }
 
+// Loads every kernel of this file (cudaFuncGetAttributes), see preload_kernels.
+template <class T>
+static void preload_nearfield_t() {
+    cudaFuncAttributes a;
+    cudaFuncGetAttributes(&a, uf_kernel<T>);
+    cudaFuncGetAttributes(&a, lut_build_kernel<T>);
+    cudaFuncGetAttributes(&a, phase_kernel<T>);
+    cudaFuncGetAttributes(&a, us_sh_kernel<T>);
+    cudaFuncGetAttributes(&a, sum_only_kernel<T>);
+    cudaFuncGetAttributes(&a, rotate_fields_kernel<T>);
+}
+void preload_nearfield_kernels() {
+    preload_nearfield_t<float>();
+    preload_nearfield_t<double>();
+    cudaFuncAttributes a;
+    cudaFuncGetAttributes(&a, uf_table_kernel);
+    cudaFuncGetAttributes(&a, mie_kernel);
+    cudaFuncGetAttributes(&a, coef_rows_batch_kernel);
+    cudaFuncGetAttributes(&a, legendre_table_kernel);
+    cudaFuncGetAttributes(&a, us_lut_f64_kernel);
+    cudaFuncGetAttributes(&a, us_lut_tex_kernel<false, 1>);
+    cudaFuncGetAttributes(&a, us_lut_tex_kernel<true, 1>);
+    cudaFuncGetAttributes(&a, us_lut_tex_kernel<true, 2>);
+    cudaFuncGetAttributes(&a, lut_build_tex_batch_kernel);
+    cudaFuncGetAttributes(&a, sh_recur_kernel);
+    cudaFuncGetAttributes(&a, sh_wave_kernel);
+    cudaFuncGetAttributes(&a, sh_coef_kernel);
+}
+
 #define BS_INST(T)                                                                                              \
     template void launch_rotate_fields<T>(int, float, float, const cpx<T>*, cpx<T>*, cudaStream_t);             \
     template void launch_uf<T>(const Scene&, const double*, const double*, cpx<T>*, cudaStream_t);              \
