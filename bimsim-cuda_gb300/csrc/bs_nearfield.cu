@@ -493,10 +493,42 @@ __device__ __forceinline__ f32x2 f2_fma(f32x2 a, f32x2 b, f32x2 c) {
     asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
     return r;
 }
+__device__ __forceinline__ f32x2 f2_pack(float a, float b) {
+    f32x2 r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ f32x2 f2_mul(f32x2 a, f32x2 b) {
+    f32x2 r;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
 __device__ __forceinline__ float2 f2_unpack(f32x2 v) {
     float2 r;
     asm("mov.b64 {%0, %1}, %2;" : "=f"(r.x), "=f"(r.y) : "l"(v));
     return r;
+}
+
+// theta_index of two pixels with the polynomial and the final products in packed
+// f32x2 instructions; every lane rounds as the scalar instruction, so t0, t1 are
+// theta_index(c0, ...), theta_index(c1, ...) bit for bit.
+__device__ __forceinline__ void theta_index2(float c0, float c1, float tsc, float tscpi, float& t0, float& t1) {
+    const float ax0 = fminf(fabsf(c0), 1.f), ax1 = fminf(fabsf(c1), 1.f);
+    float s0, s1;
+    asm("sqrt.approx.f32 %0, %1;" : "=f"(s0) : "f"(1.f - ax0));
+    asm("sqrt.approx.f32 %0, %1;" : "=f"(s1) : "f"(1.f - ax1));
+    const f32x2 ax = f2_pack(ax0, ax1);
+    f32x2 g = f2_splat(-1.411853940e-03f);
+    g = f2_fma(g, ax, f2_splat(7.149144541e-03f));
+    g = f2_fma(g, ax, f2_splat(-1.768672466e-02f));
+    g = f2_fma(g, ax, f2_splat(3.125903755e-02f));
+    g = f2_fma(g, ax, f2_splat(-5.028845742e-02f));
+    g = f2_fma(g, ax, f2_splat(8.899561316e-02f));
+    g = f2_fma(g, ax, f2_splat(-2.145996839e-01f));
+    g = f2_fma(g, ax, f2_splat(1.570796371e+00f));
+    const float2 v = f2_unpack(f2_mul(f2_mul(f2_pack(s0, s1), f2_splat(tsc)), g));
+    t0 = c0 < 0.f ? tscpi - v.x : v.x;
+    t1 = c1 < 0.f ? tscpi - v.y : v.y;
 }
 
 __device__ __forceinline__ void copy_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
@@ -764,10 +796,19 @@ __global__ void __launch_bounds__(UST_TILE / PPT, STAGE ? (PPT == 1 ? 3 : 4) : 6
                     const float4 kk = s_k[w];
                     const float2 pw = s_p[w];
                     const f32x2 pwx = f2_splat(pw.x), pwy = f2_splat(pw.y);
+                    float tt[PPT];
+                    if (PPT == 2) {
+                        theta_index2(fmaf(kk.x, rx[0], fmaf(kk.y, ry[0], kk.z * rz[0])),
+                                     fmaf(kk.x, rx[PPT - 1], fmaf(kk.y, ry[PPT - 1], kk.z * rz[PPT - 1])), tsc,
+                                     tscpi, tt[0], tt[PPT - 1]);
+                    } else {
+#pragma unroll
+                        for (int j = 0; j < PPT; j++)  // cb = 0: every d > 0 here
+                            tt[j] = theta_index(fmaf(kk.x, rx[j], fmaf(kk.y, ry[j], kk.z * rz[j])), tsc, tscpi);
+                    }
 #pragma unroll
                     for (int j = 0; j < PPT; j++) {
-                        const float c = fmaf(kk.x, rx[j], fmaf(kk.y, ry[j], kk.z * rz[j]));  // cb = 0: every d > 0 here
-                        const float t = theta_index(c, tsc, tscpi);
+                        const float t = tt[j];
                         const float tf = floorf(t);
                         const float be = t - tf;
                         // in the window by construction; the unsigned clamp only keeps a bad bound in bounds
