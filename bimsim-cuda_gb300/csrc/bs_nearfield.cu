@@ -789,38 +789,56 @@ __global__ void __launch_bounds__(UST_TILE / PPT, STAGE ? (PPT == 1 ? 3 : 4) : 6
                     alp[j] = f2_splat(al[j]);
                     ax[j] = ay[j] = 0ull;
                 }
+                // one lookup of pixel j at angle index t, wave weight (pwx, pwy)
+                auto lookup = [&](int j, float t, f32x2 pwx, f32x2 pwy) {
+                    const float tf = floorf(t);
+                    const float be = t - tf;
+                    // in the window by construction; the unsigned clamp only keeps a bad bound in bounds
+                    const unsigned lt = min((unsigned)((int)tf - t_lo), lt_max);
+                    const f32x2* q = reinterpret_cast<const f32x2*>(row0[j] + lt);
+                    const f32x2 e00 = q[0], e01 = q[1], e10 = q[drow[j]], e11 = q[drow[j] + 1];
+                    const f32x2 bep = f2_splat(be);
+                    const f32x2 a0 = f2_fma(bep, f2_sub(e01, e00), e00);
+                    const f32x2 a1 = f2_fma(bep, f2_sub(e11, e10), e10);
+                    const f32x2 v = f2_fma(alp[j], f2_sub(a1, a0), a0);
+                    ax[j] = f2_fma(pwx, v, ax[j]);
+                    ay[j] = f2_fma(pwy, v, ay[j]);
+                };
+                // cb = 0 here: every d > 0.  The angle indices of two lookups at a time (the thread's
+                // two pixels, or one pixel's two consecutive waves) in packed instructions; the lookups
+                // and their sums run in wave order, so the bits are those of one at a time.
                 // 32 lookups per thread per unrolled step (config 2: 697 ms; 8: 721 ms, 16: 700 ms,
                 // 64: 792 ms)
-#pragma unroll(32 / PPT)
-                for (int w = 0; w < nw; w++) {
-                    const float4 kk = s_k[w];
-                    const float2 pw = s_p[w];
-                    const f32x2 pwx = f2_splat(pw.x), pwy = f2_splat(pw.y);
-                    float tt[PPT];
-                    if (PPT == 2) {
+                if (PPT == 2) {
+#pragma unroll 16
+                    for (int w = 0; w < nw; w++) {
+                        const float4 kk = s_k[w];
+                        const float2 pw = s_p[w];
+                        const f32x2 pwx = f2_splat(pw.x), pwy = f2_splat(pw.y);
+                        float t0, t1;
                         theta_index2(fmaf(kk.x, rx[0], fmaf(kk.y, ry[0], kk.z * rz[0])),
                                      fmaf(kk.x, rx[PPT - 1], fmaf(kk.y, ry[PPT - 1], kk.z * rz[PPT - 1])), tsc,
-                                     tscpi, tt[0], tt[PPT - 1]);
-                    } else {
-#pragma unroll
-                        for (int j = 0; j < PPT; j++)  // cb = 0: every d > 0 here
-                            tt[j] = theta_index(fmaf(kk.x, rx[j], fmaf(kk.y, ry[j], kk.z * rz[j])), tsc, tscpi);
+                                     tscpi, t0, t1);
+                        lookup(0, t0, pwx, pwy);
+                        lookup(PPT - 1, t1, pwx, pwy);
                     }
-#pragma unroll
-                    for (int j = 0; j < PPT; j++) {
-                        const float t = tt[j];
-                        const float tf = floorf(t);
-                        const float be = t - tf;
-                        // in the window by construction; the unsigned clamp only keeps a bad bound in bounds
-                        const unsigned lt = min((unsigned)((int)tf - t_lo), lt_max);
-                        const f32x2* q = reinterpret_cast<const f32x2*>(row0[j] + lt);
-                        const f32x2 e00 = q[0], e01 = q[1], e10 = q[drow[j]], e11 = q[drow[j] + 1];
-                        const f32x2 bep = f2_splat(be);
-                        const f32x2 a0 = f2_fma(bep, f2_sub(e01, e00), e00);
-                        const f32x2 a1 = f2_fma(bep, f2_sub(e11, e10), e10);
-                        const f32x2 v = f2_fma(alp[j], f2_sub(a1, a0), a0);
-                        ax[j] = f2_fma(pwx, v, ax[j]);
-                        ay[j] = f2_fma(pwy, v, ay[j]);
+                } else {
+                    int w = 0;
+#pragma unroll 16
+                    for (; w + 1 < nw; w += 2) {
+                        const float4 k0 = s_k[w], k1 = s_k[w + 1];
+                        const float2 p0 = s_p[w], p1 = s_p[w + 1];
+                        float t0, t1;
+                        theta_index2(fmaf(k0.x, rx[0], fmaf(k0.y, ry[0], k0.z * rz[0])),
+                                     fmaf(k1.x, rx[0], fmaf(k1.y, ry[0], k1.z * rz[0])), tsc, tscpi, t0, t1);
+                        lookup(0, t0, f2_splat(p0.x), f2_splat(p0.y));
+                        lookup(0, t1, f2_splat(p1.x), f2_splat(p1.y));
+                    }
+                    if (w < nw) {
+                        const float4 kk = s_k[w];
+                        const float2 pw = s_p[w];
+                        lookup(0, theta_index(fmaf(kk.x, rx[0], fmaf(kk.y, ry[0], kk.z * rz[0])), tsc, tscpi),
+                               f2_splat(pw.x), f2_splat(pw.y));
                     }
                 }
 #pragma unroll
