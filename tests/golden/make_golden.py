@@ -37,7 +37,7 @@ def cplx_list(v):
     return [[float(v[2 * i]), float(v[2 * i + 1])] for i in range(len(v) // 2)]
 
 
-def main():
+def main(out_dir=HERE):
     if not os.path.exists(LIB):
         sys.exit("build oracle/_ref first: make -C oracle ref")
     r = C.CDLL(LIB)
@@ -196,10 +196,10 @@ def main():
     out["material_kk"] = kks
 
     for key, val in out.items():
-        with open(os.path.join(HERE, key + ".json"), "w") as fh:
+        with open(os.path.join(out_dir, key + ".json"), "w") as fh:
             json.dump(val, fh, separators=(",", ":"))
     print("wrote", ", ".join(sorted(out)))
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1] if len(sys.argv) > 1 else HERE)

@@ -174,7 +174,7 @@ def quiet():
             os.close(fd)
 
 
-def main():
+def main(out_dir=HERE):
     libs = {}
     for b in ("f32", "f64"):
         path = os.path.join(REPO, "oracle", "_ref", f"libref_sim_{b}.so")
@@ -271,9 +271,9 @@ def main():
                                                                    if "{dir}/" + f in flags},
                      "spheres": [{"in": get(f"sphere{s}.in").tolist()} for s in range(int(dims[4]))]}
         print(name, "parsed: R =", int(dims[0]), "spheres =", int(dims[4]))
-    with open(os.path.join(HERE, "ref_sim.json"), "w") as fh:
+    with open(os.path.join(out_dir, "ref_sim.json"), "w") as fh:
         json.dump(out, fh, separators=(",", ":"))
-    print("wrote ref_sim.json", os.path.getsize(os.path.join(HERE, "ref_sim.json")), "bytes")
+    print("wrote ref_sim.json", os.path.getsize(os.path.join(out_dir, "ref_sim.json")), "bytes")
 
     # the reference's executable end to end (ref_sim_save: main.cpp's steps, then fileoutStruct::Save): the
     # ENVI files and the absorbance-spectrum text it writes, one run per entry of "runs" in the same
@@ -299,7 +299,7 @@ def main():
                                "data": base64.b64encode(open(os.path.join(d, f), "rb").read()).decode()}
         rec["as.txt"] = open(os.path.join(d, "as.txt")).read()
         files[name] = rec
-    with open(os.path.join(HERE, "ref_cli_files.json"), "w") as fh:
+    with open(os.path.join(out_dir, "ref_cli_files.json"), "w") as fh:
         json.dump(files, fh, separators=(",", ":"))
     print("wrote ref_cli_files.json")
 
@@ -315,10 +315,10 @@ def main():
         rgb = np.zeros(3 * vals.size, np.uint8)
         lib.ref_colormap(vals.ctypes.data_as(C.c_void_p), vals.size, 0.0, 3.5, cm, rgb.ctypes.data_as(C.c_void_p))
         cmap[name] = rgb.tobytes().hex()
-    with open(os.path.join(HERE, "ref_colormap.json"), "w") as fh:
+    with open(os.path.join(out_dir, "ref_colormap.json"), "w") as fh:
         json.dump(cmap, fh, separators=(",", ":"))
     print("wrote ref_colormap.json")
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1] if len(sys.argv) > 1 else HERE)
