@@ -134,7 +134,10 @@ const char* bs_last_error(void);
 
 /* Allocate a context on the current CUDA device (microscopeStruct::init,
  * microscope.cu:537; nearfieldStruct::init, nearfield.cpp:25).  The context
- * owns all device memory and one CUDA stream. */
+ * owns all device memory and one CUDA stream.  The first context of a device
+ * in a process loads every kernel of the library there: CUDA otherwise loads
+ * a kernel at its first launch, and such a load waits for the kernels that
+ * other streams are running. */
 bs_status bs_create(const bs_params* params, bs_ctx** out);
 
 /* Free everything the context holds (microscopeStruct::destroy). */
